@@ -1,0 +1,183 @@
+"""First Brillouin zone, irreducible wedge and irreducible polyhedron.
+
+Set-up code (host, numpy/scipy).  The reference constructs the same objects in
+``src/bz.cpp`` (Voronoi cutting) and ``src/bz_wedge.cpp`` (wedge search); both
+are one-time set-up and outside the GPU query path.  What the query path
+consumes from here is flat:
+
+* per first-zone face: three points on the face, its unit outward normal, the
+  primitive reciprocal-lattice vector τ whose bisector it is, and |τ|
+  (reference ``BrillouinZone::moveinto``, ``src/bz_move.cpp:123-141``);
+* the irreducible-wedge normals (``BrillouinZone::_inside_wedge_outer``,
+  ``src/bz.hpp:757-763``);
+* the point-group matrices with their inverse and identity indices.
+
+Construction here is this package's own: the zone is the Voronoi cell of the
+primitive reciprocal lattice (scipy's Qhull half-space intersection), and the
+wedge is the Dirichlet domain of one generic point under the reciprocal-space
+point group, a fundamental domain for any finite orthogonal group.  It is a
+different construction from the reference's, so the wedge it chooses may
+differ; the query path only requires that it be a fundamental domain.
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+from scipy.spatial import HalfspaceIntersection
+
+from .crystal import Lattice, PointSymmetry
+
+
+def _unique_rows(x, tol):
+    out = []
+    for p in x:
+        if not any(np.linalg.norm(p - q) < tol for q in out):
+            out.append(p)
+    return np.array(out)
+
+
+def _polytope(halfspaces, interior):
+    """Vertices and per-halfspace vertex lists of {x : A x + b <= 0}."""
+    hs = HalfspaceIntersection(halfspaces, interior)
+    scale = np.max(np.abs(hs.intersections)) if len(hs.intersections) else 1.0
+    verts = _unique_rows(hs.intersections, 1e-9 * max(scale, 1.0))
+    faces = []
+    A, b = halfspaces[:, :3], halfspaces[:, 3]
+    nrm = np.linalg.norm(A, axis=1)
+    for i in range(len(halfspaces)):
+        d = (verts @ A[i] + b[i]) / nrm[i]
+        on = np.nonzero(np.abs(d) < 1e-9 * max(scale, 1.0))[0]
+        faces.append(on)
+    return verts, faces
+
+
+def _ccw(verts, idx, normal):
+    """Order face vertex indices counter-clockwise seen from outside."""
+    p = verts[idx]
+    c = p.mean(axis=0)
+    u = p[0] - c
+    u /= np.linalg.norm(u)
+    v = np.cross(normal, u)
+    ang = np.arctan2((p - c) @ v, (p - c) @ u)
+    return np.asarray(idx)[np.argsort(ang)]
+
+
+def orient3d(a, b, c, d):
+    """(a-d)·((b-d)×(c-d)) — the reference's pseudo_orient3d
+    (``src/geometry.hpp:118-139``)."""
+    return np.dot(a - d, np.cross(b - d, c - d))
+
+
+def _plane_triple(verts, ring):
+    """Three vertices of a face ring spanning the largest triangle."""
+    best, trip = -1.0, None
+    n = len(ring)
+    for j in range(1, n - 1):
+        for k in range(j + 1, n):
+            area = np.linalg.norm(np.cross(verts[ring[j]] - verts[ring[0]], verts[ring[k]] - verts[ring[0]]))
+            if area > best:
+                best, trip = area, (ring[0], ring[j], ring[k])
+    return trip
+
+
+class BrillouinZone:
+    """First Brillouin zone and irreducible polyhedron of a lattice.
+
+    Mirrors the reference's ``BrillouinZone(lattice, time_reversal=False,
+    wedge_search=True)`` surface (``wrap/_bz.cpp:156-177``).
+    """
+
+    def __init__(self, lattice: Lattice, time_reversal=False, wedge_search=True,
+                 extent=2):
+        self.lattice = lattice
+        self.time_reversal = bool(time_reversal)
+        self.wedge_search = bool(wedge_search)
+        self.Bp = lattice.primitive_B()
+        self._first_zone(extent)
+        pg = lattice.pointgroup
+        if self.time_reversal:
+            pg = pg.add_space_inversion()
+        self.pointgroup: PointSymmetry = pg
+        self._wedge()
+
+    # ---------------------------------------------------------------- zone
+    def _first_zone(self, extent):
+        ns = np.array([n for n in itertools.product(range(-extent, extent + 1), repeat=3) if any(n)])
+        G = ns @ self.Bp
+        hs = np.hstack([G, -0.5 * np.sum(G * G, axis=1)[:, None]])
+        verts, faces = _polytope(hs, np.zeros(3))
+        keep = [i for i, f in enumerate(faces) if len(f) >= 3]
+        self.vertices = verts
+        self.face_tau = ns[keep].astype(np.int32)
+        Gk = G[keep]
+        self.face_tau_len = np.linalg.norm(Gk, axis=1)
+        self.face_normal = Gk / self.face_tau_len[:, None]
+        rings, abc = [], []
+        for i, fi in zip(keep, range(len(keep))):
+            ring = _ccw(verts, faces[i], self.face_normal[fi])
+            rings.append(ring)
+            a, b, c = _plane_triple(verts, ring)
+            pa, pb, pc = verts[a], verts[b], verts[c]
+            if orient3d(pa, pb, pc, np.zeros(3)) < 0:
+                pb, pc = pc, pb
+            abc.append(np.concatenate([pa, pb, pc]))
+        self.face_rings = rings
+        self.face_abc = np.array(abc)
+        self.halfspaces = hs[keep]
+        self.volume = abs(np.linalg.det(self.Bp))
+
+    # --------------------------------------------------------------- wedge
+    def _cartesian_ops(self):
+        """Reciprocal-space Cartesian action of each point operation:
+        q_xyz -> S q_xyz with S = Bᵀ Wᵀ B⁻ᵀ (q_hkl -> Wᵀ q_hkl)."""
+        B = self.lattice.B
+        Binv_T = np.linalg.inv(B.T)
+        return np.array([B.T @ W.T @ Binv_T for W in self.pointgroup.W])
+
+    def _wedge(self):
+        S = self._cartesian_ops()
+        inr = np.min(self.face_tau_len) / 2
+        normals = []
+        if self.wedge_search and self.pointgroup.size > 1:
+            p0 = np.array([0.9, 0.2, 0.1]) + np.array([1.3e-3, 2.9e-3, 0.7e-3])
+            p0 = 0.25 * inr * p0 / np.linalg.norm(p0)
+            cand = []
+            for s in S:
+                n = p0 - s @ p0
+                if np.linalg.norm(n) > 1e-9 * inr:
+                    cand.append(n / np.linalg.norm(n))
+            cand = _unique_rows(np.array(cand), 1e-9)
+            hs = np.vstack([self.halfspaces, np.hstack([-cand, np.zeros((len(cand), 1))])])
+            verts, faces = _polytope(hs, p0)
+            nz = len(self.halfspaces)
+            for k in range(len(cand)):
+                if len(faces[nz + k]) >= 3:
+                    normals.append(cand[k])
+        self.wedge_normal = np.array(normals).reshape(-1, 3)
+        # the irreducible polyhedron: zone ∩ wedge
+        hs = np.vstack([self.halfspaces, np.hstack([-self.wedge_normal, np.zeros((len(self.wedge_normal), 1))])])
+        if len(self.wedge_normal):
+            interior = p0
+        else:
+            interior = np.zeros(3)
+        verts, faces = _polytope(hs, interior)
+        self.ir_vertices = verts
+        self.ir_halfspaces = hs
+        self.ir_faces = [f for f in faces if len(f) >= 3]
+
+    # ------------------------------------------------------------- helpers
+    def isinside(self, q_hkl):
+        """Inside the first zone (tolerant orient3d test, outer lattice)."""
+        x = np.atleast_2d(q_hkl) @ self.lattice.B
+        a, b, c = self.face_abc[:, 0:3], self.face_abc[:, 3:6], self.face_abc[:, 6:9]
+        out = []
+        for p in x:
+            o = np.einsum("ij,ij->i", a - p, np.cross(b - p, c - p))
+            out.append(o.min() > -1e-12)
+        return np.array(out)
+
+    @property
+    def ir_volume(self):
+        from scipy.spatial import ConvexHull
+        return ConvexHull(self.ir_vertices).volume

@@ -1,0 +1,289 @@
+"""Hybrid cube / tetrahedron trellis over the irreducible polyhedron.
+
+Set-up code (host).  The reference builds its ``PolyTrellis`` in
+``src/trellis_poly_parallel.tpp:74-482`` with TetGen for the cut cells; that
+construction is outside the GPU query path.  This module builds a trellis with
+the same structure and the same node semantics from scipy's Qhull:
+
+* knots along x, y, z from the polyhedron's bounding box with spacing
+  ``L / ceil(L / cbrt(max_volume))``, appended until the last knot reaches the
+  maximum (reference ``trellis_poly_parallel.tpp:88-101``);
+* a cell wholly inside the polyhedron is a cube node whose eight vertex
+  indices are ordered (000)(100)(110)(010)(101)(001)(011)(111), so entries i
+  and 7-i are body-diagonal partners (``src/trellis_node.hpp:127-131``);
+* a cell cut by the polyhedron surface is a poly node: the convex cut cell is
+  tetrahedralised (Delaunay), each tetrahedron stored with its four vertex
+  indices (positively oriented), circumsphere and volume
+  (``src/trellis_node.hpp:216-364``);
+* any other cell is a null node.
+
+Node linear index is ``i + nx*(j + ny*k)`` (``trellis_poly.hpp:557-562``).
+"""
+from __future__ import annotations
+
+import numpy as np
+from scipy.spatial import Delaunay, cKDTree
+
+NODE_NULL, NODE_CUBE, NODE_POLY = 0, 1, 2
+
+# corner order of a cube node: (000)(100)(110)(010)(101)(001)(011)(111)
+CUBE_CORNERS = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                         [1, 0, 1], [0, 0, 1], [0, 1, 1], [1, 1, 1]])
+_BOX_EDGES = [(0, 1), (1, 2), (2, 3), (3, 0), (5, 4), (4, 7), (7, 6), (6, 5),
+              (0, 5), (1, 4), (2, 7), (3, 6)]
+
+
+def make_knots(vmin, vmax, max_volume):
+    lengths = vmax - vmin
+    step = lengths / np.ceil(lengths / np.cbrt(max_volume))
+    knots = []
+    for i in range(3):
+        k = [vmin[i]]
+        while k[-1] < vmax[i]:
+            k.append(k[-1] + step[i])
+        knots.append(np.array(k))
+    return knots
+
+
+def _poly_edges(verts, halfspaces, tol):
+    A, b = halfspaces[:, :3], halfspaces[:, 3]
+    nrm = np.linalg.norm(A, axis=1)
+    on = np.abs((verts @ A.T + b) / nrm) < tol  # (nv, nh)
+    edges = []
+    for i in range(len(verts)):
+        for j in range(i + 1, len(verts)):
+            if np.count_nonzero(on[i] & on[j]) >= 2:
+                edges.append((i, j))
+    return np.array(edges, dtype=int).reshape(-1, 2)
+
+
+def circumsphere(p):
+    """Centre and radius of the sphere through four points (4, 3)."""
+    a = p[1:] - p[0]
+    rhs = 0.5 * np.sum(a * a, axis=1)
+    c = np.linalg.solve(a, rhs)
+    return p[0] + c, np.linalg.norm(c)
+
+
+def _orient(p0, p1, p2, p3):
+    return np.dot(p0 - p3, np.cross(p1 - p3, p2 - p3))
+
+
+class TrellisBuild:
+    """Flat trellis tables (numpy) ready for the query-path C ABI."""
+
+    def __init__(self, ir_vertices, ir_halfspaces, max_volume, always_triangulate=False):
+        verts = np.asarray(ir_vertices, float)
+        hs = np.asarray(ir_halfspaces, float)
+        scale = float(np.max(np.abs(verts)))
+        tol = 1e-10 * max(scale, 1e-30)
+        self.knots = make_knots(verts.min(axis=0), verts.max(axis=0), float(max_volume))
+        kx, ky, kz = self.knots
+        nx, ny, nz = len(kx) - 1, len(ky) - 1, len(kz) - 1
+        A, b = hs[:, :3], hs[:, 3]
+        nrm = np.linalg.norm(A, axis=1)
+        An, bn = A / nrm[:, None], b / nrm
+        pedges = _poly_edges(verts, hs, tol)
+
+        # signed distances of every knot-grid point to every polyhedron plane
+        gx, gy, gz = np.meshgrid(kx, ky, kz, indexing="ij")
+        grid = np.stack([gx, gy, gz], axis=-1)           # (nx+1, ny+1, nz+1, 3)
+        dist = grid @ An.T + bn                           # (..., nh)
+        inside = np.all(dist <= tol, axis=-1)
+
+        node_type = np.zeros(nx * ny * nz, np.int32)
+        node_index = np.full(nx * ny * nz, -1, np.int32)
+        cube_pts, poly_cells = [], []
+        pts = []  # all vertex candidates (Cartesian)
+
+        def idx3(i, j, k):
+            return i + nx * (j + ny * k)
+
+        for k in range(nz):
+            for j in range(ny):
+                for i in range(nx):
+                    cin = np.array([inside[i + c[0], j + c[1], k + c[2]] for c in CUBE_CORNERS])
+                    cd = np.array([dist[i + c[0], j + c[1], k + c[2]] for c in CUBE_CORNERS])
+                    if np.any(np.all(cd > tol, axis=0)):
+                        continue  # entirely outside one plane: null
+                    if cin.all() and not always_triangulate:
+                        node_type[idx3(i, j, k)] = NODE_CUBE
+                        node_index[idx3(i, j, k)] = len(cube_pts)
+                        cube_pts.append([(i + c[0], j + c[1], k + c[2]) for c in CUBE_CORNERS])
+                        continue
+                    lo = np.array([kx[i], ky[j], kz[k]])
+                    hi = np.array([kx[i + 1], ky[j + 1], kz[k + 1]])
+                    cand = self._cut_cell(lo, hi, verts, pedges, An, bn, tol)
+                    if cand is None:
+                        continue
+                    poly_cells.append((idx3(i, j, k), cand))
+
+        # global vertex list: knot points used by cube nodes first, then the
+        # points of the cut cells, merged within tolerance
+        grid_flat = grid.reshape(-1, 3)
+        used = sorted({(a, b_, c) for cell in cube_pts for (a, b_, c) in cell})
+        lin = {g: n for n, g in enumerate(used)}
+        all_pts = [grid_flat[(a * (ny + 1) + b_) * (nz + 1) + c] for (a, b_, c) in used]
+        offsets = []
+        for _, cand in poly_cells:
+            offsets.append(len(all_pts))
+            all_pts.extend(cand)
+        all_pts = np.array(all_pts).reshape(-1, 3)
+        uniq_map = self._merge(all_pts, tol)
+        keep, inv = np.unique(uniq_map, return_inverse=True)
+        self.vertices = all_pts[keep]
+        self.cube_vertices = np.array(
+            [[inv[lin[p]] for p in cell] for cell in cube_pts], dtype=np.int32).reshape(-1, 8)
+        tets, spheres, vols, tet_off = [], [], [], [0]
+        poly_node_ids = []
+        for (lin_idx, cand), off in zip(poly_cells, offsets):
+            gid = inv[np.arange(off, off + len(cand))]
+            p = self.vertices[gid]
+            local = self._tetrahedralise(p, tol)
+            if not local:
+                continue
+            poly_node_ids.append(lin_idx)
+            for t in local:
+                q = p[list(t)]
+                o = _orient(q[0], q[1], q[2], q[3])
+                if o < 0:
+                    t = (t[0], t[2], t[1], t[3])
+                    q = p[list(t)]
+                c, r = circumsphere(q)
+                tets.append([gid[t[0]], gid[t[1]], gid[t[2]], gid[t[3]]])
+                spheres.append([c[0], c[1], c[2], r])
+                vols.append(abs(o) / 6.0)
+            tet_off.append(len(tets))
+        for n, lin_idx in enumerate(poly_node_ids):
+            node_type[lin_idx] = NODE_POLY
+            node_index[lin_idx] = n
+        self.node_type = node_type
+        self.node_index = node_index
+        self.poly_tet_offset = np.array(tet_off, dtype=np.int32)
+        self.tet_vertices = np.array(tets, dtype=np.int32).reshape(-1, 4)
+        self.tet_sphere = np.array(spheres, dtype=float).reshape(-1, 4)
+        self.tet_volume = np.array(vols, dtype=float)
+        self.shape = (nx, ny, nz)
+
+    @staticmethod
+    def _merge(points, tol):
+        tree = cKDTree(points)
+        pairs = tree.query_pairs(r=tol, output_type="ndarray")
+        parent = np.arange(len(points))
+
+        def find(a):
+            while parent[a] != a:
+                parent[a] = parent[parent[a]]
+                a = parent[a]
+            return a
+
+        for a, b in pairs:
+            ra, rb = find(a), find(b)
+            if ra != rb:
+                parent[max(ra, rb)] = min(ra, rb)
+        return np.array([find(a) for a in range(len(points))])
+
+    @staticmethod
+    def _cut_cell(lo, hi, verts, pedges, An, bn, tol):
+        corners = lo + CUBE_CORNERS * (hi - lo)
+        pts = []
+        # box corners inside the polyhedron
+        d = corners @ An.T + bn
+        pts.extend(corners[np.all(d <= tol, axis=1)])
+        # polyhedron vertices inside the box
+        inbox = np.all((verts >= lo - tol) & (verts <= hi + tol), axis=1)
+        pts.extend(verts[inbox])
+        # box edges crossing polyhedron planes
+        for a, b in _BOX_EDGES:
+            pa, pb = corners[a], corners[b]
+            da, db = d[a], d[b]
+            for h in range(len(bn)):
+                if (da[h] < -tol and db[h] > tol) or (da[h] > tol and db[h] < -tol):
+                    t = da[h] / (da[h] - db[h])
+                    x = pa + t * (pb - pa)
+                    if np.all(x @ An.T + bn <= tol):
+                        pts.append(x)
+        # polyhedron edges crossing box faces
+        for a, b in pedges:
+            pa, pb = verts[a], verts[b]
+            for ax in range(3):
+                for plane in (lo[ax], hi[ax]):
+                    ua, ub = pa[ax] - plane, pb[ax] - plane
+                    if (ua < -tol and ub > tol) or (ua > tol and ub < -tol):
+                        t = ua / (ua - ub)
+                        x = pa + t * (pb - pa)
+                        x[ax] = plane
+                        if np.all((x >= lo - tol) & (x <= hi + tol)):
+                            pts.append(x)
+        if len(pts) < 4:
+            return None
+        pts = np.array(pts)
+        keep = []
+        for p in pts:
+            if not any(np.linalg.norm(p - q) < tol for q in keep):
+                keep.append(p)
+        pts = np.clip(np.array(keep), lo, hi)
+        if len(pts) < 4:
+            return None
+        c = pts - pts.mean(axis=0)
+        if np.linalg.matrix_rank(c, tol=1e-9 * np.max(hi - lo)) < 3:
+            return None
+        return pts
+
+    @staticmethod
+    def _tetrahedralise(p, tol):
+        try:
+            tri = Delaunay(p, qhull_options="Qbb Qc Qz Q12 Qt")
+        except Exception:
+            return []
+        out = []
+        span = np.max(np.ptp(p, axis=0))
+        for s in tri.simplices:
+            q = p[s]
+            if abs(_orient(q[0], q[1], q[2], q[3])) > 1e-12 * span ** 3:
+                out.append(tuple(int(x) for x in s))
+        return out
+
+    @property
+    def n_nodes(self):
+        return self.node_type.size
+
+    def summary(self):
+        return dict(vertices=len(self.vertices), cube=int(np.sum(self.node_type == NODE_CUBE)),
+                    poly=int(np.sum(self.node_type == NODE_POLY)), tets=len(self.tet_vertices),
+                    nodes=self.n_nodes, shape=self.shape)
+
+
+class PointTrellis(TrellisBuild):
+    """A one-node trellis whose vertices are exactly the given points.
+
+    The single poly node holds the Delaunay tetrahedralisation of the points'
+    convex hull.  It is used to re-create a grid from vertex positions alone,
+    for example the reference's stored grid in its Γ-rotation fixture.
+    """
+
+    def __init__(self, points_xyz):  # noqa: D401 - deliberately skips TrellisBuild.__init__
+        p = np.asarray(points_xyz, float)
+        lo, hi = p.min(axis=0), p.max(axis=0)
+        pad = 1e-9 * max(float(np.max(hi - lo)), 1.0)
+        self.knots = [np.array([lo[d] - pad, hi[d] + pad]) for d in range(3)]
+        self.vertices = p.copy()
+        self.cube_vertices = np.zeros((0, 8), np.int32)
+        tets, spheres, vols = [], [], []
+        for t in self._tetrahedralise(p, 1e-12):
+            q = p[list(t)]
+            o = _orient(q[0], q[1], q[2], q[3])
+            if o < 0:
+                t = (t[0], t[2], t[1], t[3])
+                q = p[list(t)]
+            c, r = circumsphere(q)
+            tets.append(list(t))
+            spheres.append([c[0], c[1], c[2], r])
+            vols.append(abs(o) / 6.0)
+        self.node_type = np.array([NODE_POLY], np.int32)
+        self.node_index = np.array([0], np.int32)
+        self.poly_tet_offset = np.array([0, len(tets)], np.int32)
+        self.tet_vertices = np.array(tets, np.int32)
+        self.tet_sphere = np.array(spheres)
+        self.tet_volume = np.array(vols)
+        self.shape = (1, 1, 1)

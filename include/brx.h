@@ -1,0 +1,207 @@
+/*
+ * brx.h — C ABI of the GB300 query path for brille's BrillouinZoneTrellis3.
+ *
+ * The reference answers `ir_interpolate_at` / `interpolate_at` on the host
+ * (src/bz_trellis.hpp:113-196).  This ABI takes the same question to one
+ * GB300: a caller that already holds a constructed Brillouin zone and trellis
+ * flattens them into a brx_geometry (plain pointers and sizes), uploads it
+ * once with brx_create, fills vertex data with brx_fill and then asks for
+ * interpolated values and vectors at any number of Q points.
+ *
+ * Every function returns a brx_status; none throws and none takes a torch or
+ * C++ type.  Pointers to Q and to outputs may be host or device memory: host
+ * buffers are staged through pinned memory in chunks on the handle's streams,
+ * device buffers are used in place.  The status enum mirrors the reference's
+ * error messages (src/bz_trellis.hpp:165-169, src/bz_move.cpp:158,288-294,
+ * src/trellis_poly.hpp:345-350, src/trellis_node.hpp:593-610,
+ * src/interpolator.hpp:400-426); brx_last_error returns the message text.
+ */
+#ifndef BRX_H
+#define BRX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BRX_ABI_VERSION 1
+
+typedef enum brx_status {
+  BRX_OK = 0,
+  BRX_ERR_INVALID_ARGUMENT = 1,
+  BRX_ERR_CUDA = 2,
+  BRX_ERR_NOT_FILLED = 3,        /* "The interpolation data must be filled before interpolating." */
+  BRX_ERR_MOVE_FAILED = 4,       /* "Not all points inside Brillouin zone" (bz_move.cpp:149-159) */
+  BRX_ERR_OUTSIDE_IR = 5,        /* "Q = ... is outside of the irreducible BrillouinZone" (bz_move.cpp:288-294) */
+  BRX_ERR_NOT_FOUND = 6,         /* "interpolate_at failed to find N points" (trellis_poly.hpp:345-350) */
+  BRX_ERR_NULL_NODE = 7,         /* "Attempting to access null node at index" (trellis_node.hpp:593-610) */
+  BRX_ERR_UNSUPPORTED = 8,       /* "LengthUnit, RotatesLike combination not implemented" (interpolator.hpp:400-426) */
+  BRX_ERR_IMPOSSIBLE = 9,        /* "This shouldn't be possible" (trellis_node.hpp:298-300) */
+  BRX_ERR_OUT_OF_MEMORY = 10,
+  BRX_ERR_TIMEOUT = 11           /* a bounded device-side wait ran out */
+} brx_status;
+
+/* Node types of the trellis, reference NodeType (src/enums.hpp:73). */
+enum { BRX_NODE_NULL = 0, BRX_NODE_CUBE = 1, BRX_NODE_POLY = 2 };
+
+/* RotatesLike and LengthUnit codes as the reference's fill() decodes them
+ * (wrap/_interpolator.hpp:28-45). */
+enum { BRX_ROT_VECTOR = 0, BRX_ROT_PSEUDOVECTOR = 1, BRX_ROT_GAMMA = 2 };
+enum { BRX_LU_NONE = 0, BRX_LU_ANGSTROM = 1, BRX_LU_INVERSE_ANGSTROM = 2,
+       BRX_LU_REAL_LATTICE = 3, BRX_LU_RECIPROCAL_LATTICE = 4 };
+
+/* Element types. */
+enum { BRX_F64 = 0, BRX_C128 = 1, BRX_F32 = 2, BRX_C64 = 3, BRX_BF16 = 4 };
+
+/* Storage precision of vertex data on the device (brx_fill). */
+enum { BRX_STORE_F64 = 0,  /* as given: float64 / complex128, FP64 arithmetic */
+       BRX_STORE_F32 = 1,  /* float32 / complex64, FP32 arithmetic           */
+       BRX_STORE_BF16 = 2  /* bfloat16 (pairs for complex), FP32 arithmetic  */ };
+
+/* Query flags (brx_ir_interpolate_at / brx_interpolate_at). */
+#define BRX_FLAG_NO_MOVE   0x1u  /* do_not_move_points: Q already irreducible / in the first zone */
+#define BRX_FLAG_OUT_F32   0x2u  /* write float32 / complex64 outputs instead of the input dtype  */
+#define BRX_FLAG_ASYNC     0x4u  /* device I/O only: return without synchronising; errors are read
+                                    later with brx_sync */
+
+/*
+ * Everything the query path reads, flattened.  All arrays are row-major and
+ * are copied to the device by brx_create; the caller keeps ownership.
+ * Coordinates are Cartesian 1/Å unless stated.
+ */
+typedef struct brx_geometry {
+  /* -- lattices: the reference's BrillouinZone::_outer and _inner -- */
+  double outer_B[9];          /* rows b1,b2,b3 of the (conventional) reciprocal basis: xyz = hkl · B */
+  double prim_B[9];           /* rows of the primitive reciprocal basis */
+  int32_t to_prim_6Pt[9];     /* primitive hkl = (6Pᵀ · hkl) / 6   (src/transform.hpp:168-191) */
+  int32_t from_prim_invPt[9]; /* conventional hkl = (P⁻¹)ᵀ · primitive hkl (src/transform.hpp:212-221) */
+  int32_t is_primitive;       /* 1: conventional == primitive, no transform (PrimitiveTransform::does_nothing) */
+
+  /* -- first Brillouin zone, one entry per face (BrillouinZone::moveinto, src/bz_move.cpp:123-141) -- */
+  int32_t n_faces;
+  const double* face_abc;     /* n_faces × 9: points a, b, c on the face; orient3d(a,b,c,0) > 0 */
+  const double* face_normal;  /* n_faces × 3: unit outward normal */
+  const int32_t* face_tau;    /* n_faces × 3: primitive-lattice τ whose bisector the face is */
+  const double* face_tau_len; /* n_faces: |τ| */
+
+  /* -- irreducible wedge (BrillouinZone::_inside_wedge_outer, src/bz.hpp:757-763) -- */
+  int32_t n_wedge;
+  const double* wedge_normal; /* n_wedge × 3 */
+  int32_t wedge_le_ge;        /* 0: inside when every n·q ≥ 0; 1: when every n·q ≥ 0 or every n·q ≤ 0 */
+
+  /* -- point group (BrillouinZone::get_pointgroup_symmetry, src/bz.hpp:743-746) -- */
+  int32_t n_ops;
+  const int32_t* ops;         /* n_ops × 9: direct-lattice integer matrices W; q_ir = Wᵀ q */
+  const int32_t* op_inverse;  /* n_ops: index of W⁻¹ (PointSymmetry::get_inverse_index) */
+  int32_t identity;           /* PointSymmetry::find_identity_index */
+  double lattice_to_xyz[9];   /* direct lattice: columns are a1,a2,a3 in Å (to_xyz(angstrom)) */
+  double lattice_from_xyz[9]; /* its inverse */
+
+  /* -- trellis (PolyTrellis, src/trellis_poly.hpp; NodeContainer, src/trellis_node.hpp) -- */
+  int32_t n_knots[3];
+  const double* knots[3];     /* n_knots[d] bin edges along x, y, z */
+  int64_t n_nodes;            /* Π (n_knots[d]-1); linear index i + nx(j + ny k) */
+  const int32_t* node_type;   /* n_nodes: BRX_NODE_* */
+  const int32_t* node_index;  /* n_nodes: index into cube or poly nodes */
+  int32_t n_cube;
+  const int32_t* cube_vertices;   /* n_cube × 8, order (000)(100)(110)(010)(101)(001)(011)(111) */
+  int32_t n_poly;
+  const int32_t* poly_tet_offset; /* n_poly + 1 */
+  int64_t n_tets;
+  const int32_t* tet_vertices;    /* n_tets × 4, positively oriented */
+  const double* tet_sphere;       /* n_tets × 4: circumsphere centre x,y,z and radius */
+  const double* tet_volume;       /* n_tets */
+  int64_t n_vertices;
+  const double* vertex_xyz;       /* n_vertices × 3 */
+
+  /* -- Γ table for phonon eigenvectors (GammaTable, src/phonon.hpp:91-194) -- */
+  int32_t n_atoms;
+  const int32_t* gamma_F0;        /* n_atoms × n_ops: l = F0(k, r) */
+  const int32_t* gamma_vidx;      /* n_atoms × n_ops: index into gamma_vectors */
+  int32_t n_gamma_vectors;
+  const double* gamma_vectors;    /* n_gamma_vectors × 3: R⁻¹ r_l − r_k, fractional direct */
+
+  /* -- approx_float::Config (src/approx_config.hpp:17) -- */
+  double float_tolerance;         /* config.reciprocal, default 1e-12 */
+  int32_t digit;                  /* config.digit, default 1000 */
+} brx_geometry;
+
+/* Vertex data of one interpolator (the values or the vectors of a
+ * DualInterpolator, src/interpolatordual.hpp; decoded as in
+ * wrap/_interpolator.hpp:13-110). */
+typedef struct brx_data {
+  const void* data;               /* n_vertices × n_branches × span elements (host or device) */
+  int32_t dtype;                  /* BRX_F64 or BRX_C128 */
+  int32_t n_branches;             /* B */
+  int32_t elements[3];            /* scalars, vector elements (3 per vector), matrix elements (9 per matrix) */
+  int32_t rotates_like;           /* BRX_ROT_* */
+  int32_t length_unit;            /* BRX_LU_* */
+} brx_data;
+
+/* Per-q record of the locate stages, for index-level parity checks. */
+typedef struct brx_locate_out {
+  double* q_ir;                   /* n × 3: irreducible (or first-zone) q, r.l.u. */
+  int32_t* tau;                   /* n × 3: conventional τ with Q = Rᵀ q + τ (may be NULL) */
+  int32_t* rot;                   /* n × 2: R index and R⁻¹ index (may be NULL) */
+  int32_t* node;                  /* n × 2: node linear index and tetrahedron index (−1 for cube nodes) */
+  int32_t* n_weights;             /* n: number of (vertex, weight) pairs */
+  int32_t* vertex;                /* n × 8 */
+  double* weight;                 /* n × 8 */
+  int32_t* status;                /* n: 0 ok, else a brx_status code */
+} brx_locate_out;
+
+typedef struct brx_handle brx_handle;
+
+/* Upload the geometry; replaces BrillouinZoneTrellis3 construction as far as
+ * the query path is concerned (src/bz_trellis.hpp:56-59). */
+brx_status brx_create(const brx_geometry* geometry, int32_t device, brx_handle** out);
+void brx_destroy(brx_handle* h);
+
+/* Upload vertex data, replacing fill() (wrap/_common_grid.hpp:26-47,127-147;
+ * DualInterpolator::replace_data, src/interpolatordual.hpp:189-195).
+ * `vectors` may be NULL for a values-only grid.  storage is BRX_STORE_*. */
+brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vectors, int32_t storage);
+
+/* Optional mode-permutation table from sort() (PermutationTable,
+ * src/permutation_table.hpp:63-266): keys i*n_vertices+j sorted ascending,
+ * each naming one of n_perms permutations of n_branches modes.  Pairs not
+ * listed use the identity, as PermutationTable::safe_get does (:193-198). */
+brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* keys,
+                                const int32_t* perm_ids, int32_t n_perms, const int32_t* perms);
+
+/* ir_interpolate_at (src/bz_trellis.hpp:155-196; wrap/_common_grid.hpp:276-300).
+ * Q: n × 3 float64 in conventional r.l.u.; values_out: n × B_v × span_v and
+ * vectors_out: n × B_c × span_c in the input dtype (or float32/complex64 with
+ * BRX_FLAG_OUT_F32).  stream is a cudaStream_t or NULL for the handle's own. */
+brx_status brx_ir_interpolate_at(brx_handle* h, const double* Q, int64_t n,
+                                 void* values_out, void* vectors_out,
+                                 uint32_t flags, void* stream);
+
+/* interpolate_at: first-zone move and interpolation, no rotation
+ * (src/bz_trellis.hpp:113-129; wrap/_common_grid.hpp:412-440). */
+brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n,
+                              void* values_out, void* vectors_out,
+                              uint32_t flags, void* stream);
+
+/* The locate stages alone (ir_moveinto + node/tetrahedron search) with every
+ * intermediate index written out; `ir` selects ir_moveinto (1) or moveinto (0). */
+brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir,
+                      uint32_t flags, const brx_locate_out* out, void* stream);
+
+/* Wait for work queued with BRX_FLAG_ASYNC and report its status. */
+brx_status brx_sync(brx_handle* h, void* stream);
+
+/* Message for the last non-OK status on this handle (never NULL). */
+const char* brx_last_error(const brx_handle* h);
+
+/* Number of kernel launches this handle has issued since creation. */
+int64_t brx_launch_count(const brx_handle* h);
+
+int32_t brx_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BRX_H */

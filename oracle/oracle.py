@@ -1,0 +1,119 @@
+"""ctypes wrapper of the CPU oracle (brx_oracle.c).  TEST INFRASTRUCTURE.
+
+Only the tests, the smoke check and the CPU-baseline leg of bench.py use this
+module; the product (brille_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from brille_gb300._abi import BRX_C128, Data, GeometryHolder, make_data
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build(force=False):
+    """Compile the oracle with gcc (-ffp-contract=off keeps FP64 operation
+    order identical on x86-64 and aarch64)."""
+    src = os.path.join(HERE, "brx_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    cmd = ["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+           "-o", LIB + ".tmp", src, "-lm"]
+    subprocess.run(cmd, check=True)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+class OrcPerm(C.Structure):
+    _fields_ = [("n_keys", C.c_int64), ("keys", C.POINTER(C.c_int64)), ("ids", C.POINTER(C.c_int32)),
+                ("n_perms", C.c_int32), ("n_branches", C.c_int32), ("perms", C.POINTER(C.c_int32))]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _lib.orc_move.restype = C.c_int
+        _lib.orc_locate.restype = C.c_int
+        _lib.orc_interpolate_at.restype = C.c_int
+        _lib.orc_rotate.restype = C.c_int
+        _lib.orc_max_threads.restype = C.c_int
+    return _lib
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p()
+
+
+class Oracle:
+    """The oracle bound to one geometry (dict of tables)."""
+
+    def __init__(self, tables):
+        self.holder = GeometryHolder(tables)
+        self.g = C.byref(self.holder.struct)
+        self.t = tables
+
+    def move(self, Q, ir=True):
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, 3)
+        n = Q.shape[0]
+        q = np.zeros((n, 3))
+        tau = np.zeros((n, 3), np.int32)
+        rot = np.zeros((n, 2), np.int32)
+        st = np.zeros(n, np.int32)
+        lib().orc_move(self.g, _p(Q), C.c_int64(n), C.c_int(int(ir)), _p(q), _p(tau), _p(rot), _p(st))
+        return q, tau, rot, st
+
+    def locate(self, xyz, threads=0):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        n = xyz.shape[0]
+        node = np.zeros((n, 2), np.int32)
+        nw = np.zeros(n, np.int32)
+        vi = np.full((n, 8), -1, np.int32)
+        w = np.zeros((n, 8))
+        st = np.zeros(n, np.int32)
+        lib().orc_locate(self.g, _p(xyz), C.c_int64(n), _p(node), _p(nw), _p(vi), _p(w), _p(st), C.c_int(threads))
+        return node, nw, vi, w, st
+
+    def interpolate_at(self, Q, values, vectors=None, ir=True, no_move=False, threads=0,
+                       perm=None):
+        """values/vectors: (array (V,B,span), elements[3], rotates_like, length_unit)."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, 3)
+        n = Q.shape[0]
+        vd, va = make_data(values[0], values[0].shape[1], values[1], values[2], values[3])
+        outs = []
+        vo = np.zeros((n,) + va.shape[1:], dtype=va.dtype)
+        if vectors is not None:
+            cd, ca = make_data(vectors[0], vectors[0].shape[1], vectors[1], vectors[2], vectors[3])
+            co = np.zeros((n,) + ca.shape[1:], dtype=ca.dtype)
+            cptr = C.byref(cd)
+        else:
+            cd, ca, co, cptr = None, None, None, None
+        st = np.zeros(n, np.int32)
+        pp = None
+        if perm is not None:
+            keys, ids, perms = perm
+            keys = np.ascontiguousarray(keys, np.int64)
+            ids = np.ascontiguousarray(ids, np.int32)
+            perms = np.ascontiguousarray(perms, np.int32)
+            pstruct = OrcPerm(keys.size, keys.ctypes.data_as(C.POINTER(C.c_int64)),
+                              ids.ctypes.data_as(C.POINTER(C.c_int32)), perms.shape[0], perms.shape[1],
+                              perms.ctypes.data_as(C.POINTER(C.c_int32)))
+            pp = C.byref(pstruct)
+        rc = lib().orc_interpolate_at(self.g, C.byref(vd), cptr, pp, _p(Q), C.c_int64(n), C.c_int(int(ir)),
+                                      C.c_int(int(no_move)), _p(vo), _p(co) if co is not None else C.c_void_p(),
+                                      _p(st), C.c_int(threads))
+        return vo, co, rc, st
+
+    @staticmethod
+    def max_threads():
+        return lib().orc_max_threads()
