@@ -1,0 +1,333 @@
+#!/usr/bin/env python3
+"""Throughput of brille's ir_interpolate_at query path on GB300.
+
+One step = one ir_interpolate_at pass over one batch of seeded synthetic q
+(uniform in [-L, L]³ r.l.u.) on the workload's trellis.  Default workload:
+P6₃/mmc, a = 3.2 Å, c = 5.2 Å, 16 atoms (48 modes), eigenvalues plus
+Γ-rotated eigenvectors, FP64 predicates, FP32 gather/rotate with
+float32/complex64 outputs, q in [-2, 2]³.
+
+Reported (one JSON line from rank 0):
+  value      q-points/s, all ranks, inputs and outputs resident in HBM
+  e2e        the same through the public API with pinned host Q and outputs
+             (host→device and device→host copies inside the timed region)
+  roofline   the dominant kernel's algorithmic bytes over its CUDA-event time
+             against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP
+             path) on a bounded sample, on this host's cores
+
+`--impl reference` times that CPU implementation alone (the reference itself
+cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (crystal builder, node volume as a fraction of the zone, q half-range)
+    "hex16": ("hexagonal16", 3.2e-7, 2.0),
+    "hex16-small": ("hexagonal16", 1e-5, 2.0),
+    "diamond8": ("diamond_conventional", 1 / 5000, 1.0),
+    "diamond2": ("diamond_primitive", 1 / 5000, 1.0),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def build_workload(name, device_modes=True):
+    from brille_gb300 import workloads as W
+    from brille_gb300.bz import BrillouinZone
+    from brille_gb300.trellis import TrellisBuild
+
+    builder, fraction, qr = WORKLOADS[name]
+    lat, masses = getattr(W, builder)()
+    bz = BrillouinZone(lat)
+    t = time.time()
+    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * fraction)
+    log(f"[setup] trellis {tr.summary()} in {time.time() - t:.1f}s")
+    model = W.bvk_for(lat, masses)
+    qv = tr.vertices @ np.linalg.inv(lat.B)
+    t = time.time()
+    if device_modes:
+        w, v = model.modes_torch(qv)
+    else:
+        w, v = model.modes(qv)
+    log(f"[setup] BvK modes for {len(qv)} vertices in {time.time() - t:.1f}s")
+    return dict(name=name, lat=lat, bz=bz, tr=tr, model=model, w=w, v=v, q_range=qr)
+
+
+def bytes_per_q(B, n_atoms, out_f32):
+    s = 4 if out_f32 else 8
+    vals = B * s
+    vecs = B * 3 * n_atoms * 2 * s
+    return 24, vals, vecs
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [l.split(",") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for k, n in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def cpu_baseline(wl, target_s=12.0, threads=0):
+    """The oracle (CPU restatement of the reference's path) on a bounded sample."""
+    from brille_gb300.tables import geometry_tables
+    from oracle.oracle import Oracle
+
+    t = geometry_tables(wl["bz"], wl["tr"])
+    o = Oracle(t)
+    w, v = wl["w"], wl["v"]
+    nv, B = w.shape
+    vals = (np.ascontiguousarray(w[:, :, None]), [1, 0, 0], 0, 3)
+    vecs = (np.ascontiguousarray(v.reshape(nv, B, -1)), [0, 3 * v.shape[2], 0], 2, 1)
+    rng = np.random.default_rng(123)
+    qr = wl["q_range"]
+    n = 256
+    while True:
+        Q = rng.uniform(-qr, qr, size=(n, 3))
+        t0 = time.perf_counter()
+        o.interpolate_at(Q, vals, vecs, threads=threads)
+        dt = time.perf_counter() - t0
+        if dt > target_s / 4 or n >= 1 << 22:
+            break
+        n = int(n * min(16, max(2, (target_s / 4) / max(dt, 1e-3))))
+    n_final = max(n, int(n * target_s / max(dt, 1e-6)))
+    Q = rng.uniform(-qr, qr, size=(n_final, 3))
+    t0 = time.perf_counter()
+    _, _, rc, _ = o.interpolate_at(Q, vals, vecs, threads=threads)
+    dt = time.perf_counter() - t0
+    cores = threads if threads > 0 else Oracle.max_threads()
+    return dict(value=n_final / dt, unit="q-points/s", cores=cores, kind="port",
+                sample=f"{n_final} q uniform in [-{qr},{qr}]^3 on the same trellis, FP64, values+vectors, "
+                       f"serial move stage and OpenMP locate/gather/rotate as the reference", seconds=dt, rc=rc)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    wl = build_workload(args.workload, device_modes=False)
+    vals = []
+    import oracle.oracle as orc
+    nthreads = orc.Oracle.max_threads()
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(wl, target_s=max(2.0, 60.0 / (args.steps + args.warmup)), threads=nthreads)
+        if i >= args.warmup:
+            vals.append(r)
+    value = float(np.median([r["value"] for r in vals]))
+    out = dict(metric="interp q-pts/s on 1 GB300 (learned+coarse vs plain GPU) at <=1e-3 meV max err",
+               impl="reference", value=value, unit="q-points/s", n_gpus=0, steps=args.steps, warmup=args.warmup,
+               ms_per_step=float(np.median([r["seconds"] for r in vals])) * 1e3, higher_is_better=True,
+               scaling="weak", vs_baseline=None, dtype="f64", data="synthetic (seeded BvK model, uniform q)",
+               config=dict(workload=args.workload, trellis_vertices=int(len(wl["tr"].vertices)),
+                           modes=int(wl["w"].shape[1])),
+               cpu_baseline=dict(value=value, unit="q-points/s", cores=vals[-1]["cores"], kind="port",
+                                 sample=vals[-1]["sample"]),
+               e2e=dict(value=value, unit="q-points/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="hex16", choices=sorted(WORKLOADS))
+    ap.add_argument("--q-per-step", type=int, default=1 << 20)
+    ap.add_argument("--storage", default="f32", choices=["f32", "f64", "bf16"])
+    ap.add_argument("--out-f64", action="store_true", help="float64/complex128 outputs")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from brille_gb300 import BZTrellisQdc
+
+    wl = build_workload(args.workload)
+    B, na = wl["w"].shape[1], wl["v"].shape[2]
+    grid = BZTrellisQdc(wl["bz"], trellis=wl["tr"], device=local)
+    grid.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage=args.storage)
+    out_f32 = not args.out_f64
+    n = args.q_per_step
+    qr = wl["q_range"]
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1000 + rank)
+    nbuf = 2
+    Qs = [(torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float64) * 2 - 1) * qr for _ in range(nbuf)]
+    fdt = torch.float32 if out_f32 else torch.float64
+    cdt = torch.complex64 if out_f32 else torch.complex128
+    vals = torch.empty((n, B), dtype=fdt, device=dev)
+    vecs = torch.empty((n, B, na, 3), dtype=cdt, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def step(i):
+        grid.query_into(Qs[i % nbuf], n, vals, vecs, out_f32=out_f32, async_=True, stream=sp)
+
+    for i in range(args.warmup):
+        step(i)
+        grid.sync(sp)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    grid.profile(True)
+    l0 = grid.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for i in range(args.steps):
+            step(i)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        grid.sync(sp)
+    launches = grid.launch_count() - l0
+    stage_ms, stage_q = grid.stage_times()
+    grid.profile(False)
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    value = world * n * args.steps / (ms / 1e3)
+
+    # roofline of the dominant kernel
+    bq_in, bq_vals, bq_vecs = bytes_per_q(B, na, out_f32)
+    stage_names = ["locate", "node_sort", "gather_values", "gather_vectors"]
+    dom = int(np.argmax(stage_ms))
+    per_q_bytes = {0: bq_in + 4 * 8 + 8 * 12 + 40, 1: 16, 2: bq_vals, 3: bq_vecs}[dom]
+    achieved = per_q_bytes * stage_q / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
+    peaks = measured_peaks()
+    peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
+    roofline = dict(bound="hbm", kernel=stage_names[dom], achieved=round(achieved, 1), peak=peak,
+                    peak_source="measured" if peaks else "fallback", unit="GB/s",
+                    frac=round(achieved / peak, 4), traffic=None,
+                    algorithmic_bytes_per_q=per_q_bytes,
+                    stage_ms_per_step={k: round(v / args.steps, 3) for k, v in zip(stage_names, stage_ms)})
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        ne = n
+        Qh = torch.empty((ne, 3), dtype=torch.float64, pin_memory=True)
+        Qh.copy_(Qs[0].cpu())
+        vh = torch.empty((ne, B), dtype=fdt, pin_memory=True)
+        ch = torch.empty((ne, B, na, 3), dtype=cdt, pin_memory=True)
+        grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
+        te = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([te], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        h2d = ne * 24
+        d2h = ne * (bq_vals + bq_vecs)
+        e2e = dict(value=world * ne * args.e2e_steps / te, unit="q-points/s", h2d_bytes_per_step=h2d,
+                   d2h_bytes_per_step=d2h)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(wl)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        out = dict(
+            metric="interp q-pts/s on 1 GB300 (learned+coarse vs plain GPU) at <=1e-3 meV max err",
+            value=value, unit="q-points/s", n_gpus=world, steps=args.steps, warmup=args.warmup,
+            ms_per_step=ms_per_step, higher_is_better=True, scaling="weak", vs_baseline=None,
+            dtype="f64 predicates, f32 gather/rotate" if args.storage != "f64" else "f64",
+            data="synthetic (seeded BvK model at trellis vertices, q uniform)",
+            config=dict(workload=args.workload, path="plain fine trellis, ir_interpolate_at",
+                        trellis_vertices=int(len(wl["tr"].vertices)), modes=int(B), atoms=int(na),
+                        q_per_step=n, q_range=qr, storage=args.storage,
+                        outputs="f32/c64" if out_f32 else "f64/c128",
+                        l2="outputs of %.1f GB per step exceed the 129 MB L2" % (n * (bq_vals + bq_vecs) / 1e9),
+                        parallelism=f"replicas x{world}, q sharded, no collective on the data path"),
+            roofline=roofline, e2e=e2e, cpu_baseline=cpu, gpu_launches=int(launches),
+            clocks=clk.summary())
+        print(json.dumps(out), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

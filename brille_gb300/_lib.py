@@ -1,0 +1,71 @@
+"""Loader for the CUDA library (libbrx.so) through its C ABI.
+
+There is no CPU fallback: if the library is missing or no GPU is present the
+query path raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from ._abi import Data, Geometry, LocateOut
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libbrx.so")
+
+_lib = None
+
+
+class BrxError(RuntimeError):
+    """A non-OK status from the C ABI, carrying the library's message."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+def load(build_if_missing=True):
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(f"{LIB_PATH} has not been built; run brille_gb300.build.build()")
+        from .build import build
+        build()
+    lib = C.CDLL(LIB_PATH)
+    h = C.c_void_p
+    lib.brx_create.argtypes = [C.POINTER(Geometry), C.c_int32, C.POINTER(h)]
+    lib.brx_create.restype = C.c_int
+    lib.brx_destroy.argtypes = [h]
+    lib.brx_destroy.restype = None
+    lib.brx_fill.argtypes = [h, C.POINTER(Data), C.POINTER(Data), C.c_int32]
+    lib.brx_fill.restype = C.c_int
+    lib.brx_set_permutations.argtypes = [h, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
+    lib.brx_set_permutations.restype = C.c_int
+    for name in ("brx_ir_interpolate_at", "brx_interpolate_at"):
+        f = getattr(lib, name)
+        f.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+        f.restype = C.c_int
+    lib.brx_locate.argtypes = [h, C.c_void_p, C.c_int64, C.c_int32, C.c_uint32, C.POINTER(LocateOut), C.c_void_p]
+    lib.brx_locate.restype = C.c_int
+    lib.brx_sync.argtypes = [h, C.c_void_p]
+    lib.brx_sync.restype = C.c_int
+    lib.brx_last_error.argtypes = [h]
+    lib.brx_last_error.restype = C.c_char_p
+    lib.brx_launch_count.argtypes = [h]
+    lib.brx_launch_count.restype = C.c_int64
+    lib.brx_profile.argtypes = [h, C.c_int32]
+    lib.brx_profile.restype = C.c_int
+    lib.brx_stage_times.argtypes = [h, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int64)]
+    lib.brx_stage_times.restype = C.c_int
+    lib.brx_abi_version.argtypes = []
+    lib.brx_abi_version.restype = C.c_int32
+    _lib = lib
+    return lib
+
+
+def check(status, handle=None):
+    if status != 0:
+        msg = load().brx_last_error(handle).decode() if handle else f"status {status}"
+        raise BrxError(status, msg)

@@ -1,0 +1,791 @@
+// C ABI of the GB300 query path (include/brx.h).
+//
+// A brx_handle owns the device copy of one trellis geometry, its vertex data
+// and the per-chunk scratch of the query pipeline:
+//
+//   locate (FP64 move + wedge + node/tetrahedron search, one thread per q)
+//   -> counting sort of q by trellis node
+//   -> gather + rotate for the values, then for the vectors
+//
+// Large queries run in chunks.  With host buffers, chunks alternate between
+// two streams and two scratch sets so that copies overlap compute.  Errors
+// are collected per q on the device and turned into the reference's
+// messages on the host; no exception crosses the ABI.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/brx.h"
+#include "brx_kernels.h"
+
+using namespace brx;
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct Interp {
+  bool present = false;
+  bool cplx = false;
+  int store = ST_F64;  // StoreKind of the device copy
+  int B = 0, s = 0;
+  int el[3] = {0, 0, 0};
+  int rotates_like = 0, length_unit = 0;
+  DevBuf data;
+};
+
+struct Scratch {
+  DevBuf rec;     // records
+  DevBuf sortbuf; // counts + cursors
+  DevBuf qbuf;    // staged Q
+  DevBuf vbuf, cbuf;  // staged outputs (host I/O)
+  Records r{};
+  int32_t* order = nullptr;
+  int32_t* counts = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+}  // namespace
+
+struct brx_handle {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  DevGeom g{};
+  std::vector<DevBuf> tables;
+  brx_geometry host_geom{};
+  std::vector<double> rot_cart;
+  Interp vals, vecs;
+  int storage = BRX_STORE_F64;
+  bool filled = false;
+  // permutation table
+  DevBuf perm_keys, perm_ids, perms;
+  long long n_keys = 0;
+  int n_perms = 0;
+  Scratch sc[2];
+  long long scratch_q = 0;
+  ErrorWord* err = nullptr;       // device
+  ErrorWord* err_host = nullptr;  // pinned
+  std::string message = "no error";
+  long long launches = 0;
+  // stage timing (brx_profile): events per chunk, accumulated after sync
+  bool profile = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  double stage_ms[5] = {0, 0, 0, 0, 0};
+  long long stage_q = 0;
+  bool async_pending = false;
+  cudaStream_t async_stream = nullptr;
+  int async_ir = 0;
+  const double* async_Q = nullptr;
+  long long async_n = 0;
+};
+
+namespace {
+
+brx_status fail(brx_handle* h, brx_status st, const std::string& msg) {
+  if (h) h->message = msg;
+  return st;
+}
+
+brx_status cuda_fail(brx_handle* h, cudaError_t e, const char* where) {
+  std::string m = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(h, BRX_ERR_OUT_OF_MEMORY, m);
+  return fail(h, BRX_ERR_CUDA, m);
+}
+
+#define BRX_CUDA(h, call)                               \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
+  } while (0)
+
+template <typename T>
+brx_status upload(brx_handle* h, const T* src, size_t count, const T** dst) {
+  h->tables.emplace_back();
+  DevBuf& b = h->tables.back();
+  size_t bytes = sizeof(T) * (count ? count : 1);
+  BRX_CUDA(h, b.ensure(bytes));
+  if (count) BRX_CUDA(h, cudaMemcpy(b.p, src, sizeof(T) * count, cudaMemcpyHostToDevice));
+  *dst = static_cast<const T*>(b.p);
+  return BRX_OK;
+}
+
+// C = A·B for 3×3, accumulated from zero in k order (src/utilities.tpp:48-55)
+void mm3(double* C, const double* A, const double* B) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += A[3 * i + k] * B[3 * k + j];
+      C[3 * i + j] = s;
+    }
+}
+
+bool host_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged;
+}
+
+int span(const Interp& d) { return d.el[0] + d.el[1] + d.el[2]; }
+
+// rotation support, mirroring Interpolator::rotate_in_place (src/interpolator.hpp:387-428)
+brx_status rotation_mode(const Interp& d, int* mode, std::string* msg) {
+  *mode = ROT_NONE;
+  const int nvec = d.el[1] / 3, nmat = d.el[2] / 9;
+  const char* combo = "LengthUnit, RotatesLike combination not implemented";
+  switch (d.length_unit) {
+    case BRX_LU_REAL_LATTICE:
+      if (d.rotates_like == BRX_ROT_VECTOR) *mode = ROT_REAL;
+      else if (d.rotates_like == BRX_ROT_PSEUDOVECTOR) *mode = ROT_AXIAL;
+      else if (d.rotates_like == BRX_ROT_GAMMA) *mode = ROT_GAMMA;
+      else { *msg = "Impossible RotatesLike value!"; return BRX_ERR_UNSUPPORTED; }
+      break;
+    case BRX_LU_RECIPROCAL_LATTICE:
+      if (d.rotates_like != BRX_ROT_VECTOR) { *msg = combo; return BRX_ERR_UNSUPPORTED; }
+      *mode = ROT_RECIP;
+      break;
+    case BRX_LU_ANGSTROM:
+      if (d.rotates_like != BRX_ROT_GAMMA) { *msg = combo; return BRX_ERR_UNSUPPORTED; }
+      *mode = ROT_GAMMA;
+      break;
+    default:
+      *msg = combo;
+      return BRX_ERR_UNSUPPORTED;
+  }
+  if (*mode == ROT_GAMMA) {
+    if (!d.cplx) { *msg = "RotatesLike == Gamma requires complex valued data!"; return BRX_ERR_UNSUPPORTED; }
+    const int Nmat = (int)std::sqrt((double)nmat) / 3;
+    if (nmat > 0) {
+      if (nmat == 9 * Nmat * Nmat) {
+        *msg = "Gamma rotation of 3x3 tensors is not defined for this element count";
+        return BRX_ERR_UNSUPPORTED;
+      }
+      *mode = ROT_NONE;  // the reference rotates nothing in this case
+    }
+  }
+  if (nvec == 0 && nmat == 0) *mode = ROT_NONE;
+  return BRX_OK;
+}
+
+brx_status ensure_scratch(brx_handle* h, long long chunk) {
+  if (chunk <= h->scratch_q) return BRX_OK;
+  const size_t n = (size_t)chunk;
+  const size_t parts[9] = {24 * n, 64 * n, 12 * n, 8 * n, 8 * n, 4 * n, 32 * n, 4 * n, 4 * n};
+  size_t rec = 0;
+  for (size_t b : parts) rec += (b + 255) & ~size_t(255);
+  for (auto& s : h->sc) {
+    BRX_CUDA(h, s.rec.ensure(rec));
+    char* p = static_cast<char*>(s.rec.p);
+    auto take = [&](size_t bytes) {
+      char* at = p;
+      p += (bytes + 255) & ~size_t(255);
+      return at;
+    };
+    s.r.q_ir = reinterpret_cast<double*>(take(24 * n));
+    s.r.w = reinterpret_cast<double*>(take(64 * n));
+    s.r.tau = reinterpret_cast<int32_t*>(take(12 * n));
+    s.r.rot = reinterpret_cast<int32_t*>(take(8 * n));
+    s.r.node = reinterpret_cast<int32_t*>(take(8 * n));
+    s.r.nw = reinterpret_cast<int32_t*>(take(4 * n));
+    s.r.vidx = reinterpret_cast<int32_t*>(take(32 * n));
+    s.r.status = reinterpret_cast<int32_t*>(take(4 * n));
+    s.order = reinterpret_cast<int32_t*>(take(4 * n));
+    BRX_CUDA(h, s.sortbuf.ensure(sizeof(int32_t) * node_sort_scratch_ints(h->g.n_nodes)));
+    s.counts = static_cast<int32_t*>(s.sortbuf.p);
+  }
+  h->scratch_q = chunk;
+  return BRX_OK;
+}
+
+GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, long long n, int rot_mode, bool phase) {
+  GatherParams p{};
+  p.nw = s.r.nw;
+  p.vidx = s.r.vidx;
+  p.w = s.r.w;
+  p.rot = s.r.rot;
+  p.q_ir = s.r.q_ir;
+  p.status = s.r.status;
+  p.order = s.order;
+  p.n = n;
+  p.data = d.data.p;
+  p.B = d.B;
+  p.s = span(d);
+  p.nsc = d.el[0];
+  p.nvec = d.el[1] / 3;
+  p.nmat = d.el[2] / 9;
+  p.rot_mode = rot_mode;
+  p.gamma_cart = d.length_unit == BRX_LU_ANGSTROM;
+  p.phase_allowed = phase ? 1 : 0;
+  p.Nmat = 0;
+  p.n_keys = h->n_keys;
+  p.keys = static_cast<const long long*>(h->perm_keys.p);
+  p.perm_ids = static_cast<const int32_t*>(h->perm_ids.p);
+  p.n_perms = h->n_perms;
+  p.perms = static_cast<const int32_t*>(h->perms.p);
+  p.n_vertices = h->host_geom.n_vertices;
+  p.ops = h->g.ops;
+  p.rot_cart = h->g.rot_cart;
+  p.n_ops = h->g.n_ops;
+  p.gamma_F0 = h->g.gamma_F0;
+  p.gamma_vidx = h->g.gamma_vidx;
+  p.gamma_vectors = h->g.gamma_vectors;
+  const int cmax = 24;
+  int nc = 1;
+  while (nc < 32 && (p.s + nc - 1) / nc > cmax) nc <<= 1;
+  p.n_chunks = nc;
+  p.chunk_len = (p.s + nc - 1) / nc;
+  return p;
+}
+
+size_t smem_budget(brx_handle* h) {
+  size_t b = 72 * 1024;
+  if (h->smem_optin && b > h->smem_optin) b = h->smem_optin;
+  return b;
+}
+
+size_t out_elem_bytes(const Interp& d, bool f32) {
+  size_t e = f32 ? 4 : 8;
+  return e * (d.cplx ? 2 : 1);
+}
+
+// Read the device error word and build the reference's message.
+brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, bool q_host) {
+  ErrorWord ew = *h->err_host;
+  if (!ew.flags) return BRX_OK;
+  auto has = [&](int st) { return (ew.flags >> st) & 1; };
+  double qv[3] = {0, 0, 0};
+  long long i = ew.first_bad;
+  if (i >= 0 && i < n) {
+    if (q_host) std::memcpy(qv, Q + 3 * i, sizeof qv);
+    else cudaMemcpy(qv, Q + 3 * i, sizeof qv, cudaMemcpyDeviceToHost);
+  }
+  char buf[512];
+  if (has(BRX_ERR_MOVE_FAILED)) {
+    std::snprintf(buf, sizeof buf, "Not all points inside Brillouin zone (%d of %lld still outside; first Q = [%.17g %.17g %.17g])",
+                  ew.count, n, qv[0], qv[1], qv[2]);
+    return fail(h, BRX_ERR_MOVE_FAILED, buf);
+  }
+  if (has(BRX_ERR_OUTSIDE_IR)) {
+    std::snprintf(buf, sizeof buf, "Q = [%.17g %.17g %.17g] is outside of the irreducible BrillouinZone", qv[0], qv[1], qv[2]);
+    return fail(h, BRX_ERR_OUTSIDE_IR, buf);
+  }
+  if (has(BRX_ERR_IMPOSSIBLE)) return fail(h, BRX_ERR_IMPOSSIBLE, "This shouldn't be possible");
+  if (has(BRX_ERR_NULL_NODE)) {
+    std::snprintf(buf, sizeof buf, "Attempting to access null node for point Q = [%.17g %.17g %.17g]", qv[0], qv[1], qv[2]);
+    return fail(h, BRX_ERR_NULL_NODE, buf);
+  }
+  if (has(BRX_ERR_NOT_FOUND)) {
+    std::snprintf(buf, sizeof buf, "interpolate_at failed to find %d point%s", ew.count, ew.count > 1 ? "s." : ".");
+    return fail(h, BRX_ERR_NOT_FOUND, buf);
+  }
+  (void)ir;
+  return fail(h, BRX_ERR_CUDA, "unknown device error");
+}
+
+cudaEvent_t next_event(brx_handle* h) {
+  if (h->ev_used == h->ev_pool.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    h->ev_pool.push_back(e);
+  }
+  return h->ev_pool[h->ev_used++];
+}
+
+// accumulate stage durations from the events recorded since the last call
+void harvest_events(brx_handle* h) {
+  for (size_t i = 0; i + 5 < h->ev_used + 1 && i + 4 < h->ev_used; i += 5) {
+    for (int k = 0; k < 4; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, h->ev_pool[i + k], h->ev_pool[i + k + 1]) == cudaSuccess) h->stage_ms[k] += ms;
+    }
+  }
+  h->ev_used = 0;
+}
+
+brx_status reset_errors(brx_handle* h, cudaStream_t s) {
+  ErrorWord z{0, 0, (long long)0x7fffffffffffffffLL};
+  *h->err_host = z;
+  BRX_CUDA(h, cudaMemcpyAsync(h->err, h->err_host, sizeof(ErrorWord), cudaMemcpyHostToDevice, s));
+  return BRX_OK;
+}
+
+// The whole query, chunked.  mode: 0 interpolate_at, 1 ir_interpolate_at.
+brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* vals_out, void* vecs_out,
+                     uint32_t flags, void* user_stream, const brx_locate_out* lout) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (n < 0 || (n > 0 && !Q)) return fail(h, BRX_ERR_INVALID_ARGUMENT, "Q must be a non-null (n,3) array");
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  const bool locate_only = lout != nullptr;
+  if (!locate_only) {
+    if (!h->filled) return fail(h, BRX_ERR_NOT_FILLED, "The interpolation data must be filled before interpolating.");
+    if (!vals_out || (h->vecs.present && !vecs_out))
+      return fail(h, BRX_ERR_INVALID_ARGUMENT, "output buffers must be provided");
+  }
+  const bool no_move = flags & BRX_FLAG_NO_MOVE;
+  const bool f32 = flags & BRX_FLAG_OUT_F32;
+  int vmode = ROT_NONE, cmode = ROT_NONE;
+  if (ir && !locate_only) {
+    std::string msg;
+    brx_status st = rotation_mode(h->vals, &vmode, &msg);
+    if (st) return fail(h, st, msg);
+    if (h->vecs.present) {
+      st = rotation_mode(h->vecs, &cmode, &msg);
+      if (st) return fail(h, st, msg);
+    }
+  }
+  const int kmode = no_move ? 2 : (ir ? 1 : 0);
+  if (n == 0) return BRX_OK;
+
+  const bool q_host = host_ptr(Q);
+  const bool o_host = locate_only ? host_ptr(lout->status) : host_ptr(vals_out);
+  const bool any_host = q_host || o_host;
+  const bool async = (flags & BRX_FLAG_ASYNC) && !any_host;
+
+  size_t out_q = 0;  // output bytes per q
+  if (!locate_only) {
+    out_q += (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
+    if (h->vecs.present) out_q += (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
+  }
+  long long chunk = 1LL << 22;
+  if (o_host && out_q) chunk = std::max<long long>(1024, std::min<long long>(chunk, (512LL << 20) / (long long)out_q));
+  if (chunk > n) chunk = n;
+  brx_status st = ensure_scratch(h, chunk);
+  if (st) return st;
+
+  cudaStream_t us = static_cast<cudaStream_t>(user_stream);
+  const int nstreams = (any_host && !us) ? 2 : 1;
+  cudaStream_t main_s = us ? us : h->sc[0].stream;
+  if (h->async_pending && (any_host || !(flags & BRX_FLAG_ASYNC) || main_s != h->async_stream))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "asynchronous queries must be synchronised with brx_sync first");
+  if (!h->async_pending) {
+    // queued asynchronous queries on one stream share one error word until brx_sync
+    st = reset_errors(h, main_s);
+    if (st) return st;
+  }
+  if (nstreams == 2) {
+    BRX_CUDA(h, cudaEventRecord(h->sc[0].done, main_s));
+    BRX_CUDA(h, cudaStreamWaitEvent(h->sc[1].stream, h->sc[0].done, 0));
+  }
+  const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
+  const size_t crow = h->vecs.present ? (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32) : 0;
+  if (!locate_only && o_host) {
+    for (int k = 0; k < nstreams; ++k) {
+      BRX_CUDA(h, h->sc[k].vbuf.ensure(vrow * (size_t)chunk + 16));
+      if (crow) BRX_CUDA(h, h->sc[k].cbuf.ensure(crow * (size_t)chunk + 16));
+    }
+  }
+  if (q_host)
+    for (int k = 0; k < nstreams; ++k) BRX_CUDA(h, h->sc[k].qbuf.ensure(24 * (size_t)chunk + 16));
+
+  long long ci = 0;
+  for (long long base = 0; base < n; base += chunk, ++ci) {
+    const long long m = std::min(chunk, n - base);
+    Scratch& s = h->sc[nstreams == 2 ? (ci & 1) : 0];
+    cudaStream_t cs = nstreams == 2 ? s.stream : main_s;
+    const double* Qd = Q + 3 * base;
+    if (q_host) {
+      BRX_CUDA(h, cudaMemcpyAsync(s.qbuf.p, Q + 3 * base, 24 * (size_t)m, cudaMemcpyHostToDevice, cs));
+      Qd = static_cast<const double*>(s.qbuf.p);
+    }
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (h->profile && !locate_only) {
+      for (auto& e : ev) e = next_event(h);
+      cudaEventRecord(ev[0], cs);
+      h->stage_q += m;
+    }
+    launch_locate(h->g, Qd, m, base, kmode, s.r, h->err, h->num_sms, cs);
+    ++h->launches;
+    if (ev[1]) cudaEventRecord(ev[1], cs);
+    if (locate_only) {
+      auto cp = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+        if (!dst) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, cs);
+      };
+      BRX_CUDA(h, cp(lout->q_ir ? lout->q_ir + 3 * base : nullptr, s.r.q_ir, 24 * (size_t)m));
+      BRX_CUDA(h, cp(lout->tau ? lout->tau + 3 * base : nullptr, s.r.tau, 12 * (size_t)m));
+      BRX_CUDA(h, cp(lout->rot ? lout->rot + 2 * base : nullptr, s.r.rot, 8 * (size_t)m));
+      BRX_CUDA(h, cp(lout->node ? lout->node + 2 * base : nullptr, s.r.node, 8 * (size_t)m));
+      BRX_CUDA(h, cp(lout->n_weights ? lout->n_weights + base : nullptr, s.r.nw, 4 * (size_t)m));
+      BRX_CUDA(h, cp(lout->vertex ? lout->vertex + 8 * base : nullptr, s.r.vidx, 32 * (size_t)m));
+      BRX_CUDA(h, cp(lout->weight ? lout->weight + 8 * base : nullptr, s.r.w, 64 * (size_t)m));
+      BRX_CUDA(h, cp(lout->status ? lout->status + base : nullptr, s.r.status, 4 * (size_t)m));
+      continue;
+    }
+    launch_node_sort(s.r.node, s.r.status, m, h->g.n_nodes, s.counts, s.order, cs);
+    h->launches += 3;
+    if (ev[2]) cudaEventRecord(ev[2], cs);
+    char* vdst = o_host ? static_cast<char*>(s.vbuf.p) : static_cast<char*>(vals_out) + vrow * (size_t)base;
+    {
+      GatherParams p = gather_params(h, h->vals, s, m, ir ? vmode : ROT_NONE, false);
+      p.out = vdst;
+      p.q_tile = gather_pick_tile(p, h->vals.store, h->vals.cplx, smem_budget(h));
+      h->launches += launch_gather(p, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h), cs);
+    }
+    if (ev[3]) cudaEventRecord(ev[3], cs);
+    char* cdst = nullptr;
+    if (h->vecs.present) {
+      cdst = o_host ? static_cast<char*>(s.cbuf.p) : static_cast<char*>(vecs_out) + crow * (size_t)base;
+      GatherParams p = gather_params(h, h->vecs, s, m, ir ? cmode : ROT_NONE, h->vecs.cplx);
+      p.out = cdst;
+      p.q_tile = gather_pick_tile(p, h->vecs.store, h->vecs.cplx, smem_budget(h));
+      h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h), cs);
+    }
+    if (ev[4]) cudaEventRecord(ev[4], cs);
+    BRX_CUDA(h, cudaGetLastError());
+    if (o_host) {
+      BRX_CUDA(h, cudaMemcpyAsync(static_cast<char*>(vals_out) + vrow * (size_t)base, vdst, vrow * (size_t)m,
+                                  cudaMemcpyDeviceToHost, cs));
+      if (cdst)
+        BRX_CUDA(h, cudaMemcpyAsync(static_cast<char*>(vecs_out) + crow * (size_t)base, cdst, crow * (size_t)m,
+                                    cudaMemcpyDeviceToHost, cs));
+    }
+  }
+  BRX_CUDA(h, cudaGetLastError());
+  if (nstreams == 2) {
+    BRX_CUDA(h, cudaEventRecord(h->sc[1].done, h->sc[1].stream));
+    BRX_CUDA(h, cudaStreamWaitEvent(main_s, h->sc[1].done, 0));
+  }
+  BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(ErrorWord), cudaMemcpyDeviceToHost, main_s));
+  if (async) {
+    h->async_pending = true;
+    h->async_stream = main_s;
+    h->async_ir = ir;
+    h->async_Q = Q;
+    h->async_n = n;
+    return BRX_OK;
+  }
+  BRX_CUDA(h, cudaStreamSynchronize(main_s));
+  if (nstreams == 2) BRX_CUDA(h, cudaStreamSynchronize(h->sc[1].stream));
+  if (h->profile) harvest_events(h);
+  return collect_errors(h, ir, Q, n, q_host);
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t brx_abi_version(void) { return BRX_ABI_VERSION; }
+
+brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out) {
+  if (!gin || !out) return BRX_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const brx_geometry& G = *gin;
+  if (G.n_faces < 4 || !G.face_abc || !G.face_normal || !G.face_tau || !G.face_tau_len) return BRX_ERR_INVALID_ARGUMENT;
+  if (G.n_ops < 1 || !G.ops || !G.op_inverse || G.identity < 0 || G.identity >= G.n_ops) return BRX_ERR_INVALID_ARGUMENT;
+  if (G.n_wedge < 0 || (G.n_wedge > 0 && !G.wedge_normal)) return BRX_ERR_INVALID_ARGUMENT;
+  for (int d = 0; d < 3; ++d)
+    if (G.n_knots[d] < 2 || !G.knots[d]) return BRX_ERR_INVALID_ARGUMENT;
+  long long nn = (long long)(G.n_knots[0] - 1) * (G.n_knots[1] - 1) * (G.n_knots[2] - 1);
+  if (G.n_nodes != nn || !G.node_type || !G.node_index || G.n_vertices < 1 || !G.vertex_xyz)
+    return BRX_ERR_INVALID_ARGUMENT;
+  // every index in the tables must stay in bounds: checked here once so the
+  // kernels can trust them
+  for (long long i = 0; i < G.n_nodes; ++i) {
+    int t = G.node_type[i], k = G.node_index[i];
+    if (t == BRX_NODE_CUBE && (k < 0 || k >= G.n_cube)) return BRX_ERR_INVALID_ARGUMENT;
+    if (t == BRX_NODE_POLY && (k < 0 || k >= G.n_poly)) return BRX_ERR_INVALID_ARGUMENT;
+    if (t != BRX_NODE_NULL && t != BRX_NODE_CUBE && t != BRX_NODE_POLY) return BRX_ERR_INVALID_ARGUMENT;
+  }
+  for (long long i = 0; i < 8LL * G.n_cube; ++i)
+    if (G.cube_vertices[i] < 0 || G.cube_vertices[i] >= G.n_vertices) return BRX_ERR_INVALID_ARGUMENT;
+  if (G.n_poly > 0) {
+    if (!G.poly_tet_offset || G.poly_tet_offset[0] != 0 || G.poly_tet_offset[G.n_poly] != G.n_tets)
+      return BRX_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < G.n_poly; ++i)
+      if (G.poly_tet_offset[i + 1] < G.poly_tet_offset[i]) return BRX_ERR_INVALID_ARGUMENT;
+  }
+  for (long long i = 0; i < 4LL * G.n_tets; ++i)
+    if (G.tet_vertices[i] < 0 || G.tet_vertices[i] >= G.n_vertices) return BRX_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < G.n_ops; ++i)
+    if (G.op_inverse[i] < 0 || G.op_inverse[i] >= G.n_ops) return BRX_ERR_INVALID_ARGUMENT;
+  if (G.n_atoms > 0) {
+    for (long long i = 0; i < (long long)G.n_atoms * G.n_ops; ++i)
+      if (G.gamma_F0[i] < 0 || G.gamma_F0[i] >= G.n_atoms || G.gamma_vidx[i] < 0 || G.gamma_vidx[i] >= G.n_gamma_vectors)
+        return BRX_ERR_INVALID_ARGUMENT;
+  }
+
+  brx_handle* h = new (std::nothrow) brx_handle();
+  if (!h) return BRX_ERR_OUT_OF_MEMORY;
+  h->device = device;
+  h->host_geom = G;
+  auto bail = [&](brx_status st) {
+    brx_destroy(h);
+    return st;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(BRX_ERR_CUDA);
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bail(BRX_ERR_CUDA);
+  h->num_sms = prop.multiProcessorCount;
+  h->smem_optin = prop.sharedMemPerBlockOptin;
+  h->tables.reserve(64);
+  DevGeom& g = h->g;
+  std::memcpy(g.outer_B, G.outer_B, sizeof g.outer_B);
+  std::memcpy(g.prim_B, G.prim_B, sizeof g.prim_B);
+  std::memcpy(g.to_prim_6Pt, G.to_prim_6Pt, sizeof g.to_prim_6Pt);
+  std::memcpy(g.from_prim_invPt, G.from_prim_invPt, sizeof g.from_prim_invPt);
+  g.is_primitive = G.is_primitive;
+  g.n_faces = G.n_faces;
+  g.n_wedge = G.n_wedge;
+  g.wedge_le_ge = G.wedge_le_ge;
+  g.n_ops = G.n_ops;
+  g.identity = G.identity;
+  g.n_nodes = G.n_nodes;
+  g.n_atoms = G.n_atoms;
+  g.t_main = make_tol(G.float_tolerance, G.digit);
+  g.t_def = make_tol(0.0, 1);
+  brx_status st = BRX_OK;
+#define UP(src, cnt, dst) \
+  if ((st = upload(h, src, (size_t)(cnt), &dst)) != BRX_OK) return bail(st)
+  UP(G.face_abc, 9 * G.n_faces, g.face_abc);
+  UP(G.face_normal, 3 * G.n_faces, g.face_normal);
+  UP(G.face_tau, 3 * G.n_faces, g.face_tau);
+  UP(G.face_tau_len, G.n_faces, g.face_tau_len);
+  UP(G.wedge_normal, 3 * G.n_wedge, g.wedge_normal);
+  UP(G.ops, 9 * G.n_ops, g.ops);
+  UP(G.op_inverse, G.n_ops, g.op_inverse);
+  for (int d = 0; d < 3; ++d) {
+    g.n_knots[d] = G.n_knots[d];
+    UP(G.knots[d], G.n_knots[d], g.knots[d]);
+  }
+  UP(G.node_type, G.n_nodes, g.node_type);
+  UP(G.node_index, G.n_nodes, g.node_index);
+  UP(G.cube_vertices, 8LL * G.n_cube, g.cube_vertices);
+  UP(G.poly_tet_offset, G.n_poly + 1, g.poly_tet_offset);
+  UP(G.tet_vertices, 4LL * G.n_tets, g.tet_vertices);
+  UP(G.tet_sphere, 4LL * G.n_tets, g.tet_sphere);
+  UP(G.tet_volume, G.n_tets, g.tet_volume);
+  UP(G.vertex_xyz, 3LL * G.n_vertices, g.vertex_xyz);
+  UP(G.gamma_F0, (long long)G.n_atoms * G.n_ops, g.gamma_F0);
+  UP(G.gamma_vidx, (long long)G.n_atoms * G.n_ops, g.gamma_vidx);
+  UP(G.gamma_vectors, 3LL * G.n_gamma_vectors, g.gamma_vectors);
+  // Cartesian rotations L·W·L⁻¹ (src/interpolator.hpp:413-419)
+  h->rot_cart.resize(9 * (size_t)G.n_ops);
+  for (int j = 0; j < G.n_ops; ++j) {
+    double W[9], t[9];
+    for (int e = 0; e < 9; ++e) W[e] = (double)G.ops[9 * j + e];
+    mm3(t, G.lattice_to_xyz, W);
+    mm3(&h->rot_cart[9 * (size_t)j], t, G.lattice_from_xyz);
+  }
+  UP(h->rot_cart.data(), h->rot_cart.size(), g.rot_cart);
+#undef UP
+  // the host copy keeps only counts: no pointer into caller memory survives
+  h->host_geom.face_abc = h->host_geom.face_normal = h->host_geom.face_tau_len = nullptr;
+  h->host_geom.face_tau = nullptr;
+  h->host_geom.wedge_normal = h->host_geom.tet_sphere = h->host_geom.tet_volume = nullptr;
+  h->host_geom.vertex_xyz = h->host_geom.gamma_vectors = nullptr;
+  h->host_geom.ops = h->host_geom.op_inverse = h->host_geom.node_type = h->host_geom.node_index = nullptr;
+  h->host_geom.cube_vertices = h->host_geom.poly_tet_offset = h->host_geom.tet_vertices = nullptr;
+  h->host_geom.gamma_F0 = h->host_geom.gamma_vidx = nullptr;
+  for (int d = 0; d < 3; ++d) h->host_geom.knots[d] = nullptr;
+  for (auto& s : h->sc) {
+    if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess) return bail(BRX_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) return bail(BRX_ERR_CUDA);
+  }
+  if (cudaMalloc(&h->err, sizeof(ErrorWord)) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
+  if (cudaHostAlloc(&h->err_host, sizeof(ErrorWord), cudaHostAllocDefault) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
+  *out = h;
+  return BRX_OK;
+}
+
+void brx_destroy(brx_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  for (auto& s : h->sc) {
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    s.rec.release();
+    s.sortbuf.release();
+    s.qbuf.release();
+    s.vbuf.release();
+    s.cbuf.release();
+    if (s.done) cudaEventDestroy(s.done);
+    if (s.stream) cudaStreamDestroy(s.stream);
+  }
+  for (auto& b : h->tables) b.release();
+  for (auto e : h->ev_pool) cudaEventDestroy(e);
+  h->vals.data.release();
+  h->vecs.data.release();
+  h->perm_keys.release();
+  h->perm_ids.release();
+  h->perms.release();
+  if (h->err) cudaFree(h->err);
+  if (h->err_host) cudaFreeHost(h->err_host);
+  delete h;
+}
+
+static brx_status fill_one(brx_handle* h, const brx_data* d, Interp& dst, int storage) {
+  if (!d) { dst.present = false; return BRX_OK; }
+  if (!d->data || d->n_branches < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "data must be non-empty");
+  if (d->dtype != BRX_F64 && d->dtype != BRX_C128) return fail(h, BRX_ERR_INVALID_ARGUMENT, "data must be float64 or complex128");
+  for (int i = 0; i < 3; ++i)
+    if (d->elements[i] < 0) return fail(h, BRX_ERR_INVALID_ARGUMENT, "negative element count");
+  if (d->elements[1] % 3 || d->elements[2] % 9)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "vector elements must be a multiple of 3 and matrix elements of 9");
+  const int s = d->elements[0] + d->elements[1] + d->elements[2];
+  if (s < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "each branch needs at least one element");
+  if (s > 32 * 24) return fail(h, BRX_ERR_INVALID_ARGUMENT, "more than 768 elements per branch are not supported");
+  dst.present = true;
+  dst.cplx = d->dtype == BRX_C128;
+  dst.B = d->n_branches;
+  dst.s = s;
+  for (int i = 0; i < 3; ++i) dst.el[i] = d->elements[i];
+  dst.rotates_like = d->rotates_like;
+  dst.length_unit = d->length_unit;
+  const size_t count = (size_t)h->host_geom.n_vertices * dst.B * s * (dst.cplx ? 2 : 1);  // reals
+  const bool src_host = host_ptr(d->data);
+  std::vector<double> tmp;
+  const double* src = static_cast<const double*>(d->data);
+  if (!src_host) {
+    tmp.resize(count);
+    BRX_CUDA(h, cudaMemcpy(tmp.data(), d->data, sizeof(double) * count, cudaMemcpyDeviceToHost));
+    src = tmp.data();
+  }
+  dst.store = storage == BRX_STORE_F64 ? ST_F64 : (storage == BRX_STORE_F32 ? ST_F32 : ST_BF16);
+  if (storage == BRX_STORE_F64) {
+    BRX_CUDA(h, dst.data.ensure(sizeof(double) * count));
+    BRX_CUDA(h, cudaMemcpy(dst.data.p, src, sizeof(double) * count, cudaMemcpyHostToDevice));
+  } else if (storage == BRX_STORE_F32) {
+    std::vector<float> f(count);
+    for (size_t i = 0; i < count; ++i) f[i] = (float)src[i];
+    BRX_CUDA(h, dst.data.ensure(sizeof(float) * count));
+    BRX_CUDA(h, cudaMemcpy(dst.data.p, f.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+  } else {
+    std::vector<__nv_bfloat16> f(count);
+    for (size_t i = 0; i < count; ++i) f[i] = __float2bfloat16_rn((float)src[i]);
+    BRX_CUDA(h, dst.data.ensure(sizeof(__nv_bfloat16) * count));
+    BRX_CUDA(h, cudaMemcpy(dst.data.p, f.data(), sizeof(__nv_bfloat16) * count, cudaMemcpyHostToDevice));
+  }
+  return BRX_OK;
+}
+
+brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vectors, int32_t storage) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!values) return fail(h, BRX_ERR_INVALID_ARGUMENT, "values must be provided");
+  if (storage < BRX_STORE_F64 || storage > BRX_STORE_BF16) return fail(h, BRX_ERR_INVALID_ARGUMENT, "unknown storage");
+  if (vectors && vectors->n_branches != values->n_branches)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "The values and vectors must have matching number of points and branches");
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  h->filled = false;
+  // bfloat16 storage applies to the eigenvectors; eigenvalues keep float32
+  brx_status st = fill_one(h, values, h->vals, storage == BRX_STORE_BF16 ? BRX_STORE_F32 : storage);
+  if (st) return st;
+  st = fill_one(h, vectors, h->vecs, storage);
+  if (st) return st;
+  h->storage = storage;
+  h->filled = true;
+  // new data invalidates any permutation table (DualInterpolator::replace_data)
+  h->n_keys = 0;
+  h->n_perms = 0;
+  return BRX_OK;
+}
+
+brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* keys, const int32_t* perm_ids,
+                                int32_t n_perms, const int32_t* perms) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!h->filled) return fail(h, BRX_ERR_NOT_FILLED, "The interpolation data must be filled before setting permutations.");
+  if (n_keys < 0 || n_perms < 0 || (n_keys > 0 && (!keys || !perm_ids || !perms || n_perms < 1)))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "invalid permutation table");
+  const int B = h->vals.B;
+  for (long long i = 0; i < n_keys; ++i) {
+    if (i && keys[i] <= keys[i - 1]) return fail(h, BRX_ERR_INVALID_ARGUMENT, "permutation keys must be strictly increasing");
+    if (perm_ids[i] < 0 || perm_ids[i] >= n_perms) return fail(h, BRX_ERR_INVALID_ARGUMENT, "permutation id out of range");
+  }
+  for (long long i = 0; i < (long long)n_perms * B; ++i)
+    if (perms[i] < 0 || perms[i] >= B) return fail(h, BRX_ERR_INVALID_ARGUMENT, "permutation entry out of range");
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  h->n_keys = 0;
+  h->n_perms = 0;
+  if (n_keys == 0) return BRX_OK;
+  BRX_CUDA(h, h->perm_keys.ensure(sizeof(int64_t) * n_keys));
+  BRX_CUDA(h, h->perm_ids.ensure(sizeof(int32_t) * n_keys));
+  BRX_CUDA(h, h->perms.ensure(sizeof(int32_t) * (size_t)n_perms * B));
+  BRX_CUDA(h, cudaMemcpy(h->perm_keys.p, keys, sizeof(int64_t) * n_keys, cudaMemcpyHostToDevice));
+  BRX_CUDA(h, cudaMemcpy(h->perm_ids.p, perm_ids, sizeof(int32_t) * n_keys, cudaMemcpyHostToDevice));
+  BRX_CUDA(h, cudaMemcpy(h->perms.p, perms, sizeof(int32_t) * (size_t)n_perms * B, cudaMemcpyHostToDevice));
+  h->n_keys = n_keys;
+  h->n_perms = n_perms;
+  return BRX_OK;
+}
+
+brx_status brx_ir_interpolate_at(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out,
+                                 uint32_t flags, void* stream) {
+  return run_query(h, 1, Q, n, values_out, vectors_out, flags, stream, nullptr);
+}
+
+brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out,
+                              uint32_t flags, void* stream) {
+  return run_query(h, 0, Q, n, values_out, vectors_out, flags, stream, nullptr);
+}
+
+brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir, uint32_t flags,
+                      const brx_locate_out* out, void* stream) {
+  if (!h || !out) return BRX_ERR_INVALID_ARGUMENT;
+  if (!out->status) return fail(h, BRX_ERR_INVALID_ARGUMENT, "brx_locate needs a status array");
+  brx_status st = run_query(h, ir ? 1 : 0, Q, n, nullptr, nullptr, flags & ~BRX_FLAG_ASYNC, stream, out);
+  // per-q status is returned in out->status; the call itself succeeds
+  if (st == BRX_ERR_MOVE_FAILED || st == BRX_ERR_OUTSIDE_IR || st == BRX_ERR_NOT_FOUND || st == BRX_ERR_NULL_NODE ||
+      st == BRX_ERR_IMPOSSIBLE)
+    return BRX_OK;
+  return st;
+}
+
+brx_status brx_sync(brx_handle* h, void* stream) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!h->async_pending) return BRX_OK;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->async_stream;
+  BRX_CUDA(h, cudaStreamSynchronize(s));
+  h->async_pending = false;
+  if (h->profile) harvest_events(h);
+  return collect_errors(h, h->async_ir, h->async_Q, h->async_n, false);
+}
+
+const char* brx_last_error(const brx_handle* h) { return h ? h->message.c_str() : "null handle"; }
+
+int64_t brx_launch_count(const brx_handle* h) { return h ? h->launches : 0; }
+
+brx_status brx_profile(brx_handle* h, int32_t enable) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  h->profile = enable != 0;
+  h->ev_used = 0;
+  for (double& x : h->stage_ms) x = 0;
+  h->stage_q = 0;
+  return BRX_OK;
+}
+
+brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count) {
+  if (!h || !ms || n < 0) return BRX_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n && i < 4; ++i) ms[i] = h->stage_ms[i];
+  if (q_count) *q_count = h->stage_q;
+  return BRX_OK;
+}
+
+}  // extern "C"

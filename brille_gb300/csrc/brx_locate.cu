@@ -1,0 +1,372 @@
+// K1+K2: first-zone move, irreducible-wedge search and trellis locate.
+//
+// One thread per q.  The small per-zone tables (faces, wedge normals, point
+// operations) are staged in shared memory once per CTA; trellis tables are
+// read through the read-only path.  All predicates are FP64 (brx_device.cuh).
+//
+// Reference: BrillouinZone::moveinto / part_moveinto_prim
+// (src/bz_move.cpp:14-53, 103-163), ir_moveinto (:257-285),
+// _inside_wedge_outer (src/bz.hpp:757-763), PolyTrellis::node_subscript
+// (src/trellis_poly.hpp:382-434), CubeNode/PolyNode::indices_weights
+// (src/trellis_node.hpp:132-149, 275-364).
+#include "brx_device.cuh"
+#include "brx_kernels.h"
+#include "../../include/brx.h"
+
+namespace brx {
+
+struct SmemZone {
+  double* abc;      // n_faces × 9
+  double* normal;   // n_faces × 3
+  double* tau_len;  // n_faces
+  int32_t* tau;     // n_faces × 3
+  double* wedge;    // n_wedge × 3
+  int32_t* ops;     // n_ops × 9
+  int32_t* opinv;   // n_ops
+};
+
+__device__ bool inside_all_faces(const DevGeom& g, const SmemZone& z, const double x[3]) {
+  double vmin = 0.0;
+  for (int f = 0; f < g.n_faces; ++f) {
+    const double* abc = z.abc + 9 * f;
+    double o = orient3d(abc, abc + 3, abc + 6, x);
+    if (f == 0 || o < vmin) vmin = o;
+  }
+  return vmin > 0 || approx(vmin, 0.0, g.t_main);
+}
+
+// Returns 0 or BRX_ERR_MOVE_FAILED; q_out in conventional r.l.u.
+__device__ int moveinto_one(const DevGeom& g, const SmemZone& z, const double Q[3], double q_out[3],
+                            int32_t tau_out[3]) {
+  double Qp[3], q[3], x[3];
+  int32_t tau[3], last[3];
+  if (g.is_primitive) {
+    for (int i = 0; i < 3; ++i) Qp[i] = Q[i];
+  } else {
+    matvec_i(Qp, g.to_prim_6Pt, Q);
+    for (int i = 0; i < 3; ++i) Qp[i] = __ddiv_rn(Qp[i], 6.0);
+  }
+  for (int i = 0; i < 3; ++i) {
+    tau[i] = (int32_t)round(Qp[i]);
+    q[i] = dsub(Qp[i], (double)tau[i]);
+    last[i] = tau[i];
+  }
+  const int max_count = g.n_faces;
+  int count = 0;
+  for (;;) {
+    if (!(count++ < max_count)) break;
+    hkl_to_xyz(x, g.prim_B, q);
+    if (inside_all_faces(g, z, x)) break;
+    int max_nm = 0, max_at = 0, any_pos = 0;
+    double dmax = 0.0;
+    for (int j = 0; j < g.n_faces; ++j) {
+      double dj = dot3(x, z.normal + 3 * j);
+      int nj = (int)round(__ddiv_rn(dj, z.tau_len[j]));
+      if (nj > 0) any_pos = 1;
+      const int32_t* tj = z.tau + 3 * j;
+      bool back = (tj[0] + last[0]) != 0 || (tj[1] + last[1]) != 0 || (tj[2] + last[2]) != 0;
+      if (nj > 0 && nj >= max_nm && (0 == max_nm || (back && dj > dmax))) {
+        max_at = j;
+        max_nm = nj;
+        dmax = dj;
+      }
+    }
+    if (any_pos) {
+      const int32_t* tj = z.tau + 3 * max_at;
+      for (int i = 0; i < 3; ++i) {
+        q[i] = dsub(q[i], dmul((double)tj[i], (double)max_nm));
+        tau[i] += tj[i] * max_nm;
+        last[i] = tj[i] * max_nm;
+      }
+    }
+  }
+  if (g.is_primitive) {
+    for (int i = 0; i < 3; ++i) { q_out[i] = q[i]; tau_out[i] = tau[i]; }
+  } else {
+    matvec_i(q_out, g.from_prim_invPt, q);
+    for (int i = 0; i < 3; ++i) {
+      long long s = 0;
+      for (int k = 0; k < 3; ++k) s += (long long)g.from_prim_invPt[3 * i + k] * tau[k];
+      tau_out[i] = (int32_t)s;
+    }
+  }
+  hkl_to_xyz(x, g.outer_B, q_out);
+  return inside_all_faces(g, z, x) ? 0 : BRX_ERR_MOVE_FAILED;
+}
+
+__device__ bool inside_wedge(const DevGeom& g, const SmemZone& z, const double x[3]) {
+  if (g.n_wedge == 0) return true;
+  if (g.wedge_le_ge) {
+    bool all_le = true, all_ge = true;
+    for (int i = 0; i < g.n_wedge; ++i) {
+      double d = dot3(z.wedge + 3 * i, x);
+      if (!cmp_le(d, 0.0, g.t_def)) all_le = false;
+      if (!cmp_ge(d, 0.0, g.t_def)) all_ge = false;
+    }
+    return all_le || all_ge;
+  }
+  for (int i = 0; i < g.n_wedge; ++i)
+    if (!cmp_ge(dot3(z.wedge + 3 * i, x), 0.0, g.t_main)) return false;
+  return true;
+}
+
+__device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32_t rot[2]) {
+  double x[3], qj[3];
+  hkl_to_xyz(x, g.outer_B, q);
+  if (inside_wedge(g, z, x)) {
+    rot[0] = rot[1] = g.identity;
+    return 0;
+  }
+  for (int j = 0; j < g.n_ops; ++j) {
+    const int32_t* W = z.ops + 9 * j;
+    int32_t Wt[9] = {W[0], W[3], W[6], W[1], W[4], W[7], W[2], W[5], W[8]};
+    matvec_i(qj, Wt, q);
+    hkl_to_xyz(x, g.outer_B, qj);
+    if (inside_wedge(g, z, x)) {
+      q[0] = qj[0]; q[1] = qj[1]; q[2] = qj[2];
+      rot[1] = j;
+      rot[0] = z.opinv[j];
+      return 0;
+    }
+  }
+  return BRX_ERR_OUTSIDE_IR;
+}
+
+__device__ __forceinline__ int find_bin(const double* e, int n, double x) {
+  int d = n;
+  for (int i = 0; i < n; ++i)
+    if (__ldg(e + i) > x) { d = i; break; }
+  if (d > n - 1 && x < __ldg(e)) d = 0;
+  return d > 0 ? d - 1 : d;
+}
+
+__device__ __forceinline__ int on_boundary(const DevGeom& g, const double* e, int n, double x, int i) {
+  if (i + 2 < n && approx(__ldg(e + i + 1), x, g.t_def)) return 1;
+  if (i > 0 && approx(__ldg(e + i), x, g.t_def)) return -1;
+  return 0;
+}
+
+__device__ __forceinline__ bool sub_ok_not_null(const DevGeom& g, const int s[3]) {
+  for (int d = 0; d < 3; ++d)
+    if (s[d] < 0 || s[d] >= g.n_knots[d] - 1) return false;
+  long long idx = s[0] + (long long)(g.n_knots[0] - 1) * (s[1] + (long long)(g.n_knots[1] - 1) * s[2]);
+  return __ldg(g.node_type + idx) != BRX_NODE_NULL;
+}
+
+__device__ long long node_subscript(const DevGeom& g, const double x[3]) {
+  int sub[3], close[3], ns[3];
+  for (int d = 0; d < 3; ++d) sub[d] = find_bin(g.knots[d], g.n_knots[d], x[d]);
+  bool bad = !sub_ok_not_null(g, sub);
+  if (bad) {
+    int num_close = 0;
+    for (int i = 0; i < 3; ++i) {
+      close[i] = on_boundary(g, g.knots[i], g.n_knots[i], x[i], sub[i]);
+      if (close[i]) ++num_close;
+    }
+    ns[0] = sub[0]; ns[1] = sub[1]; ns[2] = sub[2];
+    if (num_close > 0)
+      for (int i = 0; i < 3 && bad; ++i)
+        if (close[i]) {
+          ns[0] = sub[0]; ns[1] = sub[1]; ns[2] = sub[2];
+          ns[i] += close[i];
+          bad = !sub_ok_not_null(g, ns);
+        }
+    if (bad && num_close > 1)
+      for (int i = 0; i < 3 && bad; ++i)
+        if (close[i])
+          for (int j = 0; j < 3 && bad; ++j)
+            if (close[j]) {
+              ns[0] = sub[0]; ns[1] = sub[1]; ns[2] = sub[2];
+              ns[i] += close[i];
+              ns[j] += close[j];
+              bad = !sub_ok_not_null(g, ns);
+            }
+    if (bad && num_close > 2) {
+      for (int i = 0; i < 3; ++i) ns[i] = sub[i] + close[i];
+      bad = !sub_ok_not_null(g, ns);
+    }
+    if (!bad) { sub[0] = ns[0]; sub[1] = ns[1]; sub[2] = ns[2]; }
+  }
+  for (int d = 0; d < 3; ++d)
+    if (sub[d] < 0 || sub[d] >= g.n_knots[d] - 1) return -1;
+  return sub[0] + (long long)(g.n_knots[0] - 1) * (sub[1] + (long long)(g.n_knots[1] - 1) * sub[2]);
+}
+
+__device__ __forceinline__ void load3(double out[3], const double* p) {
+  out[0] = __ldg(p); out[1] = __ldg(p + 1); out[2] = __ldg(p + 2);
+}
+
+__device__ double tet_contains(const DevGeom& g, long long t, const double x[3], double w[4], bool shortcut) {
+  if (shortcut) {
+    double s[4];
+    const double* sp = g.tet_sphere + 4 * t;
+    s[0] = __ldg(sp); s[1] = __ldg(sp + 1); s[2] = __ldg(sp + 2); s[3] = __ldg(sp + 3);
+    double v0 = dsub(s[0], x[0]), v1 = dsub(s[1], x[1]), v2 = dsub(s[2], x[2]);
+    double d2 = 0.0;
+    d2 = dadd(d2, dmul(v0, v0));
+    d2 = dadd(d2, dmul(v1, v1));
+    d2 = dadd(d2, dmul(v2, v2));
+    double r2 = dmul(s[3], s[3]);
+    if (!(d2 < r2 || approx(d2, r2, g.t_def))) return -d2;
+  }
+  const int32_t* vi = g.tet_vertices + 4 * t;
+  double a[3], b[3], c[3], d[3];
+  load3(a, g.vertex_xyz + 3 * (long long)__ldg(vi));
+  load3(b, g.vertex_xyz + 3 * (long long)__ldg(vi + 1));
+  load3(c, g.vertex_xyz + 3 * (long long)__ldg(vi + 2));
+  load3(d, g.vertex_xyz + 3 * (long long)__ldg(vi + 3));
+  double vol6 = dmul(__ldg(g.tet_volume + t), 6.0);
+  w[0] = __ddiv_rn(orient3d(x, b, c, d), vol6);
+  w[1] = __ddiv_rn(orient3d(a, x, c, d), vol6);
+  w[2] = __ddiv_rn(orient3d(a, b, x, d), vol6);
+  w[3] = __ddiv_rn(orient3d(a, b, c, x), vol6);
+  bool any_neg = false;
+  double mn = w[0];
+  for (int j = 0; j < 4; ++j) {
+    if (w[j] < 0.0 && !approx(w[j], 0.0, g.t_def)) any_neg = true;
+    if (w[j] < mn) mn = w[j];
+  }
+  return any_neg ? mn : 0.0;
+}
+
+// Returns the number of (vertex, weight) pairs, or −status.
+__device__ int node_weights(const DevGeom& g, long long node, const double x[3], int32_t* tet_out,
+                            int32_t vidx[8], double w8[8]) {
+  *tet_out = -1;
+  const int type = __ldg(g.node_type + node);
+  const int32_t ni = __ldg(g.node_index + node);
+  if (type == BRX_NODE_CUBE) {
+    const int32_t* cv = g.cube_vertices + 8 * (long long)ni;
+    int32_t ids[8];
+    for (int i = 0; i < 8; ++i) ids[i] = __ldg(cv + i);
+    double a[3], b[3];
+    load3(a, g.vertex_xyz + 3 * (long long)ids[0]);
+    load3(b, g.vertex_xyz + 3 * (long long)ids[7]);
+    double vol = 1.0;
+    for (int d = 0; d < 3; ++d) vol = dmul(vol, fabs(dsub(a[d], b[d])));
+    int n = 0;
+    for (int i = 0; i < 8; ++i) {
+      double v[3];
+      load3(v, g.vertex_xyz + 3 * (long long)ids[i]);
+      double p = 1.0;
+      for (int d = 0; d < 3; ++d) p = dmul(p, fabs(dsub(x[d], v[d])));
+      double wi = __ddiv_rn(p, vol);
+      if (cmp_gt(wi, 0.0, g.t_def)) { vidx[n] = ids[7 - i]; w8[n] = wi; ++n; }
+    }
+    return n;
+  }
+  if (type == BRX_NODE_POLY) {
+    const int32_t tb = __ldg(g.poly_tet_offset + ni), te = __ldg(g.poly_tet_offset + ni + 1);
+    double w[4] = {0, 0, 0, 0};
+    double best = 0.0;
+    int32_t best_i = -1;
+    for (int32_t t = tb; t < te; ++t) {
+      double mn = tet_contains(g, t, x, w, true);
+      if (mn >= 0.0) {
+        int n = 0;
+        for (int j = 0; j < 4; ++j)
+          if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
+        *tet_out = t;
+        return n;
+      }
+      if (best_i < 0 || mn > best) { best = mn; best_i = t; }
+    }
+    if (best_i < 0) return 0;
+    double val = tet_contains(g, best_i, x, w, false);
+    if (val > 0.0) return -BRX_ERR_IMPOSSIBLE;
+    int n = 0;
+    for (int j = 0; j < 4; ++j)
+      if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)best_i + j); w8[n] = w[j]; ++n; }
+    *tet_out = best_i;
+    return n;
+  }
+  return -BRX_ERR_NULL_NODE;
+}
+
+__device__ __forceinline__ void report(ErrorWord* err, long long i, int st) {
+  atomicOr(&err->flags, 1 << st);
+  atomicAdd(&err->count, 1);
+  atomicMin(&err->first_bad, i + 0LL);
+}
+
+// mode: 0 interpolate_at (moveinto), 1 ir_interpolate_at (ir_moveinto),
+// 2 no move (Q already in the trellis domain)
+__global__ void __launch_bounds__(kLocateThreads)
+locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long base, int mode,
+              Records r, ErrorWord* err) {
+  extern __shared__ double smem_d[];
+  SmemZone z;
+  double* p = smem_d;
+  z.abc = p; p += 9 * g.n_faces;
+  z.normal = p; p += 3 * g.n_faces;
+  z.tau_len = p; p += g.n_faces;
+  z.wedge = p; p += 3 * g.n_wedge;
+  int32_t* ip = reinterpret_cast<int32_t*>(p);
+  z.tau = ip; ip += 3 * g.n_faces;
+  z.ops = ip; ip += 9 * g.n_ops;
+  z.opinv = ip;
+  for (int i = threadIdx.x; i < 9 * g.n_faces; i += blockDim.x) z.abc[i] = g.face_abc[i];
+  for (int i = threadIdx.x; i < 3 * g.n_faces; i += blockDim.x) {
+    z.normal[i] = g.face_normal[i];
+    z.tau[i] = g.face_tau[i];
+  }
+  for (int i = threadIdx.x; i < g.n_faces; i += blockDim.x) z.tau_len[i] = g.face_tau_len[i];
+  for (int i = threadIdx.x; i < 3 * g.n_wedge; i += blockDim.x) z.wedge[i] = g.wedge_normal[i];
+  for (int i = threadIdx.x; i < 9 * g.n_ops; i += blockDim.x) z.ops[i] = g.ops[i];
+  for (int i = threadIdx.x; i < g.n_ops; i += blockDim.x) z.opinv[i] = g.op_inverse[i];
+  __syncthreads();
+
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double Qi[3] = {Q[3 * i], Q[3 * i + 1], Q[3 * i + 2]};
+    double q[3];
+    int32_t tau[3] = {0, 0, 0}, rot[2] = {g.identity, g.identity};
+    int st = 0;
+    if (mode == 2) {
+      q[0] = Qi[0]; q[1] = Qi[1]; q[2] = Qi[2];
+    } else {
+      st = moveinto_one(g, z, Qi, q, tau);
+      if (!st && mode == 1) st = wedge_one(g, z, q, rot);
+    }
+    int32_t nt[2] = {-1, -1}, vi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int nw = 0;
+    if (!st) {
+      double x[3];
+      hkl_to_xyz(x, g.outer_B, q);
+      long long node = node_subscript(g, x);
+      nt[0] = (int32_t)node;
+      if (node < 0) {
+        st = BRX_ERR_NOT_FOUND;
+      } else {
+        int k = node_weights(g, node, x, &nt[1], vi, w);
+        if (k > 0) nw = k;
+        else st = (k == 0) ? BRX_ERR_NOT_FOUND : -k;
+      }
+    }
+    r.q_ir[3 * i] = q[0]; r.q_ir[3 * i + 1] = q[1]; r.q_ir[3 * i + 2] = q[2];
+    if (r.tau) { r.tau[3 * i] = tau[0]; r.tau[3 * i + 1] = tau[1]; r.tau[3 * i + 2] = tau[2]; }
+    r.rot[2 * i] = rot[0]; r.rot[2 * i + 1] = rot[1];
+    r.node[2 * i] = nt[0]; r.node[2 * i + 1] = nt[1];
+    r.nw[i] = nw;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = vi[k]; r.w[8 * i + k] = w[k]; }
+    r.status[i] = st;
+    if (st) report(err, base + i, st);
+  }
+}
+
+size_t locate_smem_bytes(const DevGeom& g) {
+  return sizeof(double) * (13 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge) +
+         sizeof(int32_t) * (3 * (size_t)g.n_faces + 10 * (size_t)g.n_ops) + 16;
+}
+
+void launch_locate(const DevGeom& g, const double* Q, long long n, long long base, int mode, const Records& r,
+                   ErrorWord* err, int num_sms, cudaStream_t s) {
+  if (n <= 0) return;
+  long long blocks = (n + kLocateThreads - 1) / kLocateThreads;
+  long long cap = (long long)num_sms * 8;
+  if (blocks > cap) blocks = cap;
+  locate_kernel<<<(unsigned)blocks, kLocateThreads, locate_smem_bytes(g), s>>>(g, Q, n, base, mode, r, err);
+}
+
+}  // namespace brx

@@ -1,0 +1,299 @@
+"""BZTrellisQdd / BZTrellisQdc / BZTrellisQcc on one GB300.
+
+Mirrors the reference's pybind11 grid surface (wrap/_trellis.hpp:27-101,
+wrap/_common_grid.hpp:21-440): construction from a BrillouinZone and a
+maximum node volume, ``fill``, ``ir_interpolate_at`` and ``interpolate_at``
+with the same argument meaning, output shapes and error messages
+(raised as RuntimeError).  Queries run through libbrx.so (the C ABI in
+include/brx.h); ``useparallel``/``threads`` are accepted for compatibility
+and have no effect on the GPU.
+
+Additions, all keyword-only: ``storage`` on fill ("f64" as given, "f32",
+"bf16" for the vertex data kept on the device) and ``out_f32`` on the queries
+(float32 / complex64 results).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._lib import BrxError, check, load
+from .bz import BrillouinZone
+from .tables import geometry_tables
+from .trellis import TrellisBuild
+
+_STORAGE = {"f64": _abi.BRX_STORE_F64, "f32": _abi.BRX_STORE_F32, "bf16": _abi.BRX_STORE_BF16}
+
+
+def _elements(arr, el):
+    """Decode an elements vector and the data shape as the reference's
+    fill_check / Interpolator::check_elements do (wrap/_interpolator.hpp:13-110,
+    src/interpolator.hpp:547-586).  Returns (B, [scalars, vector elems,
+    matrix elems], rotates_like, length_unit)."""
+    el = np.asarray(el).astype(np.int64).ravel()
+    e = [int(el[i]) if i < el.size else 0 for i in range(3)]
+    rot = int(el[3]) if el.size > 3 else 0
+    lu = int(el[4]) if el.size > 4 else 3
+    if rot not in (0, 1, 2):
+        raise RuntimeError(f"Unknown RotatesLike value {rot}")
+    if lu not in (0, 1, 2, 3, 4):
+        raise RuntimeError(f"Unknown LengthUnit value {lu}")
+    shape = arr.shape
+    x = sum(e)
+    if arr.ndim == 1:
+        if x == 0:
+            e[0] = x = 1
+        if x > 1:
+            raise RuntimeError("1-D data must represent one scalar per point!")
+        B = 1
+    elif arr.ndim == 2:
+        if x == 0:
+            e[0] = x = shape[1]
+        if shape[1] % x:
+            raise RuntimeError("2-D data requires an integer number of branches!")
+        B = shape[1] // x
+    elif arr.ndim == 3:
+        if x == 0:
+            e[0] = x = shape[2]
+        if shape[2] != x:
+            raise RuntimeError("3-D data requires that the last dimension matches the specified number of elements!")
+        B = shape[1]
+    elif arr.ndim == 4:
+        if shape[3] != 3:
+            raise RuntimeError("4-D data can only be 3-vectors")
+        if x == 0:
+            e[1] = x = shape[2] * 3
+        if shape[2] * 3 != x:
+            raise RuntimeError("4-D data requires that the last two dimensions match the specified number of vector elements!")
+        B = shape[1]
+    elif arr.ndim == 5:
+        if shape[3] != 3 or shape[4] != 3:
+            raise RuntimeError("5-D data can only be matrices")
+        if x == 0:
+            e[2] = x = shape[2] * 9
+        if shape[2] * 9 != x:
+            raise RuntimeError("5-D data requires the last three dimensions match the specified number of matrix elements!")
+        B = shape[1]
+    else:
+        raise RuntimeError("Interpolator data is expected to be 1- to 5-D")
+    return B, e, rot, lu
+
+
+def _ptr(obj):
+    """Address of a numpy array or of an object with data_ptr() (torch)."""
+    if obj is None:
+        return None
+    if hasattr(obj, "data_ptr"):
+        return obj.data_ptr()
+    return obj.ctypes.data
+
+
+class _Grid:
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = True
+
+    def __init__(self, bz: BrillouinZone, max_volume=None, always_triangulate=False, *, trellis=None,
+                 device=0, float_tolerance=1e-12, digit=1000):
+        if trellis is None:
+            if max_volume is None:
+                raise ValueError("max_volume is required")
+            trellis = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, max_volume, always_triangulate)
+        self.bz = bz
+        self.trellis = trellis
+        self.tables = geometry_tables(bz, trellis, gamma=True, float_tolerance=float_tolerance, digit=digit)
+        self._geom = _abi.GeometryHolder(self.tables)
+        self.device = device
+        self._h = None
+        self._fill = None
+
+    # ------------------------------------------------------------ accessors
+    @property
+    def invA(self):
+        return self.trellis.vertices.copy()
+
+    @property
+    def rlu(self):
+        return self.trellis.vertices @ np.linalg.inv(self.bz.lattice.B)
+
+    @property
+    def vertices(self):
+        return self.rlu
+
+    @property
+    def tetrahedra(self):
+        return self.trellis.tet_vertices.copy()
+
+    @property
+    def values(self):
+        return None if self._fill is None else self._fill["values"]
+
+    @property
+    def vectors(self):
+        return None if self._fill is None else self._fill["vectors"]
+
+    # --------------------------------------------------------------- handle
+    def _handle(self):
+        if self._h is None:
+            lib = load()
+            h = C.c_void_p()
+            st = lib.brx_create(C.byref(self._geom.struct), self.device, C.byref(h))
+            if st != 0:
+                raise BrxError(st, f"brx_create failed with status {st}")
+            self._h = h
+        return self._h
+
+    def __del__(self):
+        try:
+            if self._h is not None:
+                load().brx_destroy(self._h)
+        except Exception:
+            pass
+
+    # ----------------------------------------------------------------- fill
+    def fill(self, values, values_elements, *args, storage="f64"):
+        """fill(values, values_elements[, values_weights], vectors,
+        vectors_elements[, vectors_weights][, sort])
+        (wrap/_common_grid.hpp:26-47, 127-147)."""
+        values_weights = vectors_weights = (1.0, 1.0, 1.0)
+        vectors = vectors_elements = None
+        if len(args) >= 4:
+            values_weights, vectors, vectors_elements, vectors_weights = args[:4]
+            rest = args[4:]
+        elif len(args) >= 2:
+            vectors, vectors_elements = args[:2]
+            rest = args[2:]
+        elif len(args) == 0:
+            rest = ()
+        else:
+            raise TypeError("fill() takes values and vectors with their element specifications")
+        sort = bool(rest[0]) if rest else False
+        if sort:
+            raise NotImplementedError("mode sorting on fill is not implemented; supply a permutation table "
+                                      "with set_permutations()")
+        vdt = np.complex128 if self.VALUE_COMPLEX else np.float64
+        cdt = np.complex128 if self.VECTOR_COMPLEX else np.float64
+        vals = np.ascontiguousarray(np.asarray(values), dtype=vdt)
+        nv = self.trellis.vertices.shape[0]
+        if vals.shape[0] != nv:
+            raise RuntimeError(f"Provided {vals.shape[0]} arrays but {nv} were expected!")
+        Bv, ev, rv, lv = _elements(vals, values_elements)
+        vd, vkeep = _abi.make_data(vals.reshape(nv, -1), Bv, ev, rv, lv)
+        cd = ckeep = None
+        Bc = ev_c = None
+        if vectors is not None:
+            vecs = np.ascontiguousarray(np.asarray(vectors), dtype=cdt)
+            if vecs.shape[0] != nv:
+                raise RuntimeError(f"Provided {vecs.shape[0]} arrays but {nv} were expected!")
+            Bc, ev_c, rc, lc = _elements(vecs, vectors_elements)
+            if Bc != Bv:
+                raise RuntimeError("The values and vectors must have matching number of points and branches")
+            cd, ckeep = _abi.make_data(vecs.reshape(nv, -1), Bc, ev_c, rc, lc)
+        h = self._handle()
+        st = load().brx_fill(h, C.byref(vd), C.byref(cd) if cd is not None else None, _STORAGE[storage])
+        check(st, h)
+        self._fill = dict(values=vals, vectors=None if vectors is None else np.asarray(vectors),
+                          vshape=vals.shape[1:], cshape=None if vectors is None else np.shape(vectors)[1:],
+                          vdtype=vdt, cdtype=cdt, values_weights=values_weights, vectors_weights=vectors_weights,
+                          storage=storage)
+        return True
+
+    def set_permutations(self, keys, perm_ids, perms):
+        """Mode permutations per vertex pair (keys i*n_vertices+j, sorted)."""
+        keys = np.ascontiguousarray(keys, np.int64)
+        ids = np.ascontiguousarray(perm_ids, np.int32)
+        perms = np.ascontiguousarray(perms, np.int32)
+        h = self._handle()
+        check(load().brx_set_permutations(h, keys.size, keys.ctypes.data, ids.ctypes.data,
+                                          perms.shape[0] if perms.ndim == 2 else 0, perms.ctypes.data), h)
+
+    # -------------------------------------------------------------- queries
+    def _query(self, ir, Q, do_not_move_points=False, out_f32=False):
+        if self._fill is None:
+            raise RuntimeError("The interpolation data must be filled before interpolating.")
+        Q = np.ascontiguousarray(np.asarray(Q, dtype=np.float64))
+        if Q.ndim != 2 or Q.shape[1] != 3:
+            raise RuntimeError("Only (n,3) two-dimensional Q vectors supported in interpolating.")
+        n = Q.shape[0]
+        f = self._fill
+        vdt = np.complex64 if (out_f32 and f["vdtype"] == np.complex128) else (np.float32 if out_f32 else f["vdtype"])
+        cdt = np.complex64 if (out_f32 and f["cdtype"] == np.complex128) else (np.float32 if out_f32 else f["cdtype"])
+        vals = np.empty((n,) + tuple(f["vshape"]), dtype=vdt)
+        vecs = np.empty((n,) + tuple(f["cshape"]), dtype=cdt) if f["cshape"] is not None else None
+        flags = (_abi.BRX_FLAG_NO_MOVE if do_not_move_points else 0) | (_abi.BRX_FLAG_OUT_F32 if out_f32 else 0)
+        fn = load().brx_ir_interpolate_at if ir else load().brx_interpolate_at
+        h = self._handle()
+        st = fn(h, Q.ctypes.data, n, vals.ctypes.data, vecs.ctypes.data if vecs is not None else None, flags, None)
+        check(st, h)
+        return vals, vecs
+
+    def ir_interpolate_at(self, Q, useparallel=False, threads=-1, do_not_move_points=False, *, out_f32=False):
+        """(wrap/_common_grid.hpp:276-300; src/bz_trellis.hpp:155-196)"""
+        return self._query(True, Q, do_not_move_points, out_f32)
+
+    def interpolate_at(self, Q, useparallel=False, threads=-1, do_not_move_points=False, *, out_f32=False):
+        """(wrap/_common_grid.hpp:412-440; src/bz_trellis.hpp:113-129)"""
+        return self._query(False, Q, do_not_move_points, out_f32)
+
+    def query_into(self, Q, n, values_out, vectors_out, *, ir=True, out_f32=False, no_move=False,
+                   async_=False, stream=None):
+        """Raw query on caller-owned buffers (numpy arrays, torch tensors or
+        integer addresses; host or device).  Returns nothing; raises on error."""
+        flags = ((_abi.BRX_FLAG_NO_MOVE if no_move else 0) | (_abi.BRX_FLAG_OUT_F32 if out_f32 else 0) |
+                 (_abi.BRX_FLAG_ASYNC if async_ else 0))
+        fn = load().brx_ir_interpolate_at if ir else load().brx_interpolate_at
+        h = self._handle()
+        addr = lambda o: o if isinstance(o, int) else _ptr(o)  # noqa: E731
+        st = fn(h, addr(Q), int(n), addr(values_out), addr(vectors_out) if vectors_out is not None else None, flags,
+                stream)
+        check(st, h)
+
+    def sync(self, stream=None):
+        h = self._handle()
+        check(load().brx_sync(h, stream), h)
+
+    def locate(self, Q, ir=True, do_not_move_points=False):
+        """Every intermediate index of the locate stages (for parity checks)."""
+        Q = np.ascontiguousarray(np.asarray(Q, dtype=np.float64).reshape(-1, 3))
+        n = Q.shape[0]
+        out = dict(q_ir=np.zeros((n, 3)), tau=np.zeros((n, 3), np.int32), rot=np.zeros((n, 2), np.int32),
+                   node=np.zeros((n, 2), np.int32), n_weights=np.zeros(n, np.int32),
+                   vertex=np.zeros((n, 8), np.int32), weight=np.zeros((n, 8)), status=np.zeros(n, np.int32))
+        lo = _abi.LocateOut()
+        for k, v in out.items():
+            setattr(lo, k, v.ctypes.data_as(type(getattr(lo, k))))
+        h = self._handle()
+        flags = _abi.BRX_FLAG_NO_MOVE if do_not_move_points else 0
+        check(load().brx_locate(h, Q.ctypes.data, n, 1 if ir else 0, flags, C.byref(lo), None), h)
+        return out
+
+    def profile(self, enable=True):
+        h = self._handle()
+        check(load().brx_profile(h, 1 if enable else 0), h)
+
+    def stage_times(self):
+        """(ms per stage: locate, sort, values gather, vectors gather; q count)."""
+        ms = (C.c_double * 4)()
+        q = C.c_int64()
+        h = self._handle()
+        check(load().brx_stage_times(h, ms, 4, C.byref(q)), h)
+        return list(ms), int(q.value)
+
+    def launch_count(self):
+        return int(load().brx_launch_count(self._handle()))
+
+
+class BZTrellisQdd(_Grid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = False
+
+
+class BZTrellisQdc(_Grid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = True
+
+
+class BZTrellisQcc(_Grid):
+    VALUE_COMPLEX = True
+    VECTOR_COMPLEX = True

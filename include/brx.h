@@ -58,7 +58,7 @@ enum { BRX_F64 = 0, BRX_C128 = 1, BRX_F32 = 2, BRX_C64 = 3, BRX_BF16 = 4 };
 /* Storage precision of vertex data on the device (brx_fill). */
 enum { BRX_STORE_F64 = 0,  /* as given: float64 / complex128, FP64 arithmetic */
        BRX_STORE_F32 = 1,  /* float32 / complex64, FP32 arithmetic           */
-       BRX_STORE_BF16 = 2  /* bfloat16 (pairs for complex), FP32 arithmetic  */ };
+       BRX_STORE_BF16 = 2  /* eigenvectors as bfloat16 pairs, eigenvalues float32; FP32 arithmetic */ };
 
 /* Query flags (brx_ir_interpolate_at / brx_interpolate_at). */
 #define BRX_FLAG_NO_MOVE   0x1u  /* do_not_move_points: Q already irreducible / in the first zone */
@@ -198,6 +198,14 @@ const char* brx_last_error(const brx_handle* h);
 
 /* Number of kernel launches this handle has issued since creation. */
 int64_t brx_launch_count(const brx_handle* h);
+
+/* Stage timing with CUDA events on the launching stream: enable (1) or
+ * disable (0); either call clears the accumulated times. */
+brx_status brx_profile(brx_handle* h, int32_t enable);
+
+/* Milliseconds spent, since brx_profile, in the stages locate, node sort,
+ * values gather and vectors gather (ms[0..3]), and the q count they covered. */
+brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count);
 
 int32_t brx_abi_version(void);
 

@@ -454,17 +454,29 @@ static void gather_one(const brx_data* d, const orc_perm* perm, int64_t nv, int 
  * interpolator_real.tpp:19-64, interpolator_recip.tpp:19-64,
  * interpolator_axial.tpp:19-68, interpolator_gamma.tpp:49-139)
  * ------------------------------------------------------------------------- */
+/* Γ-rotated 3×3 tensors: the reference takes Nmat = ⌊√n⌋/3 for n matrices
+ * and rotates nothing at all unless n == 9·Nmat² (interpolator_gamma.tpp:
+ * 62-68); when n == 9·Nmat² it rotates only Nmat² of the n blocks and copies
+ * the rest from an uninitialised buffer.  That case is rejected here. */
+static int gamma_matrices_ill_defined(const brx_data* d) {
+  int nmat = d->elements[2] / 9;
+  int Nmat = (int)sqrt((double)nmat) / 3;
+  return nmat > 0 && nmat == 9 * Nmat * Nmat;
+}
+
 /* status of a (RotatesLike, LengthUnit, complex) combination */
 int orc_rotation_supported(const brx_data* d) {
   int cplx = d->dtype == BRX_C128;
   switch (d->length_unit) {
     case BRX_LU_REAL_LATTICE:
       if (d->rotates_like == BRX_ROT_GAMMA && !cplx) return BRX_ERR_UNSUPPORTED;
+      if (d->rotates_like == BRX_ROT_GAMMA && gamma_matrices_ill_defined(d)) return BRX_ERR_UNSUPPORTED;
       return (d->rotates_like >= 0 && d->rotates_like <= 2) ? BRX_OK : BRX_ERR_UNSUPPORTED;
     case BRX_LU_RECIPROCAL_LATTICE:
       return d->rotates_like == BRX_ROT_VECTOR ? BRX_OK : BRX_ERR_UNSUPPORTED;
     case BRX_LU_ANGSTROM:
       if (d->rotates_like != BRX_ROT_GAMMA) return BRX_ERR_UNSUPPORTED;
+      if (gamma_matrices_ill_defined(d)) return BRX_ERR_UNSUPPORTED;
       return cplx ? BRX_OK : BRX_ERR_UNSUPPORTED;
     default:
       return BRX_ERR_UNSUPPORTED;
@@ -547,30 +559,6 @@ static void rotate_one(const brx_geometry* g, const brx_data* d, const double q_
         }
         memcpy(xb + o0 * 2, tmp, sizeof(double) * 2 * 3 * nvec);
       }
-      if (nmat > 0) {
-        for (int n = 0; n < Nmat; ++n) {
-          const double* dn = g->gamma_vectors + 3 * g->gamma_vidx[n * g->n_ops + Rii];
-          double dq = 0.0;
-          for (int c = 0; c < 3; ++c) dq += q_ir[c] * dn[c];
-          double rr = cos(TWO_PI * dq), ri = sin(TWO_PI * dq);
-          int v = g->gamma_F0[n * g->n_ops + Rii];
-          for (int m = 0; m < Nmat; ++m) {
-            const double* dm = g->gamma_vectors + 3 * g->gamma_vidx[m * g->n_ops + iRii];
-            double dq2 = 0.0;
-            for (int c = 0; c < 3; ++c) dq2 += q_ir[c] * dm[c];
-            double ir_ = cos(TWO_PI * dq2), ii = sin(TWO_PI * dq2);
-            int k = g->gamma_F0[m * g->n_ops + iRii];
-            mm(t0, xb + (o + 9 * (n * Nmat + m)) * 2, 2, R, 1);
-            mm(t1, Ri, 1, t0, 2);
-            double pr = rr * ir_ - ri * ii, pi = rr * ii + ri * ir_;
-            for (int j = 0; j < 9; ++j) {
-              tmp[((v * Nmat + k) * 9 + j) * 2] = pr * t1[2 * j] - pi * t1[2 * j + 1];
-              tmp[((v * Nmat + k) * 9 + j) * 2 + 1] = pr * t1[2 * j + 1] + pi * t1[2 * j];
-            }
-          }
-        }
-        memcpy(xb + o * 2, tmp, sizeof(double) * 2 * 9 * nmat);
-      }
     }
     return;
   }
@@ -626,6 +614,38 @@ int orc_move(const brx_geometry* g, const double* Q, int64_t n, int ir, double* 
     int st = moveinto_one(g, Q + 3 * i, q + 3 * i, tau + 3 * i);
     if (!st && ir) st = wedge_one(g, q + 3 * i, r2);
     if (rot) { rot[2 * i] = r2[0]; rot[2 * i + 1] = r2[1]; }
+    status[i] = st;
+    if (st && !worst) worst = st;
+  }
+  return worst;
+}
+
+/* move (ir or first zone, or none) then locate, per q, as the GPU's
+ * locate stage does; writes every intermediate index */
+int orc_move_locate(const brx_geometry* g, const double* Q, int64_t n, int ir, int no_move, double* q, int32_t* tau,
+                    int32_t* rot, int32_t* node_tet, int32_t* nw, int32_t* vidx, double* w, int32_t* status) {
+  int worst = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int32_t r2[2] = {g->identity, g->identity};
+    int st = 0;
+    tau[3 * i] = tau[3 * i + 1] = tau[3 * i + 2] = 0;
+    if (no_move) {
+      for (int k = 0; k < 3; ++k) q[3 * i + k] = Q[3 * i + k];
+    } else {
+      st = moveinto_one(g, Q + 3 * i, q + 3 * i, tau + 3 * i);
+      if (!st && ir) st = wedge_one(g, q + 3 * i, r2);
+    }
+    rot[2 * i] = r2[0];
+    rot[2 * i + 1] = r2[1];
+    node_tet[2 * i] = node_tet[2 * i + 1] = -1;
+    nw[i] = 0;
+    for (int k = 0; k < 8; ++k) { vidx[8 * i + k] = 0; w[8 * i + k] = 0.0; }
+    if (!st) {
+      double x[3];
+      hkl_to_xyz(x, g->outer_B, q + 3 * i);
+      int k = locate_one(g, x, node_tet + 2 * i, vidx + 8 * i, w + 8 * i);
+      if (k > 0) nw[i] = k; else st = -k;
+    }
     status[i] = st;
     if (st && !worst) worst = st;
   }

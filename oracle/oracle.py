@@ -44,6 +44,7 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(build())
         _lib.orc_move.restype = C.c_int
+        _lib.orc_move_locate.restype = C.c_int
         _lib.orc_locate.restype = C.c_int
         _lib.orc_interpolate_at.restype = C.c_int
         _lib.orc_rotate.restype = C.c_int
@@ -72,6 +73,18 @@ class Oracle:
         st = np.zeros(n, np.int32)
         lib().orc_move(self.g, _p(Q), C.c_int64(n), C.c_int(int(ir)), _p(q), _p(tau), _p(rot), _p(st))
         return q, tau, rot, st
+
+    def move_locate(self, Q, ir=True, no_move=False):
+        """Every intermediate index of move + locate, as brx_locate returns them."""
+        Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(-1, 3)
+        n = Q.shape[0]
+        out = dict(q_ir=np.zeros((n, 3)), tau=np.zeros((n, 3), np.int32), rot=np.zeros((n, 2), np.int32),
+                   node=np.zeros((n, 2), np.int32), n_weights=np.zeros(n, np.int32),
+                   vertex=np.zeros((n, 8), np.int32), weight=np.zeros((n, 8)), status=np.zeros(n, np.int32))
+        lib().orc_move_locate(self.g, _p(Q), C.c_int64(n), C.c_int(int(ir)), C.c_int(int(no_move)),
+                              _p(out["q_ir"]), _p(out["tau"]), _p(out["rot"]), _p(out["node"]),
+                              _p(out["n_weights"]), _p(out["vertex"]), _p(out["weight"]), _p(out["status"]))
+        return out
 
     def locate(self, xyz, threads=0):
         xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
