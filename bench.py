@@ -36,7 +36,7 @@ sys.path.insert(0, ROOT)
 
 WORKLOADS = {
     # name: (crystal builder, node volume as a fraction of the zone, q half-range)
-    "hex16": ("hexagonal16", 3.2e-7, 2.0),
+    "hex16": ("hexagonal16", 2.4e-7, 2.0),
     "hex16-small": ("hexagonal16", 1e-5, 2.0),
     "diamond8": ("diamond_conventional", 1 / 5000, 1.0),
     "diamond2": ("diamond_primitive", 1 / 5000, 1.0),
@@ -47,7 +47,7 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def build_workload(name, device_modes=True):
+def build_workload(name):
     from brille_gb300 import workloads as W
     from brille_gb300.bz import BrillouinZone
     from brille_gb300.trellis import TrellisBuild
@@ -61,11 +61,9 @@ def build_workload(name, device_modes=True):
     model = W.bvk_for(lat, masses)
     qv = tr.vertices @ np.linalg.inv(lat.B)
     t = time.time()
-    if device_modes:
-        w, v = model.modes_torch(qv)
-    else:
-        w, v = model.modes(qv)
-    log(f"[setup] BvK modes for {len(qv)} vertices in {time.time() - t:.1f}s")
+    procs = min(16, os.cpu_count() or 1)
+    w, v = model.modes(qv, chunk=2048, processes=procs if len(qv) > 8192 else 0)
+    log(f"[setup] BvK modes for {len(qv)} vertices in {time.time() - t:.1f}s ({procs} processes)")
     return dict(name=name, lat=lat, bz=bz, tr=tr, model=model, w=w, v=v, q_range=qr)
 
 
@@ -164,7 +162,7 @@ def cpu_baseline(wl, target_s=12.0, threads=0):
 def run_reference(args, rank):
     if rank != 0:
         return
-    wl = build_workload(args.workload, device_modes=False)
+    wl = build_workload(args.workload)
     vals = []
     import oracle.oracle as orc
     nthreads = orc.Oracle.max_threads()
@@ -233,7 +231,7 @@ def main():
     cdt = torch.complex64 if out_f32 else torch.complex128
     vals = torch.empty((n, B), dtype=fdt, device=dev)
     vecs = torch.empty((n, B, na, 3), dtype=cdt, device=dev)
-    stream = torch.cuda.current_stream(dev)
+    stream = torch.cuda.Stream(dev)
     sp = stream.cuda_stream
 
     def step(i):
@@ -254,8 +252,8 @@ def main():
         for i in range(args.steps):
             step(i)
         ev1.record(stream)
-        torch.cuda.synchronize()
         grid.sync(sp)
+        torch.cuda.synchronize()
     launches = grid.launch_count() - l0
     stage_ms, stage_q = grid.stage_times()
     grid.profile(False)

@@ -59,63 +59,81 @@ class BvKModel:
         self._phi = np.array([t[3] for t in terms])
         self._self = self_term
         self._inv_sqrt_m = 1.0 / np.sqrt(self.masses)
+        # mass-weighted force constants summed per cell translation:
+        # D(q) = Σ_L exp(2πi q·n_L) Ψ_L, Ψ_L a (3n × 3n) matrix
+        cells_used, inv = np.unique(self._nL, axis=0, return_inverse=True)
+        psi = np.zeros((len(cells_used), n, 3, n, 3))
+        for t in range(len(ks)):
+            psi[inv[t], ks[t], :, kps[t], :] += self._phi[t]
+        zero = np.nonzero(np.all(cells_used == 0, axis=1))[0]
+        if len(zero) == 0:
+            cells_used = np.vstack([cells_used, np.zeros(3)])
+            psi = np.concatenate([psi, np.zeros((1, n, 3, n, 3))])
+            zero = [len(cells_used) - 1]
+        for k in range(n):
+            psi[zero[0], k, :, k, :] += self_term[k]
+        sm = self._inv_sqrt_m
+        psi *= sm[None, :, None, None, None] * sm[None, None, None, :, None]
+        self._cells = cells_used
+        self._psi = psi.reshape(len(cells_used), 9 * n * n)
 
     def dynamical_matrix(self, q_rlu):
         """(N, 3n, 3n) Hermitian dynamical matrices at conventional r.l.u. q."""
         q = np.atleast_2d(np.asarray(q_rlu, float))
-        N, n = q.shape[0], self.n_atoms
-        D = np.zeros((N, n, 3, n, 3), complex)
-        ph = np.exp(2j * np.pi * (q @ self._nL.T))  # (N, T)
-        for t in range(len(self._k)):
-            D[:, self._k[t], :, self._kp[t], :] += ph[:, t, None, None] * self._phi[t][None]
-        for k in range(n):
-            D[:, k, :, k, :] += self._self[k][None]
-        s = self._inv_sqrt_m
-        D *= s[None, :, None, None, None] * s[None, None, None, :, None]
-        return D.reshape(N, 3 * n, 3 * n)
+        ph = np.exp(2j * np.pi * (q @ self._cells.T))  # (N, cells)
+        D = ph @ self._psi
+        return D.reshape(len(q), 3 * self.n_atoms, 3 * self.n_atoms)
 
-    def modes(self, q_rlu, chunk=4096):
-        """(ħω meV (N, 3n), eigenvectors (N, 3n, n, 3)) sorted by energy."""
+    def _modes_serial(self, q):
+        n = self.n_atoms
+        D = self.dynamical_matrix(q)
+        D = 0.5 * (D + np.conj(np.swapaxes(D, 1, 2)))
+        lam, vec = np.linalg.eigh(D)
+        w = np.sign(lam) * np.sqrt(np.abs(lam)) * HBAR_OMEGA_MEV
+        v = np.swapaxes(vec, 1, 2).reshape(-1, 3 * n, n, 3)
+        return w, v
+
+    def modes(self, q_rlu, chunk=4096, processes=0):
+        """(ħω meV (N, 3n), eigenvectors (N, 3n, n, 3)) sorted by energy.
+
+        processes > 1 spreads the eigensolves over a spawn-started pool (safe
+        in a process that has already initialised CUDA)."""
         q = np.atleast_2d(np.asarray(q_rlu, float))
         N, n = q.shape[0], self.n_atoms
         w = np.empty((N, 3 * n))
         v = np.empty((N, 3 * n, n, 3), complex)
-        for a in range(0, N, chunk):
-            D = self.dynamical_matrix(q[a:a + chunk])
-            D = 0.5 * (D + np.conj(np.swapaxes(D, 1, 2)))
-            lam, vec = np.linalg.eigh(D)
-            w[a:a + chunk] = np.sign(lam) * np.sqrt(np.abs(lam)) * HBAR_OMEGA_MEV
-            v[a:a + chunk] = np.swapaxes(vec, 1, 2).reshape(-1, 3 * n, n, 3)
+        parts = [(a, min(N, a + chunk)) for a in range(0, N, chunk)]
+        if processes > 1 and len(parts) > 1:
+            import multiprocessing as mp
+            from multiprocessing import shared_memory
+
+            shm_w = shared_memory.SharedMemory(create=True, size=w.nbytes)
+            shm_v = shared_memory.SharedMemory(create=True, size=v.nbytes)
+            try:
+                with mp.get_context("spawn").Pool(processes) as pool:
+                    pool.starmap(_modes_worker, [(self, q[a:b], a, N, shm_w.name, shm_v.name) for a, b in parts])
+                w[:] = np.ndarray(w.shape, w.dtype, buffer=shm_w.buf)
+                v[:] = np.ndarray(v.shape, v.dtype, buffer=shm_v.buf)
+            finally:
+                for s_ in (shm_w, shm_v):
+                    s_.close()
+                    s_.unlink()
+        else:
+            for a, b in parts:
+                w[a:b], v[a:b] = self._modes_serial(q[a:b])
         return w, v
 
-    def modes_torch(self, q_rlu, device="cuda", chunk=65536):
-        """The same on a GPU through torch (FP64 eigh), for large vertex sets."""
-        import torch
 
-        q = torch.as_tensor(np.atleast_2d(q_rlu), dtype=torch.float64, device=device)
-        nL = torch.as_tensor(self._nL, dtype=torch.float64, device=device)
-        phi = torch.as_tensor(self._phi, dtype=torch.complex128, device=device)
-        n = self.n_atoms
-        k = torch.as_tensor(self._k, device=device)
-        kp = torch.as_tensor(self._kp, device=device)
-        selfm = torch.as_tensor(self._self, dtype=torch.complex128, device=device)
-        s = torch.as_tensor(self._inv_sqrt_m, dtype=torch.float64, device=device)
-        scale = (s[:, None, None, None] * s[None, None, :, None]).to(torch.complex128)
-        idx = (k * n + kp)
-        ws, vs = [], []
-        for a in range(0, q.shape[0], chunk):
-            qa = q[a:a + chunk]
-            ph = torch.exp(2j * np.pi * (qa @ nL.T))                       # (M, T)
-            contrib = ph[:, :, None, None] * phi[None]                      # (M, T, 3, 3)
-            D = torch.zeros(qa.shape[0], n * n, 3, 3, dtype=torch.complex128, device=device)
-            D.index_add_(1, idx, contrib)
-            D = D.reshape(-1, n, n, 3, 3)
-            ar = torch.arange(n, device=device)
-            D[:, ar, ar] += selfm[None]
-            D = D.permute(0, 1, 3, 2, 4) * scale[None]
-            D = D.reshape(-1, 3 * n, 3 * n)
-            D = 0.5 * (D + D.conj().transpose(1, 2))
-            lam, vec = torch.linalg.eigh(D)
-            ws.append((torch.sign(lam) * torch.sqrt(lam.abs()) * HBAR_OMEGA_MEV).cpu().numpy())
-            vs.append(vec.transpose(1, 2).reshape(-1, 3 * n, n, 3).cpu().numpy())
-        return np.concatenate(ws), np.concatenate(vs)
+def _modes_worker(model, q, a, N, name_w, name_v):
+    from multiprocessing import shared_memory
+
+    n = model.n_atoms
+    wa, va = model._modes_serial(q)
+    sw = shared_memory.SharedMemory(name=name_w)
+    sv = shared_memory.SharedMemory(name=name_v)
+    try:
+        np.ndarray((N, 3 * n), float, buffer=sw.buf)[a:a + len(q)] = wa
+        np.ndarray((N, 3 * n, n, 3), complex, buffer=sv.buf)[a:a + len(q)] = va
+    finally:
+        sw.close()
+        sv.close()

@@ -60,12 +60,16 @@ struct Interp {
 
 struct Scratch {
   DevBuf rec;     // records
-  DevBuf sortbuf; // counts + cursors
+  DevBuf sortbuf; // counts, offsets, cursors, block sums
+  DevBuf groupbuf;  // work descriptors + their count + queue cursors
   DevBuf qbuf;    // staged Q
   DevBuf vbuf, cbuf;  // staged outputs (host I/O)
   Records r{};
   int32_t* order = nullptr;
-  int32_t* counts = nullptr;
+  int32_t* sort_scratch = nullptr;
+  GroupDesc* groups = nullptr;
+  int32_t* n_groups = nullptr;
+  int32_t* counters = nullptr;  // one work-queue cursor per interpolator
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
 };
@@ -200,7 +204,7 @@ brx_status rotation_mode(const Interp& d, int* mode, std::string* msg) {
 brx_status ensure_scratch(brx_handle* h, long long chunk) {
   if (chunk <= h->scratch_q) return BRX_OK;
   const size_t n = (size_t)chunk;
-  const size_t parts[9] = {24 * n, 64 * n, 12 * n, 8 * n, 8 * n, 4 * n, 32 * n, 4 * n, 4 * n};
+  const size_t parts[10] = {24 * n, 64 * n, 12 * n, 8 * n, 8 * n, 4 * n, 32 * n, 4 * n, 4 * n, 4 * n};
   size_t rec = 0;
   for (size_t b : parts) rec += (b + 255) & ~size_t(255);
   for (auto& s : h->sc) {
@@ -220,23 +224,34 @@ brx_status ensure_scratch(brx_handle* h, long long chunk) {
     s.r.vidx = reinterpret_cast<int32_t*>(take(32 * n));
     s.r.status = reinterpret_cast<int32_t*>(take(4 * n));
     s.order = reinterpret_cast<int32_t*>(take(4 * n));
-    BRX_CUDA(h, s.sortbuf.ensure(sizeof(int32_t) * node_sort_scratch_ints(h->g.n_nodes)));
-    s.counts = static_cast<int32_t*>(s.sortbuf.p);
+    s.r.key = reinterpret_cast<int32_t*>(take(4 * n));
+    BRX_CUDA(h, s.sortbuf.ensure(sizeof(int32_t) * group_scratch_ints(n_group_keys(h->g.n_cube, h->g.n_tets))));
+    s.sort_scratch = static_cast<int32_t*>(s.sortbuf.p);
+    BRX_CUDA(h, s.groupbuf.ensure(sizeof(GroupDesc) * n + 256));
+    s.groups = static_cast<GroupDesc*>(s.groupbuf.p);
+    s.n_groups = reinterpret_cast<int32_t*>(static_cast<char*>(s.groupbuf.p) + sizeof(GroupDesc) * n + 64);
+    s.counters = s.n_groups + 16;
   }
   h->scratch_q = chunk;
   return BRX_OK;
 }
 
-GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, long long n, int rot_mode, bool phase) {
+GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, long long n, int rot_mode, bool phase,
+                           int which) {
   GatherParams p{};
   p.nw = s.r.nw;
   p.vidx = s.r.vidx;
   p.w = s.r.w;
   p.rot = s.r.rot;
   p.q_ir = s.r.q_ir;
-  p.status = s.r.status;
   p.order = s.order;
+  p.groups = s.groups;
+  p.n_groups = s.n_groups;
+  p.counter = s.counters + which;
   p.n = n;
+  p.n_cube = h->g.n_cube;
+  p.cube_vertices = h->g.cube_vertices;
+  p.tet_vertices = h->g.tet_vertices;
   p.data = d.data.p;
   p.B = d.B;
   p.s = span(d);
@@ -246,7 +261,6 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.rot_mode = rot_mode;
   p.gamma_cart = d.length_unit == BRX_LU_ANGSTROM;
   p.phase_allowed = phase ? 1 : 0;
-  p.Nmat = 0;
   p.n_keys = h->n_keys;
   p.keys = static_cast<const long long*>(h->perm_keys.p);
   p.perm_ids = static_cast<const int32_t*>(h->perm_ids.p);
@@ -259,16 +273,12 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.gamma_F0 = h->g.gamma_F0;
   p.gamma_vidx = h->g.gamma_vidx;
   p.gamma_vectors = h->g.gamma_vectors;
-  const int cmax = 24;
-  int nc = 1;
-  while (nc < 32 && (p.s + nc - 1) / nc > cmax) nc <<= 1;
-  p.n_chunks = nc;
-  p.chunk_len = (p.s + nc - 1) / nc;
+  p.qmax = kGroupQ;
   return p;
 }
 
 size_t smem_budget(brx_handle* h) {
-  size_t b = 72 * 1024;
+  size_t b = 100 * 1024;
   if (h->smem_optin && b > h->smem_optin) b = h->smem_optin;
   return b;
 }
@@ -441,23 +451,23 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       BRX_CUDA(h, cp(lout->status ? lout->status + base : nullptr, s.r.status, 4 * (size_t)m));
       continue;
     }
-    launch_node_sort(s.r.node, s.r.status, m, h->g.n_nodes, s.counts, s.order, cs);
-    h->launches += 3;
+    h->launches += launch_grouping(s.r.key, m, n_group_keys(h->g.n_cube, h->g.n_tets), kGroupQ, s.sort_scratch,
+                                   s.order, s.groups, s.n_groups, cs);
     if (ev[2]) cudaEventRecord(ev[2], cs);
     char* vdst = o_host ? static_cast<char*>(s.vbuf.p) : static_cast<char*>(vals_out) + vrow * (size_t)base;
     {
-      GatherParams p = gather_params(h, h->vals, s, m, ir ? vmode : ROT_NONE, false);
+      GatherParams p = gather_params(h, h->vals, s, m, ir ? vmode : ROT_NONE, false, 0);
       p.out = vdst;
-      p.q_tile = gather_pick_tile(p, h->vals.store, h->vals.cplx, smem_budget(h));
+      p.MB = gather_pick_modes(p, h->vals.store, h->vals.cplx, smem_budget(h));
       h->launches += launch_gather(p, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h), cs);
     }
     if (ev[3]) cudaEventRecord(ev[3], cs);
     char* cdst = nullptr;
     if (h->vecs.present) {
       cdst = o_host ? static_cast<char*>(s.cbuf.p) : static_cast<char*>(vecs_out) + crow * (size_t)base;
-      GatherParams p = gather_params(h, h->vecs, s, m, ir ? cmode : ROT_NONE, h->vecs.cplx);
+      GatherParams p = gather_params(h, h->vecs, s, m, ir ? cmode : ROT_NONE, h->vecs.cplx, 1);
       p.out = cdst;
-      p.q_tile = gather_pick_tile(p, h->vecs.store, h->vecs.cplx, smem_budget(h));
+      p.MB = gather_pick_modes(p, h->vecs.store, h->vecs.cplx, smem_budget(h));
       h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h), cs);
     }
     if (ev[4]) cudaEventRecord(ev[4], cs);
@@ -560,6 +570,8 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
   g.n_ops = G.n_ops;
   g.identity = G.identity;
   g.n_nodes = G.n_nodes;
+  g.n_cube = G.n_cube;
+  g.n_tets = G.n_tets;
   g.n_atoms = G.n_atoms;
   g.t_main = make_tol(G.float_tolerance, G.digit);
   g.t_def = make_tol(0.0, 1);
@@ -624,6 +636,7 @@ void brx_destroy(brx_handle* h) {
     if (s.stream) cudaStreamSynchronize(s.stream);
     s.rec.release();
     s.sortbuf.release();
+    s.groupbuf.release();
     s.qbuf.release();
     s.vbuf.release();
     s.cbuf.release();

@@ -105,6 +105,8 @@ struct DevGeom {
   int64_t n_nodes;
   const int32_t* node_type;
   const int32_t* node_index;
+  int32_t n_cube;
+  long long n_tets;
   const int32_t* cube_vertices;
   const int32_t* poly_tet_offset;
   const int32_t* tet_vertices;
@@ -130,7 +132,16 @@ struct Records {
   int32_t* vidx;    // n × 8
   double* w;        // n × 8
   int32_t* status;  // n
+  int32_t* key;     // n: gather group (cube node or tetrahedron, and pivot slot)
 };
+
+// Group key of a located q: the vertex set it interpolates from (a cube
+// node's 8 corners in weight order, or one tetrahedron's 4 vertices) and the
+// slot of its pivot (first) vertex.  q with equal keys share every vertex
+// row and every antiphase factor of the gather.
+__host__ __device__ inline long long n_group_keys(int32_t n_cube, long long n_tets) {
+  return 8LL * n_cube + 4LL * n_tets;
+}
 
 // Error summary shared by all kernels of one query.
 struct ErrorWord {

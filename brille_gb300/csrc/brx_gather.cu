@@ -1,11 +1,13 @@
 // K3+K4: gather and weighted sum of vertex data, fused with the rotation
 // back by R (and the Γ permutation/phase for phonon eigenvectors).
 //
-// One CTA handles a tile of q (in node-sorted order so that neighbouring q
-// share vertex rows); threads map to (q, branch, element-chunk).  The
-// interpolated rows of the tile accumulate in registers, land in shared
-// memory, and are rotated and written out from there so that global stores
-// are coalesced rows of the output.
+// q are grouped by the vertex set they interpolate from and their pivot
+// vertex (a counting sort on the group key the locate kernel writes).  A
+// persistent CTA takes one group at a time from a work queue, stages the
+// group's vertex rows in shared memory one block of modes at a time, forms
+// the antiphase factors once for the whole group, and then writes every q's
+// rotated rows.  Vertex data are read once per group rather than once per q,
+// and global loads and stores are contiguous rows.
 //
 // Reference: Interpolator::interpolate_at_mix (src/interpolator_at.tpp:92-127),
 // antiphase (src/utilities.tpp:567-578), PermutationTable::safe_get
@@ -17,8 +19,6 @@
 #include "brx_kernels.h"
 
 namespace brx {
-
-constexpr int kChunkMax = 24;  // elements accumulated per thread
 
 template <typename T>
 struct Ar;
@@ -104,376 +104,352 @@ __device__ __forceinline__ int perm_lookup(const GatherParams& p, long long i, l
   return -1;
 }
 
-struct TileLayout {
-  size_t q, nw, vi, pid, rot, ident, w, ph, R, out, total;
+struct GroupLayout {
+  size_t q, rot, ident, w, R, ph, pid, e, Y, total;
 };
 
 template <typename Acc>
-__host__ __device__ inline TileLayout tile_layout(int QT, int B, int s, int comps, int n_atoms, bool gamma) {
-  TileLayout L;
+__host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int comps, int na) {
+  GroupLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = (o + 15) & ~size_t(15);
     o = at + bytes;
     return at;
   };
-  L.q = take(sizeof(long long) * QT);
-  L.nw = take(sizeof(int) * QT);
-  L.vi = take(sizeof(int) * 8 * QT);
-  L.pid = take(sizeof(int) * 8 * QT);
-  L.rot = take(sizeof(int) * 2 * QT);
-  L.ident = take(sizeof(int) * QT);
-  L.w = take(sizeof(Acc) * 8 * QT);
-  L.ph = take(gamma ? sizeof(Acc) * 4 * (size_t)n_atoms * QT : 0);
-  L.R = take(sizeof(Acc) * 18 * QT);
-  L.out = take(sizeof(Acc) * (size_t)QT * B * s * comps);
+  L.q = take(sizeof(long long) * QM);
+  L.rot = take(sizeof(int) * 2 * QM);
+  L.ident = take(sizeof(int) * QM);
+  L.w = take(sizeof(Acc) * 8 * QM);
+  L.R = take(sizeof(Acc) * 18 * QM);
+  L.ph = take(sizeof(Acc) * 2 * (size_t)na * QM);
+  L.pid = take(sizeof(int) * 8);
+  L.e = take(sizeof(Acc) * 2 * 8 * (size_t)MB);
+  L.Y = take(sizeof(Acc) * 8 * (size_t)MB * s * comps);
   L.total = (o + 15) & ~size_t(15);
   return L;
 }
 
 template <typename Acc, typename St, bool CPLX, typename Out>
 __global__ void __launch_bounds__(kGatherThreads)
-gather_kernel(GatherParams p) {
+group_gather_kernel(GatherParams p) {
   using A = Ar<Acc>;
-  extern __shared__ __align__(16) unsigned char sm[];
-  const int QT = p.q_tile, B = p.B, s = p.s, NC = p.n_chunks, CL = p.chunk_len;
   constexpr int comps = CPLX ? 2 : 1;
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ int s_desc[3];
+  __shared__ int s_vid[8];
+  __shared__ int s_meta[2];  // number of slots, pivot slot
+  const int B = p.B, s = p.s, MB = p.MB, QM = p.qmax;
   const bool gamma = p.rot_mode == ROT_GAMMA;
-  const int n_atoms_tab = gamma ? p.nvec : 0;
-  const TileLayout L = tile_layout<Acc>(QT, B, s, comps, n_atoms_tab, gamma);
+  const int na = gamma ? p.nvec : 0;
+  const GroupLayout L = group_layout<Acc>(QM, MB, s, comps, na);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
-  int* s_nw = reinterpret_cast<int*>(sm + L.nw);
-  int* s_vi = reinterpret_cast<int*>(sm + L.vi);
-  int* s_pid = reinterpret_cast<int*>(sm + L.pid);
   int* s_rot = reinterpret_cast<int*>(sm + L.rot);
   int* s_id = reinterpret_cast<int*>(sm + L.ident);
   Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
-  Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
   Acc* s_R = reinterpret_cast<Acc*>(sm + L.R);
-  Acc* s_out = reinterpret_cast<Acc*>(sm + L.out);
-  const long long n_tiles = (p.n + QT - 1) / QT;
+  Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
+  int* s_pid = reinterpret_cast<int*>(sm + L.pid);
+  Acc* s_e = reinterpret_cast<Acc*>(sm + L.e);
+  Acc* s_Y = reinterpret_cast<Acc*>(sm + L.Y);
+  const int G = p.nsc + p.nvec + p.nmat;
+  const int n_groups = *p.n_groups;
+  Out* out = reinterpret_cast<Out*>(p.out);
+  const int tid = threadIdx.x, nth = blockDim.x;
 
-  for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    // ---- phase A: records of the tile ----
-    for (int t = threadIdx.x; t < QT; t += blockDim.x) {
-      long long j = tile * QT + t;
-      long long qi = -1;
-      int nw = 0;
-      if (j < p.n) {
-        long long c = p.order ? (long long)p.order[j] : j;
-        if (p.status[c] == 0) { qi = c; nw = p.nw[c]; }
+  for (;;) {
+    if (tid == 0) {
+      int g = atomicAdd(p.counter, 1);
+      if (g < n_groups) {
+        GroupDesc d = p.groups[g];
+        s_desc[0] = d.key;
+        s_desc[1] = d.start;
+        s_desc[2] = d.count;
+      } else {
+        s_desc[2] = -1;
       }
-      s_q[t] = qi;
-      s_nw[t] = nw;
-      for (int x = 0; x < 8; ++x) {
-        s_vi[8 * t + x] = qi >= 0 ? p.vidx[8 * qi + x] : 0;
-        s_w[8 * t + x] = qi >= 0 ? (Acc)p.w[8 * qi + x] : (Acc)0;
+    }
+    __syncthreads();
+    const int count = s_desc[2];
+    if (count < 0) break;
+    const int key = s_desc[0], start = s_desc[1];
+    // ---- group prologue: vertex slots in weight order, pivot ----
+    if (tid < 8) {
+      int nslot, pivot, vid = 0;
+      if (key < 8 * p.n_cube) {
+        const int ni = key >> 3;
+        pivot = key & 7;
+        nslot = 8;
+        vid = __ldg(p.cube_vertices + 8 * (long long)ni + 7 - tid);
+      } else {
+        const long long t = (key - 8LL * p.n_cube) >> 2;
+        pivot = (int)((key - 8LL * p.n_cube) & 3);
+        nslot = 4;
+        vid = tid < 4 ? __ldg(p.tet_vertices + 4 * t + tid) : 0;
       }
-      int r0 = 0, r1 = 0;
-      if (qi >= 0 && p.rot_mode != ROT_NONE) { r0 = p.rot[2 * qi]; r1 = p.rot[2 * qi + 1]; }
-      s_rot[2 * t] = r0;
-      s_rot[2 * t + 1] = r1;
-      int ident = 1;
-      if (p.rot_mode != ROT_NONE && qi >= 0) {
+      s_vid[tid] = vid;
+      if (tid == 0) { s_meta[0] = nslot; s_meta[1] = pivot; }
+    }
+    __syncthreads();
+    const int nslot = s_meta[0], pivot = s_meta[1];
+    if (tid < nslot) s_pid[tid] = perm_lookup(p, s_vid[pivot], s_vid[tid]);
+    // per-q records: weights by slot, R and R⁻¹, Γ phases
+    for (int j = tid; j < count; j += nth) {
+      const long long qi = p.order[start + j];
+      s_q[j] = qi;
+      Acc wsl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      const int nw = p.nw[qi];
+      for (int k = 0; k < nw; ++k) {
+        const int v = p.vidx[8 * qi + k];
+        const Acc wk = (Acc)p.w[8 * qi + k];
+        for (int x = 0; x < nslot; ++x)
+          if (s_vid[x] == v) wsl[x] = wk;
+      }
+      for (int x = 0; x < 8; ++x) s_w[8 * j + x] = wsl[x];
+      int r0 = 0, r1 = 0, ident = 1;
+      if (p.rot_mode != ROT_NONE) {
+        r0 = p.rot[2 * qi];
+        r1 = p.rot[2 * qi + 1];
         const int32_t* W = p.ops + 9 * r0;
         ident = (W[0] == 1 && W[1] == 0 && W[2] == 0 && W[3] == 0 && W[4] == 1 && W[5] == 0 && W[6] == 0 &&
                  W[7] == 0 && W[8] == 1);
-        // R (slot 0..8) and R⁻¹ (slot 9..17) in the arithmetic type
         for (int e = 0; e < 9; ++e) {
           if (gamma && p.gamma_cart) {
-            s_R[18 * t + e] = (Acc)p.rot_cart[9 * r0 + e];
-            s_R[18 * t + 9 + e] = (Acc)p.rot_cart[9 * r1 + e];
+            s_R[18 * j + e] = (Acc)p.rot_cart[9 * r0 + e];
+            s_R[18 * j + 9 + e] = (Acc)p.rot_cart[9 * r1 + e];
           } else {
-            s_R[18 * t + e] = (Acc)p.ops[9 * r0 + e];
-            s_R[18 * t + 9 + e] = (Acc)p.ops[9 * r1 + e];
+            s_R[18 * j + e] = (Acc)p.ops[9 * r0 + e];
+            s_R[18 * j + 9 + e] = (Acc)p.ops[9 * r1 + e];
           }
         }
       }
-      s_id[t] = ident;
+      s_rot[2 * j] = r0;
+      s_rot[2 * j + 1] = r1;
+      s_id[j] = ident;
     }
     __syncthreads();
-    // permutation ids per (q, vertex); Γ phases per (q, atom)
-    for (int it = threadIdx.x; it < 8 * QT; it += blockDim.x) {
-      int t = it >> 3, x = it & 7;
-      s_pid[it] = (s_q[t] >= 0 && x < s_nw[t]) ? perm_lookup(p, s_vi[8 * t], s_vi[it]) : -1;
-    }
     if (gamma) {
-      for (int it = threadIdx.x; it < QT * n_atoms_tab; it += blockDim.x) {
-        int t = it / n_atoms_tab, k = it % n_atoms_tab;
-        long long qi = s_q[t];
-        Acc v[4] = {1, 0, 1, 0};
-        if (qi >= 0) {
-          const double q0 = p.q_ir[3 * qi], q1 = p.q_ir[3 * qi + 1], q2 = p.q_ir[3 * qi + 2];
-          for (int h = 0; h < 2; ++h) {
-            int r = s_rot[2 * t + h];
-            const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + r);
-            double dq = 0.0;
-            dq = __dadd_rn(dq, __dmul_rn(q0, d[0]));
-            dq = __dadd_rn(dq, __dmul_rn(q1, d[1]));
-            dq = __dadd_rn(dq, __dmul_rn(q2, d[2]));
-            double frac = dq - rint(dq);  // exact: e^{2πi n} = 1
-            double sn, cs;
-            sincospi(2.0 * frac, &sn, &cs);
-            v[2 * h] = (Acc)cs;
-            v[2 * h + 1] = (Acc)sn;
-          }
-        }
-        // slots: R phase (re, im), R⁻¹ phase (re, im)
-        for (int e = 0; e < 4; ++e) s_ph[4 * it + e] = v[e];
+      for (int it = tid; it < count * na; it += nth) {
+        const int j = it / na, k = it % na;
+        const long long qi = s_q[j];
+        const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + s_rot[2 * j + 1]);
+        double dq = 0.0;
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi], d[0]));
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 1], d[1]));
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 2], d[2]));
+        const double frac = dq - rint(dq);  // e^{2πi n} = 1 exactly
+        double sn, cs;
+        sincospi(2.0 * frac, &sn, &cs);
+        s_ph[2 * it] = (Acc)cs;
+        s_ph[2 * it + 1] = (Acc)sn;
       }
     }
-    __syncthreads();
-
-    // ---- phase B: gather into the shared tile ----
-    const int items = QT * B * NC;
-    const int rounds = (items + blockDim.x - 1) / blockDim.x;
-    for (int rd = 0; rd < rounds; ++rd) {
-      const int item = rd * blockDim.x + threadIdx.x;
-      const bool valid = item < items;
-      const int t = valid ? item / (B * NC) : 0;
-      const int rem = valid ? item % (B * NC) : 0;
-      const int b = rem / NC, c = rem % NC;
-      const long long qi = valid ? s_q[t] : -1;
-      const int nw = qi >= 0 ? s_nw[t] : 0;
-      const int e0 = c * CL;
-      const int e1 = min(s, e0 + CL);
-      Acc ar[kChunkMax], ai[kChunkMax];
-#pragma unroll
-      for (int i = 0; i < kChunkMax; ++i) { ar[i] = 0; ai[i] = 0; }
-      const long long piv = s_vi[8 * t];
-      for (int x = 0; x < 8; ++x) {
-        const bool act = x < nw;
-        if (!act && NC == 1) break;
-        const long long v = act ? s_vi[8 * t + x] : 0;
-        int pb = b;
-        if (act) {
-          int pid = s_pid[8 * t + x];
-          if (pid >= 0) pb = __ldg(p.perms + (long long)pid * B + b);
-        }
+    // ---- blocks of modes ----
+    for (int b0 = 0; b0 < B; b0 += MB) {
+      const int mb = min(MB, B - b0);
+      // stage the vertex rows of slots pivot..nslot-1 (slots before the pivot
+      // carry zero weight for every q of the group)
+      const int ns = nslot - pivot;
+      for (int it = tid; it < ns * mb * s; it += nth) {
+        const int e = it % s;
+        const int rb = it / s;
+        const int b = rb % mb, xs = rb / mb, x = pivot + xs;
+        const int pid = s_pid[x];
+        const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b0 + b) : b0 + b;
+        Acc re, im;
+        Ld<St, CPLX>::get(p.data, ((long long)s_vid[x] * B + row) * s + e, re, im);
+        Acc* y = s_Y + ((size_t)(x * MB + b) * s + e) * comps;
+        y[0] = re;
+        if (CPLX) y[1] = im;
+      }
+      __syncthreads();
+      // antiphase factors, one per (slot, mode), in the reference's sum order
+      for (int it = tid; it < ns * mb; it += nth) {
+        const int b = it % mb, x = pivot + it / mb;
         Acc er = 1, ei = 0;
-        if (CPLX && p.phase_allowed && x > 0) {
-          Acc rdot = 0, idot = 0;
-          if (act) {
-            const long long r0 = (piv * B + b) * s, r1 = (v * B + pb) * s;
-            for (int e = e0; e < e1; ++e) {
-              Acc xr, xi, yr, yi;
-              Ld<St, CPLX>::get(p.data, r0 + e, xr, xi);
-              Ld<St, CPLX>::get(p.data, r1 + e, yr, yi);
-              rdot = A::add(rdot, A::add(A::mul(xr, yr), A::mul(xi, yi)));
-              idot = A::add(idot, A::sub(A::mul(xr, yi), A::mul(xi, yr)));
-            }
+        if (CPLX && p.phase_allowed && x != pivot) {
+          const Acc* a = s_Y + (size_t)(pivot * MB + b) * s * comps;
+          const Acc* c = s_Y + (size_t)(x * MB + b) * s * comps;
+          Acc rd = 0, id = 0;
+          for (int e = 0; e < s; ++e) {
+            const Acc ar = a[2 * e], ai = a[2 * e + 1], br = c[2 * e], bi = c[2 * e + 1];
+            rd = A::add(rd, A::add(A::mul(ar, br), A::mul(ai, bi)));
+            id = A::add(id, A::sub(A::mul(ar, bi), A::mul(ai, br)));
           }
-          if (NC > 1) {
-            for (int off = 1; off < NC; off <<= 1) {
-              rdot = A::add(rdot, __shfl_xor_sync(0xffffffffu, rdot, off));
-              idot = A::add(idot, __shfl_xor_sync(0xffffffffu, idot, off));
-            }
-          }
-          if (act) {
-            Acc mag = sqrt(A::add(A::mul(rdot, rdot), A::mul(idot, idot)));
-            if (mag > (Acc)0) {
-              er = rdot / mag;
-              ei = -(idot / mag);
-            }
+          const Acc mag = sqrt(A::add(A::mul(rd, rd), A::mul(id, id)));
+          if (mag > (Acc)0) {
+            er = rd / mag;
+            ei = -(id / mag);
           }
         }
-        if (act) {
-          const Acc wx = s_w[8 * t + x];
-          const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
-          const long long r1 = (v * B + pb) * s;
+        s_e[2 * (x * MB + b)] = er;
+        s_e[2 * (x * MB + b) + 1] = ei;
+      }
+      __syncthreads();
+      // every q's rows for these modes: weighted sum, rotation, store
+      const int items = count * mb * G;
+      for (int it = tid; it < items; it += nth) {
+        const int gi = it % G;
+        const int jb = it / G;
+        const int b = jb % mb, j = jb / mb;
+        const long long qi = s_q[j];
+        const int bb = b0 + b;
+        const Acc* wj = s_w + 8 * j;
+        const bool rotate = p.rot_mode != ROT_NONE && (gamma || !s_id[j]);
+        const Acc* R = s_R + 18 * j;
+        const Acc* Ri = R + 9;
+        Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
+        int e0, ne;
+        if (gi < p.nsc) { e0 = gi; ne = 1; }
+        else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
+        else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
+        Acc vr[9], vi[9];
 #pragma unroll
-          for (int i = 0; i < kChunkMax; ++i) {
-            if (e0 + i < e1) {
-              Acc dr, di;
-              Ld<St, CPLX>::get(p.data, r1 + e0 + i, dr, di);
+        for (int k = 0; k < 9; ++k) { vr[k] = 0; vi[k] = 0; }
+        for (int x = pivot; x < nslot; ++x) {
+          const Acc wx = wj[x];
+          if (wx == (Acc)0) continue;
+          const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
+          const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
+          const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            if (k < ne) {
+              const Acc dr = y[k * comps];
               if (CPLX) {
-                ar[i] = A::add(ar[i], A::sub(A::mul(wr, dr), A::mul(wi, di)));
-                ai[i] = A::add(ai[i], A::add(A::mul(wr, di), A::mul(wi, dr)));
+                const Acc di = y[k * comps + 1];
+                vr[k] = A::add(vr[k], A::sub(A::mul(wr, dr), A::mul(wi, di)));
+                vi[k] = A::add(vi[k], A::add(A::mul(wr, di), A::mul(wi, dr)));
               } else {
-                ar[i] = A::add(ar[i], A::mul(wx, dr));
+                vr[k] = A::add(vr[k], A::mul(wx, dr));
               }
             }
           }
         }
-      }
-      if (valid) {
-        Acc* dst = s_out + ((size_t)(t * B + b) * s) * comps;
-#pragma unroll
-        for (int i = 0; i < kChunkMax; ++i) {
-          if (e0 + i < e1) {
-            dst[(e0 + i) * comps] = ar[i];
-            if (CPLX) dst[(e0 + i) * comps + 1] = ai[i];
+        int de = e0;
+        if (ne == 3 && rotate) {
+          Acc M[9];
+          Acc scale = 1;
+          if (p.rot_mode == ROT_RECIP) {
+            for (int a = 0; a < 3; ++a) for (int c = 0; c < 3; ++c) M[3 * a + c] = R[3 * c + a];
+          } else if (p.rot_mode == ROT_AXIAL) {
+            for (int k = 0; k < 9; ++k) M[k] = Ri[k];
+            scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                    R[2] * (R[3] * R[7] - R[4] * R[6]);
+          } else if (gamma) {
+            for (int k = 0; k < 9; ++k) M[k] = Ri[k];
+          } else {
+            for (int k = 0; k < 9; ++k) M[k] = R[k];
           }
-        }
-      }
-    }
-    __syncthreads();
-
-    // ---- phase C: rotate and store ----
-    const int G = p.nsc + p.nvec + p.nmat;
-    const int citems = QT * B * G;
-    Out* out = reinterpret_cast<Out*>(p.out);
-    for (int it = threadIdx.x; it < citems; it += blockDim.x) {
-      const int t = it / (B * G);
-      const int rem = it % (B * G);
-      const int b = rem / G, g = rem % G;
-      const long long qi = s_q[t];
-      if (qi < 0) continue;
-      const Acc* src = s_out + ((size_t)(t * B + b) * s) * comps;
-      Out* dst = out + ((size_t)qi * B + b) * (size_t)s * comps;
-      const bool rotate = p.rot_mode != ROT_NONE && (gamma || !s_id[t]);
-      const Acc* R = s_R + 18 * t;
-      const Acc* Ri = R + 9;
-      if (g < p.nsc) {
-        dst[g * comps] = (Out)src[g * comps];
-        if (CPLX) dst[g * comps + 1] = (Out)src[g * comps + 1];
-        continue;
-      }
-      if (g < p.nsc + p.nvec) {
-        const int k = g - p.nsc;
-        const int e = p.nsc + 3 * k;
-        Acc vr[3], vi[3];
-        for (int j = 0; j < 3; ++j) { vr[j] = src[(e + j) * comps]; vi[j] = CPLX ? src[(e + j) * comps + 1] : (Acc)0; }
-        if (!rotate) {
-          for (int j = 0; j < 3; ++j) {
-            dst[(e + j) * comps] = (Out)vr[j];
-            if (CPLX) dst[(e + j) * comps + 1] = (Out)vi[j];
-          }
-          continue;
-        }
-        // the 3×3 applied to this vector
-        Acc M[9];
-        Acc scale = 1;
-        if (p.rot_mode == ROT_RECIP) {
-          for (int a = 0; a < 3; ++a) for (int bb = 0; bb < 3; ++bb) M[3 * a + bb] = R[3 * bb + a];
-        } else if (p.rot_mode == ROT_AXIAL) {
-          for (int j = 0; j < 9; ++j) M[j] = Ri[j];
-          scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
-                  R[2] * (R[3] * R[7] - R[4] * R[6]);
-        } else if (p.rot_mode == ROT_GAMMA) {
-          for (int j = 0; j < 9; ++j) M[j] = Ri[j];
-        } else {
-          for (int j = 0; j < 9; ++j) M[j] = R[j];
-        }
-        Acc tr[3], ti[3];
-        for (int a = 0; a < 3; ++a) {
-          Acc sr = 0, si = 0;
-          for (int kk = 0; kk < 3; ++kk) {
-            sr = A::add(sr, A::mul(M[3 * a + kk], vr[kk]));
-            if (CPLX) si = A::add(si, A::mul(M[3 * a + kk], vi[kk]));
-          }
-          tr[a] = sr;
-          ti[a] = si;
-        }
-        int de = e;
-        if (p.rot_mode == ROT_GAMMA) {
-          const int r1 = s_rot[2 * t + 1];
-          de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + r1);
-          const Acc pr = s_ph[4 * (t * n_atoms_tab + k) + 2], pi = s_ph[4 * (t * n_atoms_tab + k) + 3];
+          Acc tr[3], ti[3];
           for (int a = 0; a < 3; ++a) {
-            Acc xr = A::sub(A::mul(pr, tr[a]), A::mul(pi, ti[a]));
-            Acc xi = A::add(A::mul(pr, ti[a]), A::mul(pi, tr[a]));
-            tr[a] = xr;
-            ti[a] = xi;
+            Acc sr = 0, si = 0;
+            for (int c = 0; c < 3; ++c) {
+              sr = A::add(sr, A::mul(M[3 * a + c], vr[c]));
+              if (CPLX) si = A::add(si, A::mul(M[3 * a + c], vi[c]));
+            }
+            tr[a] = sr;
+            ti[a] = si;
           }
-        } else if (p.rot_mode == ROT_AXIAL) {
-          for (int a = 0; a < 3; ++a) { tr[a] = A::mul(scale, tr[a]); ti[a] = A::mul(scale, ti[a]); }
-        }
-        for (int a = 0; a < 3; ++a) {
-          dst[(de + a) * comps] = (Out)tr[a];
-          if (CPLX) dst[(de + a) * comps + 1] = (Out)ti[a];
-        }
-        continue;
-      }
-      // 3×3 matrices
-      const int m = g - p.nsc - p.nvec;
-      const int e = p.nsc + 3 * p.nvec + 9 * m;
-      Acc Xr[9], Xi[9];
-      for (int j = 0; j < 9; ++j) { Xr[j] = src[(e + j) * comps]; Xi[j] = CPLX ? src[(e + j) * comps + 1] : (Acc)0; }
-      if (!rotate) {
-        for (int j = 0; j < 9; ++j) {
-          dst[(e + j) * comps] = (Out)Xr[j];
-          if (CPLX) dst[(e + j) * comps + 1] = (Out)Xi[j];
-        }
-        continue;
-      }
-      Acc Lm[9], Rm[9];  // result = Lm · (X · Rm)
-      if (p.rot_mode == ROT_RECIP) {
-        for (int a = 0; a < 3; ++a) for (int bb = 0; bb < 3; ++bb) { Lm[3 * a + bb] = R[3 * bb + a]; Rm[3 * a + bb] = Ri[3 * bb + a]; }
-      } else if (p.rot_mode == ROT_AXIAL) {
-        for (int j = 0; j < 9; ++j) { Lm[j] = Ri[j]; Rm[j] = R[j]; }
-      } else {
-        for (int j = 0; j < 9; ++j) { Lm[j] = R[j]; Rm[j] = Ri[j]; }
-      }
-      Acc Tr[9], Ti[9], Yr[9], Yi[9];
-      for (int a = 0; a < 3; ++a)
-        for (int bb = 0; bb < 3; ++bb) {
-          Acc sr = 0, si = 0;
-          for (int kk = 0; kk < 3; ++kk) {
-            sr = A::add(sr, A::mul(Xr[3 * a + kk], Rm[3 * kk + bb]));
-            si = A::add(si, A::mul(Xi[3 * a + kk], Rm[3 * kk + bb]));
+          if (gamma) {
+            const int k = gi - p.nsc;
+            de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
+            const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
+            for (int a = 0; a < 3; ++a) {
+              const Acc xr = A::sub(A::mul(pr, tr[a]), A::mul(pi, ti[a]));
+              const Acc xi = A::add(A::mul(pr, ti[a]), A::mul(pi, tr[a]));
+              tr[a] = xr;
+              ti[a] = xi;
+            }
+          } else if (p.rot_mode == ROT_AXIAL) {
+            for (int a = 0; a < 3; ++a) { tr[a] = A::mul(scale, tr[a]); ti[a] = A::mul(scale, ti[a]); }
           }
-          Tr[3 * a + bb] = sr;
-          Ti[3 * a + bb] = si;
-        }
-      for (int a = 0; a < 3; ++a)
-        for (int bb = 0; bb < 3; ++bb) {
-          Acc sr = 0, si = 0;
-          for (int kk = 0; kk < 3; ++kk) {
-            sr = A::add(sr, A::mul(Lm[3 * a + kk], Tr[3 * kk + bb]));
-            si = A::add(si, A::mul(Lm[3 * a + kk], Ti[3 * kk + bb]));
+          for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
+        } else if (ne == 9 && rotate) {
+          Acc Lm[9], Rm[9];  // result = Lm · (X · Rm)
+          if (p.rot_mode == ROT_RECIP) {
+            for (int a = 0; a < 3; ++a)
+              for (int c = 0; c < 3; ++c) { Lm[3 * a + c] = R[3 * c + a]; Rm[3 * a + c] = Ri[3 * c + a]; }
+          } else if (p.rot_mode == ROT_AXIAL) {
+            for (int k = 0; k < 9; ++k) { Lm[k] = Ri[k]; Rm[k] = R[k]; }
+          } else {
+            for (int k = 0; k < 9; ++k) { Lm[k] = R[k]; Rm[k] = Ri[k]; }
           }
-          Yr[3 * a + bb] = sr;
-          Yi[3 * a + bb] = si;
+          Acc Tr[9], Ti[9];
+          for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) {
+              Acc sr = 0, si = 0;
+              for (int k = 0; k < 3; ++k) {
+                sr = A::add(sr, A::mul(vr[3 * a + k], Rm[3 * k + c]));
+                si = A::add(si, A::mul(vi[3 * a + k], Rm[3 * k + c]));
+              }
+              Tr[3 * a + c] = sr;
+              Ti[3 * a + c] = si;
+            }
+          for (int a = 0; a < 3; ++a)
+            for (int c = 0; c < 3; ++c) {
+              Acc sr = 0, si = 0;
+              for (int k = 0; k < 3; ++k) {
+                sr = A::add(sr, A::mul(Lm[3 * a + k], Tr[3 * k + c]));
+                si = A::add(si, A::mul(Lm[3 * a + k], Ti[3 * k + c]));
+              }
+              vr[3 * a + c] = sr;
+              vi[3 * a + c] = si;
+            }
         }
-      const int de = e;
-      for (int j = 0; j < 9; ++j) {
-        dst[(de + j) * comps] = (Out)Yr[j];
-        if (CPLX) dst[(de + j) * comps + 1] = (Out)Yi[j];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          if (k < ne) {
+            dst[(de + k) * comps] = (Out)vr[k];
+            if (CPLX) dst[(de + k) * comps + 1] = (Out)vi[k];
+          }
+        }
       }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
 template <typename Acc>
-static size_t smem_for(const GatherParams& p, bool cplx, int qt) {
-  const bool gamma = p.rot_mode == ROT_GAMMA;
-  const int na = gamma ? p.nvec : 0;
-  return tile_layout<Acc>(qt, p.B, p.s, cplx ? 2 : 1, na, gamma).total;
+static size_t layout_bytes(const GatherParams& p, bool cplx, int MB) {
+  const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
+  return group_layout<Acc>(p.qmax, MB, p.s, cplx ? 2 : 1, na).total;
 }
 
-size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int q_tile) {
-  return store_kind == ST_F64 ? smem_for<double>(p, cplx, q_tile) : smem_for<float>(p, cplx, q_tile);
+size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB) {
+  return store_kind == ST_F64 ? layout_bytes<double>(p, cplx, MB) : layout_bytes<float>(p, cplx, MB);
 }
 
-int gather_pick_tile(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget) {
-  int qt = 64;
-  while (qt > 1 && gather_smem_bytes(p, store_kind, cplx, qt) > smem_budget) qt >>= 1;
-  return qt;
+int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget) {
+  int mb = p.B;
+  while (mb > 1 && gather_smem_bytes(p, store_kind, cplx, mb) > smem_budget) mb = (mb + 1) / 2;
+  // spread the modes evenly over the blocks
+  const int nblk = (p.B + mb - 1) / mb;
+  return (p.B + nblk - 1) / nblk;
 }
 
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
-  size_t smem = gather_smem_bytes(p, std::is_same<Acc, double>::value ? ST_F64 : ST_F32, CPLX, p.q_tile);
+  const size_t smem = layout_bytes<Acc>(p, CPLX, p.MB);
   static bool configured = false;
   if (!configured) {
-    cudaFuncSetAttribute(gather_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(group_gather_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         200 * 1024);
     configured = true;
   }
-  long long tiles = (p.n + p.q_tile - 1) / p.q_tile;
-  int per_sm = (int)((200 * 1024) / (smem > 0 ? smem : 1));
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, group_gather_kernel<Acc, St, CPLX, Out>, kGatherThreads,
+                                                smem);
   if (per_sm < 1) per_sm = 1;
-  if (per_sm > 8) per_sm = 8;
-  long long cap = (long long)num_sms * per_sm;
-  long long grid = tiles < cap ? tiles : cap;
-  if (grid < 1) grid = 1;
-  gather_kernel<Acc, St, CPLX, Out><<<(unsigned)grid, kGatherThreads, smem, s>>>(p);
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > p.n) grid = p.n > 0 ? p.n : 1;
+  group_gather_kernel<Acc, St, CPLX, Out><<<(unsigned)grid, kGatherThreads, smem, s>>>(p);
 }
 
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms, size_t,
                   cudaStream_t s) {
   if (p.n <= 0) return 0;
+  cudaMemsetAsync(p.counter, 0, sizeof(int32_t), s);
 #define BRX_DISPATCH(ACC, ST)                                                     \
   do {                                                                            \
     if (cplx) {                                                                   \
@@ -494,61 +470,130 @@ int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32
 }
 
 // ---------------------------------------------------------------------------
-// counting sort of q by trellis node (failed q go to the last bucket)
+// grouping: counting sort of q by group key, then one work descriptor per
+// group (at most kGroupQ q each)
 // ---------------------------------------------------------------------------
-__global__ void node_hist_kernel(const int32_t* node, const int32_t* status, long long n, long long n_nodes,
-                                 int32_t* counts) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    long long key = status[i] ? n_nodes : (long long)node[2 * i];
-    atomicAdd(counts + key, 1);
-  }
+__global__ void key_hist_kernel(const int32_t* key, long long n, int32_t* counts) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(counts + key[i], 1);
 }
 
-// single-CTA exclusive scan of counts[0..m) into counts, cursor copy in counts[m..2m)
-__global__ void node_scan_kernel(int32_t* counts, long long m) {
-  __shared__ long long part[1024];
-  const int T = blockDim.x;
-  long long per = (m + T - 1) / T;
-  long long b = threadIdx.x * per, e = min(m, b + per);
-  long long sum = 0;
-  for (long long i = b; i < e; ++i) sum += counts[i];
-  part[threadIdx.x] = sum;
+constexpr int kScanThreads = 1024, kScanPer = 8;
+
+// exclusive scan, three passes: block sums, scan of block sums, block scans
+__global__ void scan_reduce_kernel(const int32_t* in, long long m, int32_t* block_sums) {
+  __shared__ int32_t red[kScanThreads];
+  const long long base = (long long)blockIdx.x * kScanThreads * kScanPer;
+  int32_t s = 0;
+  for (int k = 0; k < kScanPer; ++k) {
+    long long i = base + (long long)k * kScanThreads + threadIdx.x;
+    if (i < m) s += in[i];
+  }
+  red[threadIdx.x] = s;
   __syncthreads();
+  for (int off = kScanThreads / 2; off > 0; off >>= 1) {
+    if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = red[0];
+}
+
+__global__ void scan_blocks_kernel(int32_t* block_sums, int nb) {
   if (threadIdx.x == 0) {
-    long long run = 0;
-    for (int i = 0; i < T; ++i) { long long v = part[i]; part[i] = run; run += v; }
-  }
-  __syncthreads();
-  long long run = part[threadIdx.x];
-  for (long long i = b; i < e; ++i) {
-    long long v = counts[i];
-    counts[i] = (int32_t)run;
-    counts[m + i] = (int32_t)run;
-    run += v;
+    int32_t run = 0;
+    for (int i = 0; i < nb; ++i) {
+      int32_t v = block_sums[i];
+      block_sums[i] = run;
+      run += v;
+    }
   }
 }
 
-__global__ void node_scatter_kernel(const int32_t* node, const int32_t* status, long long n, long long n_nodes,
-                                    int32_t* cursor, int32_t* order) {
+__global__ void scan_apply_kernel(const int32_t* in, long long m, const int32_t* block_sums, int32_t* out,
+                                  int32_t* out2) {
+  __shared__ int32_t tsum[kScanThreads];
+  const long long base = (long long)blockIdx.x * kScanThreads * kScanPer;
+  // each thread owns kScanPer consecutive elements
+  int32_t loc[kScanPer];
+  int32_t s = 0;
+  for (int k = 0; k < kScanPer; ++k) {
+    long long i = base + (long long)threadIdx.x * kScanPer + k;
+    loc[k] = i < m ? in[i] : 0;
+    s += loc[k];
+  }
+  tsum[threadIdx.x] = s;
+  __syncthreads();
+  // Hillis–Steele inclusive scan of the thread sums
+  for (int off = 1; off < kScanThreads; off <<= 1) {
+    int32_t v = threadIdx.x >= off ? tsum[threadIdx.x - off] : 0;
+    __syncthreads();
+    tsum[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int32_t run = block_sums[blockIdx.x] + (threadIdx.x ? tsum[threadIdx.x - 1] : 0);
+  for (int k = 0; k < kScanPer; ++k) {
+    long long i = base + (long long)threadIdx.x * kScanPer + k;
+    if (i < m) {
+      out[i] = run;
+      if (out2) out2[i] = run;
+    }
+    run += loc[k];
+  }
+}
+
+__global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cursor, int32_t* order) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    long long key = status[i] ? n_nodes : (long long)node[2 * i];
-    int pos = atomicAdd(cursor + key, 1);
+    int pos = atomicAdd(cursor + key[i], 1);
     order[pos] = (int32_t)i;
   }
 }
 
-size_t node_sort_scratch_ints(long long n_nodes) { return 2 * (size_t)(n_nodes + 1); }
+__global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
+                                   GroupDesc* groups, int32_t* n_groups) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n_keys; k += (long long)gridDim.x * blockDim.x) {
+    const int c = counts[k];
+    if (c <= 0) continue;
+    const int nd = (c + qmax - 1) / qmax;
+    int slot = atomicAdd(n_groups, nd);
+    for (int d = 0; d < nd; ++d) {
+      GroupDesc g;
+      g.key = (int32_t)k;
+      g.start = offsets[k] + d * qmax;
+      g.count = min(qmax, c - d * qmax);
+      groups[slot + d] = g;
+    }
+  }
+}
 
-void launch_node_sort(const int32_t* node, const int32_t* status, long long n, long long n_nodes, int32_t* counts,
-                      int32_t* order, cudaStream_t s) {
-  if (n <= 0) return;
-  long long m = n_nodes + 1;
+size_t group_scratch_ints(long long n_keys) {
+  const long long m = n_keys + 1;
+  const long long nb = (m + kScanThreads * kScanPer - 1) / (kScanThreads * kScanPer);
+  return (size_t)(3 * m + nb + 8);
+}
+
+int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax, int32_t* scratch, int32_t* order,
+                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const long long m = n_keys + 1;  // last bucket: failed q
+  const long long nb = (m + kScanThreads * kScanPer - 1) / (kScanThreads * kScanPer);
+  int32_t* counts = scratch;
+  int32_t* offsets = scratch + m;
+  int32_t* cursor = scratch + 2 * m;
+  int32_t* bsums = scratch + 3 * m;
   cudaMemsetAsync(counts, 0, sizeof(int32_t) * m, s);
+  cudaMemsetAsync(n_groups, 0, sizeof(int32_t), s);
   long long blocks = (n + 255) / 256;
-  if (blocks > 4096) blocks = 4096;
-  node_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(node, status, n, n_nodes, counts);
-  node_scan_kernel<<<1, 1024, 0, s>>>(counts, m);
-  node_scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(node, status, n, n_nodes, counts + m, order);
+  if (blocks > 8192) blocks = 8192;
+  key_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(key, n, counts);
+  scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, m, bsums);
+  scan_blocks_kernel<<<1, 32, 0, s>>>(bsums, (int)nb);
+  scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, m, bsums, offsets, cursor);
+  key_scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(key, n, cursor, order);
+  long long kb = (n_keys + 255) / 256;
+  if (kb > 8192) kb = 8192;
+  if (kb < 1) kb = 1;
+  make_groups_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, offsets, n_keys, qmax, groups, n_groups);
+  return 7;
 }
 
 }  // namespace brx

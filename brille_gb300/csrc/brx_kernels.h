@@ -14,6 +14,14 @@ constexpr int kGatherThreads = 256;
 enum RotMode { ROT_NONE = 0, ROT_REAL = 1, ROT_RECIP = 2, ROT_AXIAL = 3, ROT_GAMMA = 4 };
 enum StoreKind { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 
+struct GroupDesc {
+  int32_t key;    // group key (cube node / tetrahedron and pivot slot)
+  int32_t start;  // first entry in the key-sorted order
+  int32_t count;  // number of q (≤ kGroupQ)
+};
+
+constexpr int kGroupQ = 32;
+
 struct GatherParams {
   // locate records (chunk-local)
   const int32_t* nw;
@@ -21,9 +29,15 @@ struct GatherParams {
   const double* w;
   const int32_t* rot;
   const double* q_ir;
-  const int32_t* status;
-  const int32_t* order;      // processing order (node-sorted) or nullptr
+  const int32_t* order;      // key-sorted q indices
+  const GroupDesc* groups;   // work descriptors
+  const int32_t* n_groups;   // device count of descriptors
+  int32_t* counter;          // work-queue cursor
   long long n;
+  // trellis (group key decoding)
+  int n_cube;
+  const int32_t* cube_vertices;
+  const int32_t* tet_vertices;
   // vertex data
   const void* data;          // n_vertices × B × s (complex: interleaved pairs)
   int B, s;
@@ -31,7 +45,6 @@ struct GatherParams {
   int rot_mode;              // RotMode
   int gamma_cart;            // Γ data in Cartesian (Å) components: use L·W·L⁻¹
   int phase_allowed;         // antiphase alignment (complex vectors)
-  int Nmat;                  // Γ matrix block size (atoms)
   // permutation table (sorted keys i*n_vertices+j)
   long long n_keys;
   const long long* keys;
@@ -48,24 +61,24 @@ struct GatherParams {
   const double* gamma_vectors;
   // output
   void* out;                 // n × B × s, double or float (complex: pairs)
-  int q_tile;                // q per CTA
-  int n_chunks;              // threads per (q, branch), power of two ≤ 32
-  int chunk_len;             // elements per thread
+  int MB;                    // modes staged per block
+  int qmax;                  // q per work descriptor
 };
 
 size_t locate_smem_bytes(const DevGeom& g);
 void launch_locate(const DevGeom& g, const double* Q, long long n, long long base, int mode, const Records& r,
                    ErrorWord* err, int num_sms, cudaStream_t s);
 
-// Node-ordered processing: counting sort of q by trellis node.
-void launch_node_sort(const int32_t* node, const int32_t* status, long long n, long long n_nodes,
-                      int32_t* counts, int32_t* order, cudaStream_t s);
-size_t node_sort_scratch_ints(long long n_nodes);
+// Counting sort of q by group key and the work descriptors of the groups.
+// Returns the number of kernel launches.
+int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax, int32_t* scratch, int32_t* order,
+                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s);
+size_t group_scratch_ints(long long n_keys);
 
 // Gather + rotate for one interpolator.  Returns the number of launches.
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms,
                   size_t smem_budget, cudaStream_t s);
-size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int q_tile);
-int gather_pick_tile(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget);
+size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB);
+int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget);
 
 }  // namespace brx

@@ -351,6 +351,25 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
 #pragma unroll
     for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = vi[k]; r.w[8 * i + k] = w[k]; }
     r.status[i] = st;
+    int32_t key = (int32_t)n_group_keys(g.n_cube, g.n_tets);  // failed q: last bucket
+    if (!st) {
+      const long long node = nt[0];
+      if (nt[1] < 0) {
+        const int32_t ni = __ldg(g.node_index + node);
+        const int32_t* cv = g.cube_vertices + 8 * (long long)ni;
+        int slot = 0;
+        for (int j = 0; j < 8; ++j)
+          if (__ldg(cv + 7 - j) == vi[0]) { slot = j; break; }
+        key = 8 * ni + slot;
+      } else {
+        const int32_t* tv = g.tet_vertices + 4 * (long long)nt[1];
+        int slot = 0;
+        for (int j = 0; j < 4; ++j)
+          if (__ldg(tv + j) == vi[0]) { slot = j; break; }
+        key = (int32_t)(8LL * g.n_cube + 4LL * nt[1] + slot);
+      }
+    }
+    r.key[i] = key;
     if (st) report(err, base + i, st);
   }
 }

@@ -93,30 +93,30 @@ class TrellisBuild:
 
         node_type = np.zeros(nx * ny * nz, np.int32)
         node_index = np.full(nx * ny * nz, -1, np.int32)
-        cube_pts, poly_cells = [], []
-        pts = []  # all vertex candidates (Cartesian)
 
-        def idx3(i, j, k):
-            return i + nx * (j + ny * k)
+        def corner(arr, c):
+            return arr[c[0]:c[0] + nx, c[1]:c[1] + ny, c[2]:c[2] + nz]
 
-        for k in range(nz):
-            for j in range(ny):
-                for i in range(nx):
-                    cin = np.array([inside[i + c[0], j + c[1], k + c[2]] for c in CUBE_CORNERS])
-                    cd = np.array([dist[i + c[0], j + c[1], k + c[2]] for c in CUBE_CORNERS])
-                    if np.any(np.all(cd > tol, axis=0)):
-                        continue  # entirely outside one plane: null
-                    if cin.all() and not always_triangulate:
-                        node_type[idx3(i, j, k)] = NODE_CUBE
-                        node_index[idx3(i, j, k)] = len(cube_pts)
-                        cube_pts.append([(i + c[0], j + c[1], k + c[2]) for c in CUBE_CORNERS])
-                        continue
-                    lo = np.array([kx[i], ky[j], kz[k]])
-                    hi = np.array([kx[i + 1], ky[j + 1], kz[k + 1]])
-                    cand = self._cut_cell(lo, hi, verts, pedges, An, bn, tol)
-                    if cand is None:
-                        continue
-                    poly_cells.append((idx3(i, j, k), cand))
+        cin = np.stack([corner(inside, c) for c in CUBE_CORNERS], axis=-1)        # (nx, ny, nz, 8)
+        out_all = np.ones((nx, ny, nz, len(bn)), bool)
+        for c in CUBE_CORNERS:
+            out_all &= corner(dist, c) > tol
+        null = np.any(out_all, axis=-1)
+        cube = cin.all(axis=-1) & ~null & (not always_triangulate)
+        # linear node index i + nx (j + ny k): order cells by (k, j, i)
+        cube_ijk = np.argwhere(cube.transpose(2, 1, 0))[:, ::-1]                # (i, j, k) in linear order
+        cand_ijk = np.argwhere((~cube & ~null).transpose(2, 1, 0))[:, ::-1]
+        lin_cube = cube_ijk[:, 0] + nx * (cube_ijk[:, 1] + ny * cube_ijk[:, 2])
+        node_type[lin_cube] = NODE_CUBE
+        node_index[lin_cube] = np.arange(len(lin_cube), dtype=np.int32)
+        cube_pts = [[(i + c[0], j + c[1], k + c[2]) for c in CUBE_CORNERS] for i, j, k in cube_ijk]
+        poly_cells = []
+        for i, j, k in cand_ijk:
+            lo = np.array([kx[i], ky[j], kz[k]])
+            hi = np.array([kx[i + 1], ky[j + 1], kz[k + 1]])
+            cand = self._cut_cell(lo, hi, verts, pedges, An, bn, tol)
+            if cand is not None:
+                poly_cells.append((int(i + nx * (j + ny * k)), cand))
 
         # global vertex list: knot points used by cube nodes first, then the
         # points of the cut cells, merged within tolerance

@@ -80,3 +80,28 @@ def boundary_q(case, n, seed=0, delta=1e-6):
     q = np.concatenate(out)
     q += rng.uniform(-delta, delta, size=q.shape) * (rng.uniform(size=(len(q), 1)) < 0.5)
     return q
+
+
+def conditioned_modes(case, Q, ir=True, thresh=0.2):
+    """(N, B) mask of (q, mode) whose interpolated eigenvector is well
+    defined: for every vertex the Hermitian product with the pivot vertex's
+    row is at least `thresh` of the product of norms.  Where it is not, the
+    reference's antiphase picks a phase from rounding noise and two correct
+    implementations can disagree by O(1)."""
+    from oracle.oracle import Oracle
+
+    rec = Oracle(case["tables"]).move_locate(Q, ir=ir)
+    v = case["v"].reshape(len(case["v"]), case["v"].shape[1], -1)
+    N, B = len(Q), v.shape[1]
+    ok = np.ones((N, B), bool)
+    piv = v[rec["vertex"][:, 0]]
+    pn = np.linalg.norm(piv, axis=-1)
+    for x in range(1, 8):
+        has = rec["n_weights"] > x
+        if not has.any():
+            continue
+        vx = v[rec["vertex"][:, x]]
+        z = np.abs(np.einsum("nbe,nbe->nb", np.conj(piv), vx))
+        c = z / np.maximum(pn * np.linalg.norm(vx, axis=-1), 1e-300)
+        ok &= ~has[:, None] | (c >= thresh)
+    return ok & (rec["status"] == 0)[:, None]
