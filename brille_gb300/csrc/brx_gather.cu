@@ -16,6 +16,8 @@
 // (src/interpolator_gamma.tpp:49-139).
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "brx_kernels.h"
 
 namespace brx {
@@ -130,9 +132,93 @@ __host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int c
   return L;
 }
 
+// Store ne (1 or 3) interpolated elements; complex values as 2-wide vectors.
+template <typename Out, bool CPLX, typename Acc>
+__device__ __forceinline__ void store_group(Out* dst, const Acc* vr, const Acc* vi, int ne) {
+  if (CPLX) {
+    using V2 = typename std::conditional<std::is_same<Out, float>::value, float2, double2>::type;
+    V2* d = reinterpret_cast<V2*>(dst);
+    for (int k = 0; k < ne; ++k) {
+      V2 v;
+      v.x = (Out)vr[k];
+      v.y = (Out)vi[k];
+      d[k] = v;
+    }
+  } else {
+    for (int k = 0; k < ne; ++k) dst[k] = (Out)vr[k];
+  }
+}
+
+// One q's 3×3 matrix element group: weighted sum over the staged rows then
+// R·M·R⁻¹ (real lattice), Rᵀ·M·(R⁻¹)ᵀ (reciprocal) or R⁻¹·M·R (axial).
+// With s_e == nullptr the rows already carry their antiphase.
+template <typename Acc, bool CPLX, typename Out>
+__device__ void matrix_item(const GatherParams& p, const Acc* s_Y, const Acc* wj, const Acc* R, int ident, bool gamma,
+                            int pivot, int nslot, int MB, int s, int b, int e0, Out* dst, const Acc* s_e = nullptr) {
+  using A = Ar<Acc>;
+  constexpr int comps = CPLX ? 2 : 1;
+  Acc vr[9], vi[9];
+  for (int k = 0; k < 9; ++k) { vr[k] = 0; vi[k] = 0; }
+  for (int x = pivot; x < nslot; ++x) {
+    const Acc wx = wj[x];
+    if (wx == (Acc)0) continue;
+    const Acc er = s_e ? s_e[2 * (x * MB + b)] : (Acc)1, ei = s_e ? s_e[2 * (x * MB + b) + 1] : (Acc)0;
+    const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
+    const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+    for (int k = 0; k < 9; ++k) {
+      const Acc dr = y[k * comps];
+      if (CPLX) {
+        const Acc di = y[k * comps + 1];
+        vr[k] = A::add(vr[k], A::sub(A::mul(wr, dr), A::mul(wi, di)));
+        vi[k] = A::add(vi[k], A::add(A::mul(wr, di), A::mul(wi, dr)));
+      } else {
+        vr[k] = A::add(vr[k], A::mul(wx, dr));
+      }
+    }
+  }
+  if (p.rot_mode != ROT_NONE && !gamma && !ident) {
+    const Acc* Ri = R + 9;
+    Acc Lm[9], Rm[9];
+    if (p.rot_mode == ROT_RECIP) {
+      for (int a = 0; a < 3; ++a)
+        for (int c = 0; c < 3; ++c) { Lm[3 * a + c] = R[3 * c + a]; Rm[3 * a + c] = Ri[3 * c + a]; }
+    } else if (p.rot_mode == ROT_AXIAL) {
+      for (int k = 0; k < 9; ++k) { Lm[k] = Ri[k]; Rm[k] = R[k]; }
+    } else {
+      for (int k = 0; k < 9; ++k) { Lm[k] = R[k]; Rm[k] = Ri[k]; }
+    }
+    Acc Tr[9], Ti[9];
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) {
+        Acc sr = 0, si = 0;
+        for (int k = 0; k < 3; ++k) {
+          sr = A::add(sr, A::mul(vr[3 * a + k], Rm[3 * k + c]));
+          si = A::add(si, A::mul(vi[3 * a + k], Rm[3 * k + c]));
+        }
+        Tr[3 * a + c] = sr;
+        Ti[3 * a + c] = si;
+      }
+    for (int a = 0; a < 3; ++a)
+      for (int c = 0; c < 3; ++c) {
+        Acc sr = 0, si = 0;
+        for (int k = 0; k < 3; ++k) {
+          sr = A::add(sr, A::mul(Lm[3 * a + k], Tr[3 * k + c]));
+          si = A::add(si, A::mul(Lm[3 * a + k], Ti[3 * k + c]));
+        }
+        vr[3 * a + c] = sr;
+        vi[3 * a + c] = si;
+      }
+  }
+  for (int k = 0; k < 9; ++k) {
+    dst[(e0 + k) * comps] = (Out)vr[k];
+    if (CPLX) dst[(e0 + k) * comps + 1] = (Out)vi[k];
+  }
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
 __global__ void __launch_bounds__(kGatherThreads)
 group_gather_kernel(GatherParams p) {
+  constexpr bool kRegTile = sizeof(Acc) == 4;
   using A = Ar<Acc>;
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
@@ -287,34 +373,135 @@ group_gather_kernel(GatherParams p) {
       }
       __syncthreads();
       // every q's rows for these modes: weighted sum, rotation, store
-      const int items = count * mb * G;
-      for (int it = tid; it < items; it += nth) {
-        const int gi = it % G;
-        const int jb = it / G;
-        const int b = jb % mb, j = jb / mb;
-        const long long qi = s_q[j];
-        const int bb = b0 + b;
-        const Acc* wj = s_w + 8 * j;
-        const bool rotate = p.rot_mode != ROT_NONE && (gamma || !s_id[j]);
-        const Acc* R = s_R + 18 * j;
-        const Acc* Ri = R + 9;
-        Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
-        int e0, ne;
-        if (gi < p.nsc) { e0 = gi; ne = 1; }
-        else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
-        else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
-        Acc vr[9], vi[9];
+      if (kRegTile) {
+        // fold the antiphase into the staged rows: Y' = e^{-iθ} Y
+        if (CPLX && p.phase_allowed) {
+          for (int it = tid; it < ns * mb * s; it += nth) {
+            const int e = it % s, rb = it / s;
+            const int b = rb % mb, x = pivot + rb / mb;
+            if (x == pivot) continue;
+            const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
+            Acc* y = s_Y + ((size_t)(x * MB + b) * s + e) * comps;
+            const Acc yr = y[0], yi = y[1];
+            y[0] = er * yr - ei * yi;
+            y[1] = er * yi + ei * yr;
+          }
+          __syncthreads();
+        }
+        const int nitem = mb * G;
+        int qsplit = (2 * nth + nitem - 1) / nitem;
+        if (qsplit > count) qsplit = count;
+        if (qsplit < 1) qsplit = 1;
+        for (int it = tid; it < nitem * qsplit; it += nth) {
+          const int item = it % nitem, qs = it / nitem;
+          const int b = item / G, gi = item % G;
+          const int bb = b0 + b;
+          int e0, ne;
+          if (gi < p.nsc) { e0 = gi; ne = 1; }
+          else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
+          else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
+          if (ne <= 3) {
+            Acc yr[8][3], yi[8][3];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) { vr[k] = 0; vi[k] = 0; }
-        for (int x = pivot; x < nslot; ++x) {
-          const Acc wx = wj[x];
-          if (wx == (Acc)0) continue;
-          const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
-          const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
-          const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+            for (int x = 0; x < 8; ++x)
 #pragma unroll
-          for (int k = 0; k < 9; ++k) {
-            if (k < ne) {
+              for (int k = 0; k < 3; ++k) {
+                const bool use = x >= pivot && x < nslot && k < ne;
+                const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0 + k) * comps;
+                yr[x][k] = use ? y[0] : (Acc)0;
+                yi[x][k] = (use && CPLX) ? y[1] : (Acc)0;
+              }
+            for (int j = qs; j < count; j += qsplit) {
+              const Acc* wj = s_w + 8 * j;
+              Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+              for (int x = 0; x < 8; ++x) {
+                const Acc wx = wj[x];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                  vr[k] += wx * yr[x][k];
+                  if (CPLX) vi[k] += wx * yi[x][k];
+                }
+              }
+              const long long qi = s_q[j];
+              Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
+              int de = e0;
+              if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
+                const Acc* R = s_R + 18 * j;
+                const Acc* Ri = R + 9;
+                const Acc* M = (gamma || p.rot_mode == ROT_AXIAL) ? Ri : R;
+                const bool tr_ = p.rot_mode == ROT_RECIP;
+                Acc tr[3], ti[3];
+#pragma unroll
+                for (int a2 = 0; a2 < 3; ++a2) {
+                  Acc sr = 0, si = 0;
+#pragma unroll
+                  for (int c = 0; c < 3; ++c) {
+                    const Acc m = tr_ ? M[3 * c + a2] : M[3 * a2 + c];
+                    sr += m * vr[c];
+                    if (CPLX) si += m * vi[c];
+                  }
+                  tr[a2] = sr;
+                  ti[a2] = si;
+                }
+                if (gamma) {
+                  const int k = gi - p.nsc;
+                  de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
+                  const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
+#pragma unroll
+                  for (int a2 = 0; a2 < 3; ++a2) {
+                    vr[a2] = pr * tr[a2] - pi * ti[a2];
+                    vi[a2] = pr * ti[a2] + pi * tr[a2];
+                  }
+                } else if (p.rot_mode == ROT_AXIAL) {
+                  const Acc dt = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                                 R[2] * (R[3] * R[7] - R[4] * R[6]);
+#pragma unroll
+                  for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = dt * tr[a2]; vi[a2] = dt * ti[a2]; }
+                } else {
+#pragma unroll
+                  for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = tr[a2]; vi[a2] = ti[a2]; }
+                }
+              }
+              store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
+            }
+            continue;
+          }
+          // 3×3 matrices: read the staged rows directly
+          for (int j = qs; j < count; j += qsplit)
+            matrix_item<Acc, CPLX, Out>(p, s_Y, s_w + 8 * j, s_R + 18 * j, s_id[j], gamma, pivot, nslot, MB, s, b,
+                                        e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
+        }
+      } else {
+        const int items = count * mb * G;
+        for (int it = tid; it < items; it += nth) {
+          const int gi = it % G;
+          const int jb = it / G;
+          const int b = jb % mb, j = jb / mb;
+          const long long qi = s_q[j];
+          const int bb = b0 + b;
+          const Acc* wj = s_w + 8 * j;
+          const bool rotate = p.rot_mode != ROT_NONE && (gamma || !s_id[j]);
+          const Acc* R = s_R + 18 * j;
+          const Acc* Ri = R + 9;
+          Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
+          int e0, ne;
+          if (gi < p.nsc) { e0 = gi; ne = 1; }
+          else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
+          else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
+          if (ne == 9) {
+            matrix_item<Acc, CPLX, Out>(p, s_Y, wj, R, s_id[j], gamma, pivot, nslot, MB, s, b, e0, dst, s_e);
+            continue;
+          }
+          Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+          // the reference's order: out += (w·e^{-iθ})·d over the weighted vertices
+          for (int x = pivot; x < nslot; ++x) {
+            const Acc wx = wj[x];
+            if (wx == (Acc)0) continue;
+            const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
+            const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
+            const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+            for (int k = 0; k < ne; ++k) {
               const Acc dr = y[k * comps];
               if (CPLX) {
                 const Acc di = y[k * comps + 1];
@@ -325,84 +512,47 @@ group_gather_kernel(GatherParams p) {
               }
             }
           }
-        }
-        int de = e0;
-        if (ne == 3 && rotate) {
-          Acc M[9];
-          Acc scale = 1;
-          if (p.rot_mode == ROT_RECIP) {
-            for (int a = 0; a < 3; ++a) for (int c = 0; c < 3; ++c) M[3 * a + c] = R[3 * c + a];
-          } else if (p.rot_mode == ROT_AXIAL) {
-            for (int k = 0; k < 9; ++k) M[k] = Ri[k];
-            scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
-                    R[2] * (R[3] * R[7] - R[4] * R[6]);
-          } else if (gamma) {
-            for (int k = 0; k < 9; ++k) M[k] = Ri[k];
-          } else {
-            for (int k = 0; k < 9; ++k) M[k] = R[k];
-          }
-          Acc tr[3], ti[3];
-          for (int a = 0; a < 3; ++a) {
-            Acc sr = 0, si = 0;
-            for (int c = 0; c < 3; ++c) {
-              sr = A::add(sr, A::mul(M[3 * a + c], vr[c]));
-              if (CPLX) si = A::add(si, A::mul(M[3 * a + c], vi[c]));
+          int de = e0;
+          if (ne == 3 && rotate) {
+            Acc M[9];
+            Acc scale = 1;
+            if (p.rot_mode == ROT_RECIP) {
+              for (int a2 = 0; a2 < 3; ++a2) for (int c = 0; c < 3; ++c) M[3 * a2 + c] = R[3 * c + a2];
+            } else if (p.rot_mode == ROT_AXIAL) {
+              for (int k = 0; k < 9; ++k) M[k] = Ri[k];
+              scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                      R[2] * (R[3] * R[7] - R[4] * R[6]);
+            } else if (gamma) {
+              for (int k = 0; k < 9; ++k) M[k] = Ri[k];
+            } else {
+              for (int k = 0; k < 9; ++k) M[k] = R[k];
             }
-            tr[a] = sr;
-            ti[a] = si;
-          }
-          if (gamma) {
-            const int k = gi - p.nsc;
-            de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
-            const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
-            for (int a = 0; a < 3; ++a) {
-              const Acc xr = A::sub(A::mul(pr, tr[a]), A::mul(pi, ti[a]));
-              const Acc xi = A::add(A::mul(pr, ti[a]), A::mul(pi, tr[a]));
-              tr[a] = xr;
-              ti[a] = xi;
-            }
-          } else if (p.rot_mode == ROT_AXIAL) {
-            for (int a = 0; a < 3; ++a) { tr[a] = A::mul(scale, tr[a]); ti[a] = A::mul(scale, ti[a]); }
-          }
-          for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
-        } else if (ne == 9 && rotate) {
-          Acc Lm[9], Rm[9];  // result = Lm · (X · Rm)
-          if (p.rot_mode == ROT_RECIP) {
-            for (int a = 0; a < 3; ++a)
-              for (int c = 0; c < 3; ++c) { Lm[3 * a + c] = R[3 * c + a]; Rm[3 * a + c] = Ri[3 * c + a]; }
-          } else if (p.rot_mode == ROT_AXIAL) {
-            for (int k = 0; k < 9; ++k) { Lm[k] = Ri[k]; Rm[k] = R[k]; }
-          } else {
-            for (int k = 0; k < 9; ++k) { Lm[k] = R[k]; Rm[k] = Ri[k]; }
-          }
-          Acc Tr[9], Ti[9];
-          for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) {
+            Acc tr[3], ti[3];
+            for (int a2 = 0; a2 < 3; ++a2) {
               Acc sr = 0, si = 0;
-              for (int k = 0; k < 3; ++k) {
-                sr = A::add(sr, A::mul(vr[3 * a + k], Rm[3 * k + c]));
-                si = A::add(si, A::mul(vi[3 * a + k], Rm[3 * k + c]));
+              for (int c = 0; c < 3; ++c) {
+                sr = A::add(sr, A::mul(M[3 * a2 + c], vr[c]));
+                if (CPLX) si = A::add(si, A::mul(M[3 * a2 + c], vi[c]));
               }
-              Tr[3 * a + c] = sr;
-              Ti[3 * a + c] = si;
+              tr[a2] = sr;
+              ti[a2] = si;
             }
-          for (int a = 0; a < 3; ++a)
-            for (int c = 0; c < 3; ++c) {
-              Acc sr = 0, si = 0;
-              for (int k = 0; k < 3; ++k) {
-                sr = A::add(sr, A::mul(Lm[3 * a + k], Tr[3 * k + c]));
-                si = A::add(si, A::mul(Lm[3 * a + k], Ti[3 * k + c]));
+            if (gamma) {
+              const int k = gi - p.nsc;
+              de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
+              const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
+              for (int a2 = 0; a2 < 3; ++a2) {
+                const Acc xr = A::sub(A::mul(pr, tr[a2]), A::mul(pi, ti[a2]));
+                const Acc xi = A::add(A::mul(pr, ti[a2]), A::mul(pi, tr[a2]));
+                tr[a2] = xr;
+                ti[a2] = xi;
               }
-              vr[3 * a + c] = sr;
-              vi[3 * a + c] = si;
+            } else if (p.rot_mode == ROT_AXIAL) {
+              for (int a2 = 0; a2 < 3; ++a2) { tr[a2] = A::mul(scale, tr[a2]); ti[a2] = A::mul(scale, ti[a2]); }
             }
-        }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          if (k < ne) {
-            dst[(de + k) * comps] = (Out)vr[k];
-            if (CPLX) dst[(de + k) * comps + 1] = (Out)vi[k];
+            for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = tr[a2]; vi[a2] = ti[a2]; }
           }
+          store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
         }
       }
       __syncthreads();
