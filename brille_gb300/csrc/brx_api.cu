@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -278,7 +279,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
 }
 
 size_t smem_budget(brx_handle* h) {
-  size_t b = 100 * 1024;
+  size_t b = 52 * 1024;
   if (h->smem_optin && b > h->smem_optin) b = h->smem_optin;
   return b;
 }
@@ -609,6 +610,75 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
     mm3(&h->rot_cart[9 * (size_t)j], t, G.lattice_from_xyz);
   }
   UP(h->rot_cart.data(), h->rot_cart.size(), g.rot_cart);
+  // FP32 screens of the locate stage (brx_locate.cu): face planes through
+  // (a, b, c) with orient3d = k·(h − n̂·x), and the wedge normals carried back
+  // through each operation, m = B⁻¹ W B n (FP64 here, rounded once to FP32)
+  {
+    std::vector<float> plane(4 * (size_t)G.n_faces), band(G.n_faces);
+    bool ok = g.t_main.rel < 0.5;
+    for (int f = 0; f < G.n_faces; ++f) {
+      const double* a3 = G.face_abc + 9 * f;
+      double u[3], v[3], n[3];
+      for (int i = 0; i < 3; ++i) { u[i] = a3[3 + i] - a3[i]; v[i] = a3[6 + i] - a3[i]; }
+      n[0] = u[1] * v[2] - u[2] * v[1];
+      n[1] = u[2] * v[0] - u[0] * v[2];
+      n[2] = u[0] * v[1] - u[1] * v[0];
+      const double k = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      if (!(k > 0)) ok = false;
+      double h = 0;
+      for (int i = 0; i < 3; ++i) { n[i] /= k; h += n[i] * a3[i]; }
+      for (int i = 0; i < 3; ++i) plane[4 * f + i] = (float)n[i];
+      plane[4 * f + 3] = (float)h;
+      // |orient3d| ≤ abs/(1−rel) is the tolerance band; as a distance, /k
+      band[f] = (float)(2.0 * g.t_main.abs_ / (1.0 - g.t_main.rel) / k);
+    }
+    const int nw = G.n_wedge;
+    std::vector<float> wm(3 * (size_t)nw * (G.n_ops + 1));
+    double Bm[9], Bi[9];
+    std::memcpy(Bm, G.outer_B, sizeof Bm);
+    // inverse of B (rows b1, b2, b3)
+    const double det = Bm[0] * (Bm[4] * Bm[8] - Bm[5] * Bm[7]) - Bm[1] * (Bm[3] * Bm[8] - Bm[5] * Bm[6]) +
+                       Bm[2] * (Bm[3] * Bm[7] - Bm[4] * Bm[6]);
+    Bi[0] = (Bm[4] * Bm[8] - Bm[5] * Bm[7]) / det;
+    Bi[1] = (Bm[2] * Bm[7] - Bm[1] * Bm[8]) / det;
+    Bi[2] = (Bm[1] * Bm[5] - Bm[2] * Bm[4]) / det;
+    Bi[3] = (Bm[5] * Bm[6] - Bm[3] * Bm[8]) / det;
+    Bi[4] = (Bm[0] * Bm[8] - Bm[2] * Bm[6]) / det;
+    Bi[5] = (Bm[2] * Bm[3] - Bm[0] * Bm[5]) / det;
+    Bi[6] = (Bm[3] * Bm[7] - Bm[4] * Bm[6]) / det;
+    Bi[7] = (Bm[1] * Bm[6] - Bm[0] * Bm[7]) / det;
+    Bi[8] = (Bm[0] * Bm[4] - Bm[1] * Bm[3]) / det;
+    for (int j = 0; j <= G.n_ops; ++j) {
+      double W[9];
+      for (int e = 0; e < 9; ++e) W[e] = j < G.n_ops ? (double)G.ops[9 * j + e] : (e % 4 == 0 ? 1.0 : 0.0);
+      for (int i = 0; i < nw; ++i) {
+        const double* n = G.wedge_normal + 3 * i;
+        double t1[3], t2[3], t3[3];
+        for (int r = 0; r < 3; ++r) t1[r] = Bm[3 * r] * n[0] + Bm[3 * r + 1] * n[1] + Bm[3 * r + 2] * n[2];
+        for (int r = 0; r < 3; ++r) t2[r] = W[3 * r] * t1[0] + W[3 * r + 1] * t1[1] + W[3 * r + 2] * t1[2];
+        for (int r = 0; r < 3; ++r) t3[r] = Bi[3 * r] * t2[0] + Bi[3 * r + 1] * t2[1] + Bi[3 * r + 2] * t2[2];
+        for (int r = 0; r < 3; ++r) wm[3 * ((size_t)j * nw + i) + r] = (float)t3[r];
+        // the margin assumes orthogonal operations: |m| = |n|
+        const double mn = std::sqrt(t3[0] * t3[0] + t3[1] * t3[1] + t3[2] * t3[2]);
+        const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+        if (std::fabs(mn - nn) > 1e-6 * (nn > 1 ? nn : 1)) ok = false;
+      }
+    }
+    double nmax = 0;
+    for (int i = 0; i < nw; ++i) {
+      const double* n = G.wedge_normal + 3 * i;
+      nmax = std::max(nmax, std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]));
+    }
+    if (nw > 0 && std::fabs(nmax - 1.0) > 1e-6) ok = false;  // the margin assumes unit normals
+    g.wedge_band32 = (float)(2.0 * g.t_main.abs_ / (1.0 - g.t_main.rel));
+    // BRX_EXACT_PREDICATES=1 turns the screens off (every predicate in FP64)
+    const char* env = std::getenv("BRX_EXACT_PREDICATES");
+    if (env && env[0] == '1') ok = false;
+    g.screen = ok ? 1 : 0;
+    UP(plane.data(), plane.size(), g.face_plane32);
+    UP(band.data(), band.size(), g.face_band32);
+    UP(wm.data(), wm.size(), g.wedge_m32);
+  }
 #undef UP
   // the host copy keeps only counts: no pointer into caller memory survives
   h->host_geom.face_abc = h->host_geom.face_normal = h->host_geom.face_tau_len = nullptr;

@@ -118,6 +118,14 @@ struct DevGeom {
   const int32_t* gamma_vidx;
   const double* gamma_vectors;
   const double* rot_cart;   // n_ops × 9: L·W·L⁻¹ for Cartesian Γ data
+  // FP32 screens (see brx_locate.cu): face planes n̂·x ≤ h with the o3d
+  // tolerance band expressed as a distance, and wedge normals carried back
+  // through every operation, m_ji = B⁻¹ W_j B n_i.
+  const float* face_plane32;   // n_faces × 4: n̂, h
+  const float* face_band32;    // n_faces: width of the tolerance band in distance
+  const float* wedge_m32;      // (n_ops + 1) × n_wedge × 3 (last block: identity)
+  float wedge_band32;          // width of the wedge tolerance band
+  int32_t screen;              // 0 disables the screens (exact FP64 everywhere)
   Tol t_main;               // (float_tolerance, digit)
   Tol t_def;                // (0, 1): the reference's default comparisons
 };

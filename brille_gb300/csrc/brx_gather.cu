@@ -106,12 +106,59 @@ __device__ __forceinline__ int perm_lookup(const GatherParams& p, long long i, l
   return -1;
 }
 
+// Shared-memory row of staged vertex data: s elements of St (complex: pairs)
+// padded so that consecutive rows start on different banks.
+template <typename St, bool CPLX>
+__host__ __device__ inline int row_stride(int s) {
+  return CPLX ? 2 * s + 2 : s + 1;  // in St units
+}
+
+template <typename Acc, typename St, bool CPLX>
+__device__ __forceinline__ void ldY(const St* y, Acc& re, Acc& im) {
+  if constexpr (std::is_same<St, __nv_bfloat16>::value) {
+    if (CPLX) {
+      const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(y));
+      re = (Acc)f.x;
+      im = (Acc)f.y;
+    } else {
+      re = (Acc)__bfloat162float(*y);
+      im = 0;
+    }
+  } else {
+    if (CPLX) {
+      using V2 = typename std::conditional<std::is_same<St, float>::value, float2, double2>::type;
+      const V2 v = *reinterpret_cast<const V2*>(y);
+      re = (Acc)v.x;
+      im = (Acc)v.y;
+    } else {
+      re = (Acc)*y;
+      im = 0;
+    }
+  }
+}
+
+// copy one complex or real element (global → shared) in the storage type
+template <typename St, bool CPLX>
+__device__ __forceinline__ void cpY(St* dst, const St* src) {
+  if constexpr (CPLX) {
+    if constexpr (std::is_same<St, float>::value) {
+      *reinterpret_cast<float2*>(dst) = __ldg(reinterpret_cast<const float2*>(src));
+    } else if constexpr (std::is_same<St, double>::value) {
+      *reinterpret_cast<double2*>(dst) = __ldg(reinterpret_cast<const double2*>(src));
+    } else {
+      *reinterpret_cast<__nv_bfloat162*>(dst) = *reinterpret_cast<const __nv_bfloat162*>(src);
+    }
+  } else {
+    *dst = src[0];
+  }
+}
+
 struct GroupLayout {
   size_t q, rot, ident, w, R, ph, pid, e, Y, total;
 };
 
-template <typename Acc>
-__host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int comps, int na) {
+template <typename Acc, typename St, bool CPLX>
+__host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int na) {
   GroupLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -127,7 +174,7 @@ __host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int c
   L.ph = take(sizeof(Acc) * 2 * (size_t)na * QM);
   L.pid = take(sizeof(int) * 8);
   L.e = take(sizeof(Acc) * 2 * 8 * (size_t)MB);
-  L.Y = take(sizeof(Acc) * 8 * (size_t)MB * s * comps);
+  L.Y = take(sizeof(St) * 8 * (size_t)MB * row_stride<St, CPLX>(s));
   L.total = (o + 15) & ~size_t(15);
   return L;
 }
@@ -149,12 +196,12 @@ __device__ __forceinline__ void store_group(Out* dst, const Acc* vr, const Acc* 
   }
 }
 
-// One q's 3×3 matrix element group: weighted sum over the staged rows then
-// R·M·R⁻¹ (real lattice), Rᵀ·M·(R⁻¹)ᵀ (reciprocal) or R⁻¹·M·R (axial).
-// With s_e == nullptr the rows already carry their antiphase.
-template <typename Acc, bool CPLX, typename Out>
-__device__ void matrix_item(const GatherParams& p, const Acc* s_Y, const Acc* wj, const Acc* R, int ident, bool gamma,
-                            int pivot, int nslot, int MB, int s, int b, int e0, Out* dst, const Acc* s_e = nullptr) {
+// One q's 3×3 matrix element group: weighted sum of the staged rows (with
+// their antiphase) then R·M·R⁻¹ (real lattice), Rᵀ·M·(R⁻¹)ᵀ (reciprocal) or
+// R⁻¹·M·R (axial).
+template <typename Acc, typename St, bool CPLX, typename Out>
+__device__ void matrix_item(const GatherParams& p, const St* s_Y, int rs, const Acc* s_e, const Acc* wj, const Acc* R,
+                            int ident, bool gamma, int pivot, int nslot, int MB, int b, int e0, Out* dst) {
   using A = Ar<Acc>;
   constexpr int comps = CPLX ? 2 : 1;
   Acc vr[9], vi[9];
@@ -162,13 +209,13 @@ __device__ void matrix_item(const GatherParams& p, const Acc* s_Y, const Acc* wj
   for (int x = pivot; x < nslot; ++x) {
     const Acc wx = wj[x];
     if (wx == (Acc)0) continue;
-    const Acc er = s_e ? s_e[2 * (x * MB + b)] : (Acc)1, ei = s_e ? s_e[2 * (x * MB + b) + 1] : (Acc)0;
+    const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
     const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
-    const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+    const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
     for (int k = 0; k < 9; ++k) {
-      const Acc dr = y[k * comps];
+      Acc dr, di;
+      ldY<Acc, St, CPLX>(y + k * comps, dr, di);
       if (CPLX) {
-        const Acc di = y[k * comps + 1];
         vr[k] = A::add(vr[k], A::sub(A::mul(wr, dr), A::mul(wi, di)));
         vi[k] = A::add(vi[k], A::add(A::mul(wr, di), A::mul(wi, dr)));
       } else {
@@ -215,20 +262,66 @@ __device__ void matrix_item(const GatherParams& p, const Acc* s_Y, const Acc* wj
   }
 }
 
+// Rotate (and for Γ permute and phase) one 3-vector of one q in place;
+// returns the destination element offset.
+template <typename Acc, bool CPLX>
+__device__ __forceinline__ int rotate_vector(const GatherParams& p, bool gamma, const Acc* R, const Acc* ph, int k,
+                                             int r_inv, int e0, Acc* vr, Acc* vi) {
+  using A = Ar<Acc>;
+  const Acc* Ri = R + 9;
+  const Acc* M = (gamma || p.rot_mode == ROT_AXIAL) ? Ri : R;
+  const bool tr_ = p.rot_mode == ROT_RECIP;
+  Acc tr[3], ti[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    Acc sr = 0, si = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const Acc m = tr_ ? M[3 * c + a] : M[3 * a + c];
+      sr = A::add(sr, A::mul(m, vr[c]));
+      if (CPLX) si = A::add(si, A::mul(m, vi[c]));
+    }
+    tr[a] = sr;
+    ti[a] = si;
+  }
+  int de = e0;
+  if (gamma) {
+    de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + r_inv);
+    const Acc pr = ph[0], pi = ph[1];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      vr[a] = A::sub(A::mul(pr, tr[a]), A::mul(pi, ti[a]));
+      vi[a] = A::add(A::mul(pr, ti[a]), A::mul(pi, tr[a]));
+    }
+  } else if (p.rot_mode == ROT_AXIAL) {
+    const Acc dt = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                   R[2] * (R[3] * R[7] - R[4] * R[6]);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { vr[a] = A::mul(dt, tr[a]); vi[a] = A::mul(dt, ti[a]); }
+  } else {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
+  }
+  return de;
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
 __global__ void __launch_bounds__(kGatherThreads)
 group_gather_kernel(GatherParams p) {
-  constexpr bool kRegTile = sizeof(Acc) == 4;
   using A = Ar<Acc>;
+  // FP32 arithmetic: rows held in registers across the q of a group.
+  // FP64: the reference's operation order, rows read from shared memory.
+  constexpr bool kRegTile = sizeof(Acc) == 4;
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ int s_desc[3];
   __shared__ int s_vid[8];
   __shared__ int s_meta[2];  // number of slots, pivot slot
   const int B = p.B, s = p.s, MB = p.MB, QM = p.qmax;
+  const int rs = row_stride<St, CPLX>(s);
   const bool gamma = p.rot_mode == ROT_GAMMA;
   const int na = gamma ? p.nvec : 0;
-  const GroupLayout L = group_layout<Acc>(QM, MB, s, comps, na);
+  const GroupLayout L = group_layout<Acc, St, CPLX>(QM, MB, s, na);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
   int* s_rot = reinterpret_cast<int*>(sm + L.rot);
   int* s_id = reinterpret_cast<int*>(sm + L.ident);
@@ -237,11 +330,13 @@ group_gather_kernel(GatherParams p) {
   Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
   int* s_pid = reinterpret_cast<int*>(sm + L.pid);
   Acc* s_e = reinterpret_cast<Acc*>(sm + L.e);
-  Acc* s_Y = reinterpret_cast<Acc*>(sm + L.Y);
+  St* s_Y = reinterpret_cast<St*>(sm + L.Y);
+  const St* data = reinterpret_cast<const St*>(p.data);
   const int G = p.nsc + p.nvec + p.nmat;
   const int n_groups = *p.n_groups;
   Out* out = reinterpret_cast<Out*>(p.out);
   const int tid = threadIdx.x, nth = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
 
   for (;;) {
     if (tid == 0) {
@@ -333,20 +428,16 @@ group_gather_kernel(GatherParams p) {
     // ---- blocks of modes ----
     for (int b0 = 0; b0 < B; b0 += MB) {
       const int mb = min(MB, B - b0);
-      // stage the vertex rows of slots pivot..nslot-1 (slots before the pivot
-      // carry zero weight for every q of the group)
       const int ns = nslot - pivot;
-      for (int it = tid; it < ns * mb * s; it += nth) {
-        const int e = it % s;
-        const int rb = it / s;
-        const int b = rb % mb, xs = rb / mb, x = pivot + xs;
+      // stage the vertex rows of slots pivot..nslot-1, one warp per row
+      // (slots before the pivot carry zero weight for every q of the group)
+      for (int r = warp; r < ns * mb; r += nwarp) {
+        const int b = r % mb, x = pivot + r / mb;
         const int pid = s_pid[x];
         const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b0 + b) : b0 + b;
-        Acc re, im;
-        Ld<St, CPLX>::get(p.data, ((long long)s_vid[x] * B + row) * s + e, re, im);
-        Acc* y = s_Y + ((size_t)(x * MB + b) * s + e) * comps;
-        y[0] = re;
-        if (CPLX) y[1] = im;
+        const St* src = data + ((long long)s_vid[x] * B + row) * s * comps;
+        St* dst = s_Y + (size_t)(x * MB + b) * rs;
+        for (int e = lane; e < s; e += 32) cpY<St, CPLX>(dst + e * comps, src + e * comps);
       }
       __syncthreads();
       // antiphase factors, one per (slot, mode), in the reference's sum order
@@ -354,11 +445,13 @@ group_gather_kernel(GatherParams p) {
         const int b = it % mb, x = pivot + it / mb;
         Acc er = 1, ei = 0;
         if (CPLX && p.phase_allowed && x != pivot) {
-          const Acc* a = s_Y + (size_t)(pivot * MB + b) * s * comps;
-          const Acc* c = s_Y + (size_t)(x * MB + b) * s * comps;
+          const St* a = s_Y + (size_t)(pivot * MB + b) * rs;
+          const St* c = s_Y + (size_t)(x * MB + b) * rs;
           Acc rd = 0, id = 0;
           for (int e = 0; e < s; ++e) {
-            const Acc ar = a[2 * e], ai = a[2 * e + 1], br = c[2 * e], bi = c[2 * e + 1];
+            Acc ar, ai, br, bi;
+            ldY<Acc, St, CPLX>(a + 2 * e, ar, ai);
+            ldY<Acc, St, CPLX>(c + 2 * e, br, bi);
             rd = A::add(rd, A::add(A::mul(ar, br), A::mul(ai, bi)));
             id = A::add(id, A::sub(A::mul(ar, bi), A::mul(ai, br)));
           }
@@ -372,23 +465,8 @@ group_gather_kernel(GatherParams p) {
         s_e[2 * (x * MB + b) + 1] = ei;
       }
       __syncthreads();
-      // every q's rows for these modes: weighted sum, rotation, store
+      const int nitem = mb * G;
       if (kRegTile) {
-        // fold the antiphase into the staged rows: Y' = e^{-iθ} Y
-        if (CPLX && p.phase_allowed) {
-          for (int it = tid; it < ns * mb * s; it += nth) {
-            const int e = it % s, rb = it / s;
-            const int b = rb % mb, x = pivot + rb / mb;
-            if (x == pivot) continue;
-            const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
-            Acc* y = s_Y + ((size_t)(x * MB + b) * s + e) * comps;
-            const Acc yr = y[0], yi = y[1];
-            y[0] = er * yr - ei * yi;
-            y[1] = er * yi + ei * yr;
-          }
-          __syncthreads();
-        }
-        const int nitem = mb * G;
         int qsplit = (2 * nth + nitem - 1) / nitem;
         if (qsplit > count) qsplit = count;
         if (qsplit < 1) qsplit = 1;
@@ -400,97 +478,65 @@ group_gather_kernel(GatherParams p) {
           if (gi < p.nsc) { e0 = gi; ne = 1; }
           else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
           else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
-          if (ne <= 3) {
-            Acc yr[8][3], yi[8][3];
-#pragma unroll
-            for (int x = 0; x < 8; ++x)
-#pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                const bool use = x >= pivot && x < nslot && k < ne;
-                const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0 + k) * comps;
-                yr[x][k] = use ? y[0] : (Acc)0;
-                yi[x][k] = (use && CPLX) ? y[1] : (Acc)0;
-              }
-            for (int j = qs; j < count; j += qsplit) {
-              const Acc* wj = s_w + 8 * j;
-              Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
-#pragma unroll
-              for (int x = 0; x < 8; ++x) {
-                const Acc wx = wj[x];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                  vr[k] += wx * yr[x][k];
-                  if (CPLX) vi[k] += wx * yi[x][k];
-                }
-              }
-              const long long qi = s_q[j];
-              Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
-              int de = e0;
-              if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
-                const Acc* R = s_R + 18 * j;
-                const Acc* Ri = R + 9;
-                const Acc* M = (gamma || p.rot_mode == ROT_AXIAL) ? Ri : R;
-                const bool tr_ = p.rot_mode == ROT_RECIP;
-                Acc tr[3], ti[3];
-#pragma unroll
-                for (int a2 = 0; a2 < 3; ++a2) {
-                  Acc sr = 0, si = 0;
-#pragma unroll
-                  for (int c = 0; c < 3; ++c) {
-                    const Acc m = tr_ ? M[3 * c + a2] : M[3 * a2 + c];
-                    sr += m * vr[c];
-                    if (CPLX) si += m * vi[c];
-                  }
-                  tr[a2] = sr;
-                  ti[a2] = si;
-                }
-                if (gamma) {
-                  const int k = gi - p.nsc;
-                  de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
-                  const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
-#pragma unroll
-                  for (int a2 = 0; a2 < 3; ++a2) {
-                    vr[a2] = pr * tr[a2] - pi * ti[a2];
-                    vi[a2] = pr * ti[a2] + pi * tr[a2];
-                  }
-                } else if (p.rot_mode == ROT_AXIAL) {
-                  const Acc dt = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
-                                 R[2] * (R[3] * R[7] - R[4] * R[6]);
-#pragma unroll
-                  for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = dt * tr[a2]; vi[a2] = dt * ti[a2]; }
-                } else {
-#pragma unroll
-                  for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = tr[a2]; vi[a2] = ti[a2]; }
-                }
-              }
-              store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
-            }
+          if (ne == 9) {
+            for (int j = qs; j < count; j += qsplit)
+              matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w + 8 * j, s_R + 18 * j, s_id[j], gamma, pivot,
+                                              nslot, MB, b, e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
             continue;
           }
-          // 3×3 matrices: read the staged rows directly
-          for (int j = qs; j < count; j += qsplit)
-            matrix_item<Acc, CPLX, Out>(p, s_Y, s_w + 8 * j, s_R + 18 * j, s_id[j], gamma, pivot, nslot, MB, s, b,
-                                        e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
+          // this (mode, element group)'s rows of every slot, antiphase applied
+          Acc yr[8][3], yi[8][3];
+#pragma unroll
+          for (int x = 0; x < 8; ++x) {
+            const bool usex = x >= pivot && x < nslot;
+            const Acc er = usex ? s_e[2 * (x * MB + b)] : (Acc)0;
+            const Acc ei = usex ? s_e[2 * (x * MB + b) + 1] : (Acc)0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              Acc dr = 0, di = 0;
+              if (usex && k < ne) ldY<Acc, St, CPLX>(s_Y + (size_t)(x * MB + b) * rs + (e0 + k) * comps, dr, di);
+              yr[x][k] = er * dr - ei * di;
+              yi[x][k] = er * di + ei * dr;
+            }
+          }
+          for (int j = qs; j < count; j += qsplit) {
+            const Acc* wj = s_w + 8 * j;
+            Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+            for (int x = 0; x < 8; ++x) {
+              const Acc wx = wj[x];
+#pragma unroll
+              for (int k = 0; k < 3; ++k) {
+                vr[k] += wx * yr[x][k];
+                if (CPLX) vi[k] += wx * yi[x][k];
+              }
+            }
+            Out* dst = out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps;
+            int de = e0;
+            if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
+              const int k = gi - p.nsc;
+              de = rotate_vector<Acc, CPLX>(p, gamma, s_R + 18 * j, s_ph + 2 * (j * na + k), k, s_rot[2 * j + 1],
+                                            e0, vr, vi);
+            }
+            store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
+          }
         }
       } else {
-        const int items = count * mb * G;
+        const int items = count * nitem;
         for (int it = tid; it < items; it += nth) {
           const int gi = it % G;
           const int jb = it / G;
           const int b = jb % mb, j = jb / mb;
-          const long long qi = s_q[j];
           const int bb = b0 + b;
           const Acc* wj = s_w + 8 * j;
-          const bool rotate = p.rot_mode != ROT_NONE && (gamma || !s_id[j]);
-          const Acc* R = s_R + 18 * j;
-          const Acc* Ri = R + 9;
-          Out* dst = out + ((size_t)qi * B + bb) * (size_t)s * comps;
+          Out* dst = out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps;
           int e0, ne;
           if (gi < p.nsc) { e0 = gi; ne = 1; }
           else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
           else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
           if (ne == 9) {
-            matrix_item<Acc, CPLX, Out>(p, s_Y, wj, R, s_id[j], gamma, pivot, nslot, MB, s, b, e0, dst, s_e);
+            matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, wj, s_R + 18 * j, s_id[j], gamma, pivot, nslot, MB, b,
+                                            e0, dst);
             continue;
           }
           Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
@@ -500,11 +546,11 @@ group_gather_kernel(GatherParams p) {
             if (wx == (Acc)0) continue;
             const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
             const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
-            const Acc* y = s_Y + ((size_t)(x * MB + b) * s + e0) * comps;
+            const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
             for (int k = 0; k < ne; ++k) {
-              const Acc dr = y[k * comps];
+              Acc dr, di;
+              ldY<Acc, St, CPLX>(y + k * comps, dr, di);
               if (CPLX) {
-                const Acc di = y[k * comps + 1];
                 vr[k] = A::add(vr[k], A::sub(A::mul(wr, dr), A::mul(wi, di)));
                 vi[k] = A::add(vi[k], A::add(A::mul(wr, di), A::mul(wi, dr)));
               } else {
@@ -513,44 +559,10 @@ group_gather_kernel(GatherParams p) {
             }
           }
           int de = e0;
-          if (ne == 3 && rotate) {
-            Acc M[9];
-            Acc scale = 1;
-            if (p.rot_mode == ROT_RECIP) {
-              for (int a2 = 0; a2 < 3; ++a2) for (int c = 0; c < 3; ++c) M[3 * a2 + c] = R[3 * c + a2];
-            } else if (p.rot_mode == ROT_AXIAL) {
-              for (int k = 0; k < 9; ++k) M[k] = Ri[k];
-              scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
-                      R[2] * (R[3] * R[7] - R[4] * R[6]);
-            } else if (gamma) {
-              for (int k = 0; k < 9; ++k) M[k] = Ri[k];
-            } else {
-              for (int k = 0; k < 9; ++k) M[k] = R[k];
-            }
-            Acc tr[3], ti[3];
-            for (int a2 = 0; a2 < 3; ++a2) {
-              Acc sr = 0, si = 0;
-              for (int c = 0; c < 3; ++c) {
-                sr = A::add(sr, A::mul(M[3 * a2 + c], vr[c]));
-                if (CPLX) si = A::add(si, A::mul(M[3 * a2 + c], vi[c]));
-              }
-              tr[a2] = sr;
-              ti[a2] = si;
-            }
-            if (gamma) {
-              const int k = gi - p.nsc;
-              de = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
-              const Acc pr = s_ph[2 * (j * na + k)], pi = s_ph[2 * (j * na + k) + 1];
-              for (int a2 = 0; a2 < 3; ++a2) {
-                const Acc xr = A::sub(A::mul(pr, tr[a2]), A::mul(pi, ti[a2]));
-                const Acc xi = A::add(A::mul(pr, ti[a2]), A::mul(pi, tr[a2]));
-                tr[a2] = xr;
-                ti[a2] = xi;
-              }
-            } else if (p.rot_mode == ROT_AXIAL) {
-              for (int a2 = 0; a2 < 3; ++a2) { tr[a2] = A::mul(scale, tr[a2]); ti[a2] = A::mul(scale, ti[a2]); }
-            }
-            for (int a2 = 0; a2 < 3; ++a2) { vr[a2] = tr[a2]; vi[a2] = ti[a2]; }
+          if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
+            const int k = gi - p.nsc;
+            de = rotate_vector<Acc, CPLX>(p, gamma, s_R + 18 * j, s_ph + 2 * (j * na + k), k, s_rot[2 * j + 1], e0,
+                                          vr, vi);
           }
           store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
         }
@@ -560,14 +572,16 @@ group_gather_kernel(GatherParams p) {
   }
 }
 
-template <typename Acc>
-static size_t layout_bytes(const GatherParams& p, bool cplx, int MB) {
+template <typename Acc, typename St, bool CPLX>
+static size_t layout_bytes(const GatherParams& p, int MB) {
   const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
-  return group_layout<Acc>(p.qmax, MB, p.s, cplx ? 2 : 1, na).total;
+  return group_layout<Acc, St, CPLX>(p.qmax, MB, p.s, na).total;
 }
 
 size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB) {
-  return store_kind == ST_F64 ? layout_bytes<double>(p, cplx, MB) : layout_bytes<float>(p, cplx, MB);
+  if (store_kind == ST_F64) return cplx ? layout_bytes<double, double, true>(p, MB) : layout_bytes<double, double, false>(p, MB);
+  if (store_kind == ST_F32) return cplx ? layout_bytes<float, float, true>(p, MB) : layout_bytes<float, float, false>(p, MB);
+  return cplx ? layout_bytes<float, __nv_bfloat16, true>(p, MB) : layout_bytes<float, __nv_bfloat16, false>(p, MB);
 }
 
 int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget) {
@@ -580,7 +594,7 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
 
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
-  const size_t smem = layout_bytes<Acc>(p, CPLX, p.MB);
+  const size_t smem = layout_bytes<Acc, St, CPLX>(p, p.MB);
   static bool configured = false;
   if (!configured) {
     cudaFuncSetAttribute(group_gather_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,

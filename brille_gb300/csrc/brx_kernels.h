@@ -9,7 +9,7 @@
 namespace brx {
 
 constexpr int kLocateThreads = 128;
-constexpr int kGatherThreads = 256;
+constexpr int kGatherThreads = 128;
 
 enum RotMode { ROT_NONE = 0, ROT_REAL = 1, ROT_RECIP = 2, ROT_AXIAL = 3, ROT_GAMMA = 4 };
 enum StoreKind { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };

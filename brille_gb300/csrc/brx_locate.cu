@@ -9,13 +9,29 @@
 // _inside_wedge_outer (src/bz.hpp:757-763), PolyTrellis::node_subscript
 // (src/trellis_poly.hpp:382-434), CubeNode/PolyNode::indices_weights
 // (src/trellis_node.hpp:132-149, 275-364).
+#include <cstdint>
+
 #include "brx_device.cuh"
 #include "brx_kernels.h"
 #include "../../include/brx.h"
 
 namespace brx {
 
+// FP32 screens.  A face test or a wedge test evaluated in FP32 decides the
+// exact FP64 predicate whenever the FP32 value lies outside an error margin
+// around the predicate's tolerance band; only the undecided cases are
+// evaluated exactly.  The decision is therefore the FP64 one in every case,
+// and the first-match orders of the reference are kept.
+//
+// Margin: with unit normals and |x|₁ = Σ|x_i|, an FP32 dot product of
+// rounded operands is within 8 ε₃₂ (|x|₁ + |h|) of the exact value; 3e-6
+// covers that with a factor of over five.
+__device__ __forceinline__ float screen_margin(float x1, float h) { return 3e-6f * (x1 + fabsf(h) + 1e-6f); }
+
 struct SmemZone {
+  float* plane;     // n_faces × 4
+  float* band;      // n_faces
+  float* wm;        // (n_ops + 1) × n_wedge × 3
   double* abc;      // n_faces × 9
   double* normal;   // n_faces × 3
   double* tau_len;  // n_faces
@@ -25,7 +41,7 @@ struct SmemZone {
   int32_t* opinv;   // n_ops
 };
 
-__device__ bool inside_all_faces(const DevGeom& g, const SmemZone& z, const double x[3]) {
+__device__ bool inside_all_faces_exact(const DevGeom& g, const SmemZone& z, const double x[3]) {
   double vmin = 0.0;
   for (int f = 0; f < g.n_faces; ++f) {
     const double* abc = z.abc + 9 * f;
@@ -33,6 +49,30 @@ __device__ bool inside_all_faces(const DevGeom& g, const SmemZone& z, const doub
     if (f == 0 || o < vmin) vmin = o;
   }
   return vmin > 0 || approx(vmin, 0.0, g.t_main);
+}
+
+// point_inside_all_planes with the FP32 screen: −1 definitely outside,
+// +1 definitely inside, 0 undecided
+__device__ __forceinline__ int screen_faces(const DevGeom& g, const SmemZone& z, const double x[3]) {
+  const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+  const float xa = fabsf(x0) + fabsf(x1) + fabsf(x2);
+  int all_in = 1;
+  for (int f = 0; f < g.n_faces; ++f) {
+    const float* P = z.plane + 4 * f;
+    const float d = P[3] - (P[0] * x0 + P[1] * x1 + P[2] * x2);  // k_f·d = orient3d
+    const float m = screen_margin(xa, P[3]);
+    if (d < -(m + z.band[f])) return -1;
+    if (!(d > m)) all_in = 0;
+  }
+  return all_in;
+}
+
+__device__ bool inside_all_faces(const DevGeom& g, const SmemZone& z, const double x[3]) {
+  if (g.screen) {
+    const int s = screen_faces(g, z, x);
+    if (s) return s > 0;
+  }
+  return inside_all_faces_exact(g, z, x);
 }
 
 // Returns 0 or BRX_ERR_MOVE_FAILED; q_out in conventional r.l.u.
@@ -110,9 +150,46 @@ __device__ bool inside_wedge(const DevGeom& g, const SmemZone& z, const double x
   return true;
 }
 
+// Can W_jᵀ q (x its Cartesian form) be inside the wedge?  False only when
+// some normal puts it outside by more than the margin and the tolerance band.
+__device__ __forceinline__ bool wedge_candidate(const DevGeom& g, const float* m, float x0, float x1, float x2,
+                                                float tol) {
+  bool all_ge = true, all_le = true;
+  for (int i = 0; i < g.n_wedge; ++i) {
+    const float d = m[3 * i] * x0 + m[3 * i + 1] * x1 + m[3 * i + 2] * x2;
+    if (d < -tol) all_ge = false;
+    if (d > tol) all_le = false;
+  }
+  return all_ge || (g.wedge_le_ge && all_le);
+}
+
 __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32_t rot[2]) {
   double x[3], qj[3];
   hkl_to_xyz(x, g.outer_B, q);
+  if (g.screen && g.n_wedge > 0) {
+    // exact tests for the screened-in operations only, in the reference's order
+    const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+    const float tol = screen_margin(fabsf(x0) + fabsf(x1) + fabsf(x2), 0.f) + g.wedge_band32;
+    if (wedge_candidate(g, z.wm + 3 * g.n_wedge * g.n_ops, x0, x1, x2, tol) && inside_wedge(g, z, x)) {
+      rot[0] = rot[1] = g.identity;
+      return 0;
+    }
+    for (int j = 0; j < g.n_ops; ++j) {
+      if (!wedge_candidate(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, tol)) continue;
+      const int32_t* W = z.ops + 9 * j;
+      int32_t Wt[9] = {W[0], W[3], W[6], W[1], W[4], W[7], W[2], W[5], W[8]};
+      matvec_i(qj, Wt, q);
+      double xj[3];
+      hkl_to_xyz(xj, g.outer_B, qj);
+      if (inside_wedge(g, z, xj)) {
+        q[0] = qj[0]; q[1] = qj[1]; q[2] = qj[2];
+        rot[1] = j;
+        rot[0] = z.opinv[j];
+        return 0;
+      }
+    }
+    return BRX_ERR_OUTSIDE_IR;
+  }
   if (inside_wedge(g, z, x)) {
     rot[0] = rot[1] = g.identity;
     return 0;
@@ -297,6 +374,11 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
   extern __shared__ double smem_d[];
   SmemZone z;
   double* p = smem_d;
+  float* fp = reinterpret_cast<float*>(p);
+  z.plane = fp; fp += 4 * g.n_faces;
+  z.band = fp; fp += g.n_faces;
+  z.wm = fp; fp += 3 * g.n_wedge * (g.n_ops + 1);
+  p = reinterpret_cast<double*>(((uintptr_t)fp + 15) & ~uintptr_t(15));
   z.abc = p; p += 9 * g.n_faces;
   z.normal = p; p += 3 * g.n_faces;
   z.tau_len = p; p += g.n_faces;
@@ -314,6 +396,11 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
   for (int i = threadIdx.x; i < 3 * g.n_wedge; i += blockDim.x) z.wedge[i] = g.wedge_normal[i];
   for (int i = threadIdx.x; i < 9 * g.n_ops; i += blockDim.x) z.ops[i] = g.ops[i];
   for (int i = threadIdx.x; i < g.n_ops; i += blockDim.x) z.opinv[i] = g.op_inverse[i];
+  if (g.screen) {
+    for (int i = threadIdx.x; i < 4 * g.n_faces; i += blockDim.x) z.plane[i] = g.face_plane32[i];
+    for (int i = threadIdx.x; i < g.n_faces; i += blockDim.x) z.band[i] = g.face_band32[i];
+    for (int i = threadIdx.x; i < 3 * g.n_wedge * (g.n_ops + 1); i += blockDim.x) z.wm[i] = g.wedge_m32[i];
+  }
   __syncthreads();
 
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -375,7 +462,8 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
 }
 
 size_t locate_smem_bytes(const DevGeom& g) {
-  return sizeof(double) * (13 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge) +
+  return sizeof(float) * (5 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge * (g.n_ops + 1)) + 16 +
+         sizeof(double) * (13 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge) +
          sizeof(int32_t) * (3 * (size_t)g.n_faces + 10 * (size_t)g.n_ops) + 16;
 }
 

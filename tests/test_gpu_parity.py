@@ -214,3 +214,20 @@ def test_permutation_table():
     assert rc == 0
     assert np.array_equal(gv, ov[:, :, 0])
     assert np.abs(gc.reshape(oc.shape) - oc).max() < 1e-12
+
+
+def test_fp32_screens_match_exact_predicates():
+    """The FP32 screens of the locate stage change no decision: a handle
+    created with BRX_EXACT_PREDICATES=1 (all predicates in FP64) returns the
+    same indices on points within 1e-6 r.l.u. of every kind of boundary."""
+    import os
+    c = crystal_case("hex16")
+    Q = np.concatenate([_queries(c, 4000, seed=21), boundary_q(c, 6000, seed=22, delta=1e-9)])
+    a = _grid(c).locate(Q)
+    os.environ["BRX_EXACT_PREDICATES"] = "1"
+    try:
+        b = _grid(c).locate(Q)
+    finally:
+        del os.environ["BRX_EXACT_PREDICATES"]
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
