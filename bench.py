@@ -35,11 +35,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOADS = {
-    # name: (crystal builder, node volume as a fraction of the zone, q half-range)
-    "hex16": ("hexagonal16", 2.4e-7, 2.0),
-    "hex16-small": ("hexagonal16", 1e-5, 2.0),
-    "diamond8": ("diamond_conventional", 1 / 5000, 1.0),
-    "diamond2": ("diamond_primitive", 1 / 5000, 1.0),
+    # name: (crystal builder, node volume as a fraction of the zone, q half-range, q per step)
+    "hex16": ("hexagonal16", 2.4e-7, 2.0, 10_000_000),
+    "hex16-small": ("hexagonal16", 1e-5, 2.0, 1 << 20),
+    "diamond8": ("diamond_conventional", 1 / 5000, 1.0, 1 << 22),
+    "diamond2": ("diamond_primitive", 1 / 5000, 1.0, 1 << 22),
 }
 
 
@@ -52,7 +52,7 @@ def build_workload(name):
     from brille_gb300.bz import BrillouinZone
     from brille_gb300.trellis import TrellisBuild
 
-    builder, fraction, qr = WORKLOADS[name]
+    builder, fraction, qr, _ = WORKLOADS[name]
     lat, masses = getattr(W, builder)()
     bz = BrillouinZone(lat)
     t = time.time()
@@ -190,7 +190,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hex16", choices=sorted(WORKLOADS))
-    ap.add_argument("--q-per-step", type=int, default=1 << 20)
+    ap.add_argument("--q-per-step", type=int, default=0, help="default: the workload's batch")
     ap.add_argument("--storage", default="f32", choices=["f32", "f64", "bf16"])
     ap.add_argument("--out-f64", action="store_true", help="float64/complex128 outputs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -221,7 +221,13 @@ def main():
     grid = BZTrellisQdc(wl["bz"], trellis=wl["tr"], device=local)
     grid.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage=args.storage)
     out_f32 = not args.out_f64
-    n = args.q_per_step
+    n = args.q_per_step or WORKLOADS[args.workload][3]
+    bq_in, bq_vals, bq_vecs = bytes_per_q(B, na, out_f32)
+    free, _ = torch.cuda.mem_get_info(dev)
+    fit = int(0.85 * (free - (2 << 30)) / (bq_vals + bq_vecs + 2 * 24 + 2 * 200))
+    if n > fit:
+        log(f"[setup] {n} q per step do not fit in HBM; using {fit}")
+        n = fit
     qr = wl["q_range"]
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
@@ -267,7 +273,6 @@ def main():
     value = world * n * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel
-    bq_in, bq_vals, bq_vecs = bytes_per_q(B, na, out_f32)
     stage_names = ["locate", "node_sort", "gather_values", "gather_vectors"]
     dom = int(np.argmax(stage_ms))
     per_q_bytes = {0: bq_in + 4 * 8 + 8 * 12 + 40, 1: 16, 2: bq_vals, 3: bq_vecs}[dom]
@@ -283,9 +288,9 @@ def main():
     # end to end through the public API with pinned host buffers
     e2e = None
     if args.e2e_steps > 0:
-        ne = n
+        ne = min(n, 1 << 20)
         Qh = torch.empty((ne, 3), dtype=torch.float64, pin_memory=True)
-        Qh.copy_(Qs[0].cpu())
+        Qh.copy_(Qs[0][:ne].cpu())
         vh = torch.empty((ne, B), dtype=fdt, pin_memory=True)
         ch = torch.empty((ne, B, na, 3), dtype=cdt, pin_memory=True)
         grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)

@@ -245,6 +245,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.w = s.r.w;
   p.rot = s.r.rot;
   p.q_ir = s.r.q_ir;
+  p.status = s.r.status;
   p.order = s.order;
   p.groups = s.groups;
   p.n_groups = s.n_groups;
@@ -387,7 +388,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     out_q += (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
     if (h->vecs.present) out_q += (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
   }
-  long long chunk = 1LL << 22;
+  long long chunk = 1LL << 24;
   if (o_host && out_q) chunk = std::max<long long>(1024, std::min<long long>(chunk, (512LL << 20) / (long long)out_q));
   if (chunk > n) chunk = n;
   brx_status st = ensure_scratch(h, chunk);

@@ -572,6 +572,43 @@ group_gather_kernel(GatherParams p) {
   }
 }
 
+// Scalar-only interpolators (eigenvalues): one thread per (q, branch),
+// out = Σ_x w_x d[v_x][perm_x(b)] in the reference's order.  The rows are
+// small enough to stay in L2, so no grouping is needed.
+template <typename Acc, typename St, bool CPLX, typename Out>
+__global__ void scalar_gather_kernel(GatherParams p) {
+  using A = Ar<Acc>;
+  constexpr int comps = CPLX ? 2 : 1;
+  const St* data = reinterpret_cast<const St*>(p.data);
+  Out* out = reinterpret_cast<Out*>(p.out);
+  const int B = p.B, s = p.s;
+  const long long total = p.n * (long long)B;
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    const long long qi = it / B;
+    const int b = (int)(it % B);
+    if (p.status[qi]) continue;
+    const int nw = p.nw[qi];
+    const int piv = p.vidx[8 * qi];
+    for (int e = 0; e < s; ++e) {
+      Acc vr = 0, vi = 0;
+      for (int x = 0; x < nw; ++x) {
+        const int v = p.vidx[8 * qi + x];
+        const int pid = perm_lookup(p, piv, v);
+        const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b) : b;
+        Acc dr, di;
+        Ld<St, CPLX>::get(data, ((long long)v * B + row) * s + e, dr, di);
+        const Acc w = (Acc)p.w[8 * qi + x];
+        vr = A::add(vr, A::mul(w, dr));
+        if (CPLX) vi = A::add(vi, A::mul(w, di));
+      }
+      Out* dst = out + ((size_t)qi * B + b) * (size_t)s * comps + (size_t)e * comps;
+      dst[0] = (Out)vr;
+      if (CPLX) dst[1] = (Out)vi;
+    }
+  }
+}
+
 template <typename Acc, typename St, bool CPLX>
 static size_t layout_bytes(const GatherParams& p, int MB) {
   const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
@@ -594,6 +631,13 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
 
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
+  if (p.nvec == 0 && p.nmat == 0 && !p.phase_allowed) {
+    long long total = p.n * (long long)p.B;
+    long long blocks = (total + 255) / 256;
+    if (blocks > (long long)num_sms * 16) blocks = (long long)num_sms * 16;
+    scalar_gather_kernel<Acc, St, CPLX, Out><<<(unsigned)blocks, 256, 0, s>>>(p);
+    return;
+  }
   const size_t smem = layout_bytes<Acc, St, CPLX>(p, p.MB);
   static bool configured = false;
   if (!configured) {

@@ -29,6 +29,7 @@ struct GatherParams {
   const double* w;
   const int32_t* rot;
   const double* q_ir;
+  const int32_t* status;     // per-q status (scalar path)
   const int32_t* order;      // key-sorted q indices
   const GroupDesc* groups;   // work descriptors
   const int32_t* n_groups;   // device count of descriptors
