@@ -280,7 +280,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
 }
 
 size_t smem_budget(brx_handle* h) {
-  size_t b = 52 * 1024;
+  size_t b = 56 * 1024;
   if (h->smem_optin && b > h->smem_optin) b = h->smem_optin;
   return b;
 }

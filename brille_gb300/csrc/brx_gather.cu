@@ -154,7 +154,7 @@ __device__ __forceinline__ void cpY(St* dst, const St* src) {
 }
 
 struct GroupLayout {
-  size_t q, rot, ident, w, R, ph, pid, e, Y, total;
+  size_t q, rot, ident, w, R, ph, e, Y, total;
 };
 
 template <typename Acc, typename St, bool CPLX>
@@ -172,9 +172,8 @@ __host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int n
   L.w = take(sizeof(Acc) * 8 * QM);
   L.R = take(sizeof(Acc) * 18 * QM);
   L.ph = take(sizeof(Acc) * 2 * (size_t)na * QM);
-  L.pid = take(sizeof(int) * 8);
   L.e = take(sizeof(Acc) * 2 * 8 * (size_t)MB);
-  L.Y = take(sizeof(St) * 8 * (size_t)MB * row_stride<St, CPLX>(s));
+  L.Y = take(sizeof(St) * 2 * 8 * (size_t)MB * row_stride<St, CPLX>(s));
   L.total = (o + 15) & ~size_t(15);
   return L;
 }
@@ -305,6 +304,87 @@ __device__ __forceinline__ int rotate_vector(const GatherParams& p, bool gamma, 
   return de;
 }
 
+// Asynchronous global → shared copy of one staged element (cp.async):
+// 4, 8 or 16 bytes, so the copy of the next block of rows overlaps compute.
+template <typename St, bool CPLX>
+__device__ __forceinline__ void cp_async_elem(St* dst, const St* src) {
+  constexpr int bytes = (CPLX ? 2 : 1) * (int)sizeof(St);
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (bytes == 16) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+  } else if constexpr (bytes == 8) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+  } else if constexpr (bytes == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+  } else {
+    *dst = *src;  // 2-byte elements: a plain copy
+  }
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Group bookkeeping kept in shared memory for the current and the next group.
+struct GroupInfo {
+  int key, start, count;  // count < 0: no group
+  int nslot, pivot;
+  int vid[8];
+  int pid[8];
+};
+
+// Warp 0 takes the next work descriptor and decodes its vertex slots.
+__device__ __forceinline__ void fetch_group(const GatherParams& p, int n_groups, GroupInfo* gi, int lane) {
+  int g = 0;
+  if (lane == 0) g = atomicAdd(p.counter, 1);
+  g = __shfl_sync(0xffffffffu, g, 0);
+  if (g >= n_groups) {
+    if (lane == 0) gi->count = -1;
+    return;
+  }
+  const GroupDesc d = p.groups[g];
+  int nslot, pivot, vid = 0;
+  if (d.key < 8 * p.n_cube) {
+    pivot = d.key & 7;
+    nslot = 8;
+    if (lane < 8) vid = __ldg(p.cube_vertices + 8 * (long long)(d.key >> 3) + 7 - lane);
+  } else {
+    const long long t = (d.key - 8LL * p.n_cube) >> 2;
+    pivot = (int)((d.key - 8LL * p.n_cube) & 3);
+    nslot = 4;
+    if (lane < 4) vid = __ldg(p.tet_vertices + 4 * t + lane);
+  }
+  const int pv = __shfl_sync(0xffffffffu, vid, pivot);
+  if (lane < 8) {
+    gi->vid[lane] = vid;
+    gi->pid[lane] = lane < nslot ? perm_lookup(p, pv, vid) : -1;
+  }
+  if (lane == 0) {
+    gi->key = d.key;
+    gi->start = d.start;
+    gi->count = d.count;
+    gi->nslot = nslot;
+    gi->pivot = pivot;
+  }
+}
+
+// Issue the asynchronous copies of rows [b0, b0 + mb) of the group's used
+// slots into a staging buffer; one warp per row.
+template <typename St, bool CPLX>
+__device__ __forceinline__ void issue_rows(const GatherParams& p, const GroupInfo& gi, int b0, int mb, int MB, int rs,
+                                           St* Y, int warp, int lane, int nwarp) {
+  constexpr int comps = CPLX ? 2 : 1;
+  const St* data = reinterpret_cast<const St*>(p.data);
+  const int s = p.s, B = p.B;
+  const int ns = gi.nslot - gi.pivot;
+  for (int r = warp; r < ns * mb; r += nwarp) {
+    const int b = r % mb, x = gi.pivot + r / mb;
+    const int pid = gi.pid[x];
+    const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b0 + b) : b0 + b;
+    const St* src = data + ((long long)gi.vid[x] * B + row) * s * comps;
+    St* dst = Y + (size_t)(x * MB + b) * rs;
+    for (int e = lane; e < s; e += 32) cp_async_elem<St, CPLX>(dst + e * comps, src + e * comps);
+  }
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
 __global__ void __launch_bounds__(kGatherThreads)
 group_gather_kernel(GatherParams p) {
@@ -314,9 +394,7 @@ group_gather_kernel(GatherParams p) {
   constexpr bool kRegTile = sizeof(Acc) == 4;
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ int s_desc[3];
-  __shared__ int s_vid[8];
-  __shared__ int s_meta[2];  // number of slots, pivot slot
+  __shared__ GroupInfo s_g[2];
   const int B = p.B, s = p.s, MB = p.MB, QM = p.qmax;
   const int rs = row_stride<St, CPLX>(s);
   const bool gamma = p.rot_mode == ROT_GAMMA;
@@ -328,53 +406,29 @@ group_gather_kernel(GatherParams p) {
   Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
   Acc* s_R = reinterpret_cast<Acc*>(sm + L.R);
   Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
-  int* s_pid = reinterpret_cast<int*>(sm + L.pid);
   Acc* s_e = reinterpret_cast<Acc*>(sm + L.e);
-  St* s_Y = reinterpret_cast<St*>(sm + L.Y);
-  const St* data = reinterpret_cast<const St*>(p.data);
+  St* const s_Y0 = reinterpret_cast<St*>(sm + L.Y);
+  const size_t ybuf = (size_t)8 * MB * rs;
   const int G = p.nsc + p.nvec + p.nmat;
   const int n_groups = *p.n_groups;
   Out* out = reinterpret_cast<Out*>(p.out);
   const int tid = threadIdx.x, nth = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
+  const int nblk = (B + MB - 1) / MB;
+
+  if (warp == 0) fetch_group(p, n_groups, &s_g[0], lane);
+  __syncthreads();
+  if (s_g[0].count < 0) return;
+  issue_rows<St, CPLX>(p, s_g[0], 0, min(MB, B), MB, rs, s_Y0, warp, lane, nwarp);
+  cp_async_commit();
+  int cur = 0, buf = 0;
 
   for (;;) {
-    if (tid == 0) {
-      int g = atomicAdd(p.counter, 1);
-      if (g < n_groups) {
-        GroupDesc d = p.groups[g];
-        s_desc[0] = d.key;
-        s_desc[1] = d.start;
-        s_desc[2] = d.count;
-      } else {
-        s_desc[2] = -1;
-      }
-    }
-    __syncthreads();
-    const int count = s_desc[2];
-    if (count < 0) break;
-    const int key = s_desc[0], start = s_desc[1];
-    // ---- group prologue: vertex slots in weight order, pivot ----
-    if (tid < 8) {
-      int nslot, pivot, vid = 0;
-      if (key < 8 * p.n_cube) {
-        const int ni = key >> 3;
-        pivot = key & 7;
-        nslot = 8;
-        vid = __ldg(p.cube_vertices + 8 * (long long)ni + 7 - tid);
-      } else {
-        const long long t = (key - 8LL * p.n_cube) >> 2;
-        pivot = (int)((key - 8LL * p.n_cube) & 3);
-        nslot = 4;
-        vid = tid < 4 ? __ldg(p.tet_vertices + 4 * t + tid) : 0;
-      }
-      s_vid[tid] = vid;
-      if (tid == 0) { s_meta[0] = nslot; s_meta[1] = pivot; }
-    }
-    __syncthreads();
-    const int nslot = s_meta[0], pivot = s_meta[1];
-    if (tid < nslot) s_pid[tid] = perm_lookup(p, s_vid[pivot], s_vid[tid]);
-    // per-q records: weights by slot, R and R⁻¹, Γ phases
+    const GroupInfo& gc = s_g[cur];
+    // the next group is taken now so that its first rows can load early
+    if (warp == 0) fetch_group(p, n_groups, &s_g[cur ^ 1], lane);
+    const int count = gc.count, start = gc.start, nslot = gc.nslot, pivot = gc.pivot;
+    // per-q records: weights by slot, R and R⁻¹
     for (int j = tid; j < count; j += nth) {
       const long long qi = p.order[start + j];
       s_q[j] = qi;
@@ -384,7 +438,7 @@ group_gather_kernel(GatherParams p) {
         const int v = p.vidx[8 * qi + k];
         const Acc wk = (Acc)p.w[8 * qi + k];
         for (int x = 0; x < nslot; ++x)
-          if (s_vid[x] == v) wsl[x] = wk;
+          if (gc.vid[x] == v) wsl[x] = wk;
       }
       for (int x = 0; x < 8; ++x) s_w[8 * j + x] = wsl[x];
       int r0 = 0, r1 = 0, ident = 1;
@@ -425,21 +479,24 @@ group_gather_kernel(GatherParams p) {
         s_ph[2 * it + 1] = (Acc)sn;
       }
     }
-    // ---- blocks of modes ----
-    for (int b0 = 0; b0 < B; b0 += MB) {
+    // ---- blocks of modes, double-buffered ----
+    for (int bi = 0; bi < nblk; ++bi) {
+      const int b0 = bi * MB;
       const int mb = min(MB, B - b0);
-      const int ns = nslot - pivot;
-      // stage the vertex rows of slots pivot..nslot-1, one warp per row
-      // (slots before the pivot carry zero weight for every q of the group)
-      for (int r = warp; r < ns * mb; r += nwarp) {
-        const int b = r % mb, x = pivot + r / mb;
-        const int pid = s_pid[x];
-        const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b0 + b) : b0 + b;
-        const St* src = data + ((long long)s_vid[x] * B + row) * s * comps;
-        St* dst = s_Y + (size_t)(x * MB + b) * rs;
-        for (int e = lane; e < s; e += 32) cpY<St, CPLX>(dst + e * comps, src + e * comps);
-      }
+      cp_async_wait_all();
       __syncthreads();
+      {
+        // rows for the following block: this group's next block, or the
+        // first block of the next group
+        const GroupInfo& gn = s_g[cur ^ 1];
+        if (bi + 1 < nblk)
+          issue_rows<St, CPLX>(p, gc, b0 + MB, min(MB, B - b0 - MB), MB, rs, (s_Y0 + (buf ^ 1) * ybuf), warp, lane, nwarp);
+        else if (gn.count >= 0)
+          issue_rows<St, CPLX>(p, gn, 0, min(MB, B), MB, rs, (s_Y0 + (buf ^ 1) * ybuf), warp, lane, nwarp);
+        cp_async_commit();
+      }
+      const St* s_Y = s_Y0 + buf * ybuf;
+      const int ns = nslot - pivot;
       // antiphase factors, one per (slot, mode), in the reference's sum order
       for (int it = tid; it < ns * mb; it += nth) {
         const int b = it % mb, x = pivot + it / mb;
@@ -449,11 +506,11 @@ group_gather_kernel(GatherParams p) {
           const St* c = s_Y + (size_t)(x * MB + b) * rs;
           Acc rd = 0, id = 0;
           for (int e = 0; e < s; ++e) {
-            Acc ar, ai, br, bi;
+            Acc ar, ai, br, bi2;
             ldY<Acc, St, CPLX>(a + 2 * e, ar, ai);
-            ldY<Acc, St, CPLX>(c + 2 * e, br, bi);
-            rd = A::add(rd, A::add(A::mul(ar, br), A::mul(ai, bi)));
-            id = A::add(id, A::sub(A::mul(ar, bi), A::mul(ai, br)));
+            ldY<Acc, St, CPLX>(c + 2 * e, br, bi2);
+            rd = A::add(rd, A::add(A::mul(ar, br), A::mul(ai, bi2)));
+            id = A::add(id, A::sub(A::mul(ar, bi2), A::mul(ai, br)));
           }
           const Acc mag = sqrt(A::add(A::mul(rd, rd), A::mul(id, id)));
           if (mag > (Acc)0) {
@@ -567,9 +624,13 @@ group_gather_kernel(GatherParams p) {
           store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
         }
       }
-      __syncthreads();
+      buf ^= 1;
     }
+    __syncthreads();  // this group's records and rows are no longer read
+    cur ^= 1;
+    if (s_g[cur].count < 0) break;
   }
+  cp_async_wait_all();
 }
 
 // Scalar-only interpolators (eigenvalues): one thread per (q, branch),
