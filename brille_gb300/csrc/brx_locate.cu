@@ -209,10 +209,16 @@ __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32
   return BRX_ERR_OUTSIDE_IR;
 }
 
+// find_bin: the first knot greater than x (std::find_if in the reference)
+// found by bisection, which gives the same index because knots increase
+// strictly; a NaN compares false everywhere and lands past the end as there.
 __device__ __forceinline__ int find_bin(const double* e, int n, double x) {
-  int d = n;
-  for (int i = 0; i < n; ++i)
-    if (__ldg(e + i) > x) { d = i; break; }
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(e + mid) > x) hi = mid; else lo = mid + 1;
+  }
+  int d = lo;
   if (d > n - 1 && x < __ldg(e)) d = 0;
   return d > 0 ? d - 1 : d;
 }
