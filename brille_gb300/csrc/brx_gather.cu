@@ -473,10 +473,18 @@ group_gather_kernel(GatherParams p) {
         dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 1], d[1]));
         dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 2], d[2]));
         const double frac = dq - rint(dq);  // e^{2πi n} = 1 exactly
-        double sn, cs;
-        sincospi(2.0 * frac, &sn, &cs);
-        s_ph[2 * it] = (Acc)cs;
-        s_ph[2 * it + 1] = (Acc)sn;
+        if constexpr (sizeof(Acc) == 4) {
+          // FP32 arithmetic: the reduced argument is exact, sin/cos in FP32
+          float sn, cs;
+          sincospif(2.0f * (float)frac, &sn, &cs);
+          s_ph[2 * it] = cs;
+          s_ph[2 * it + 1] = sn;
+        } else {
+          double sn, cs;
+          sincospi(2.0 * frac, &sn, &cs);
+          s_ph[2 * it] = (Acc)cs;
+          s_ph[2 * it + 1] = (Acc)sn;
+        }
       }
     }
     // ---- blocks of modes, double-buffered ----
