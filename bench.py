@@ -38,6 +38,8 @@ WORKLOADS = {
     # name: (crystal builder, node volume as a fraction of the zone, q half-range, q per step)
     "hex16": ("hexagonal16", 2.4e-7, 2.0, 10_000_000),
     "hex16-small": ("hexagonal16", 1e-5, 2.0, 1 << 20),
+    # small trellis and batch with the group sizes of the full runs, for ncu
+    "hex16-profile": ("hexagonal16", 1e-4, 2.0, 1 << 17),
     "diamond8": ("diamond_conventional", 1 / 5000, 1.0, 1 << 22),
     "diamond2": ("diamond_primitive", 1 / 5000, 1.0, 1 << 22),
 }
@@ -261,7 +263,7 @@ def main():
         grid.sync(sp)
         torch.cuda.synchronize()
     launches = grid.launch_count() - l0
-    stage_ms, stage_q = grid.stage_times()
+    stage_ms, stage_q, stage_groups = grid.stage_times()
     grid.profile(False)
     ms = ev0.elapsed_time(ev1)
     if dist:
@@ -273,7 +275,7 @@ def main():
     value = world * n * args.steps / (ms / 1e3)
 
     # roofline of the dominant kernel
-    stage_names = ["locate", "node_sort", "gather_values", "gather_vectors"]
+    stage_names = ["locate", "grouping", "gather_values", "gather_vectors"]
     dom = int(np.argmax(stage_ms))
     per_q_bytes = {0: bq_in + 4 * 8 + 8 * 12 + 40, 1: 16, 2: bq_vals, 3: bq_vecs}[dom]
     achieved = per_q_bytes * stage_q / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
@@ -283,6 +285,7 @@ def main():
                     peak_source="measured" if peaks else "fallback", unit="GB/s",
                     frac=round(achieved / peak, 4), traffic=None,
                     algorithmic_bytes_per_q=per_q_bytes,
+                    q_per_group=round(stage_q / max(stage_groups, 1), 2),
                     stage_ms_per_step={k: round(v / args.steps, 3) for k, v in zip(stage_names, stage_ms)})
 
     # end to end through the public API with pinned host buffers

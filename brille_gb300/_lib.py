@@ -57,7 +57,7 @@ def load(build_if_missing=True):
     lib.brx_launch_count.restype = C.c_int64
     lib.brx_profile.argtypes = [h, C.c_int32]
     lib.brx_profile.restype = C.c_int
-    lib.brx_stage_times.argtypes = [h, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int64)]
+    lib.brx_stage_times.argtypes = [h, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.brx_stage_times.restype = C.c_int
     lib.brx_abi_version.argtypes = []
     lib.brx_abi_version.restype = C.c_int32

@@ -104,6 +104,9 @@ struct brx_handle {
   size_t ev_used = 0;
   double stage_ms[5] = {0, 0, 0, 0, 0};
   long long stage_q = 0;
+  long long stage_groups = 0;
+  std::vector<int32_t*> group_counts;  // pinned, one per profiled chunk
+  size_t group_used = 0;
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;
@@ -333,8 +336,19 @@ cudaEvent_t next_event(brx_handle* h) {
   return h->ev_pool[h->ev_used++];
 }
 
+int32_t* next_group_slot(brx_handle* h) {
+  if (h->group_used == h->group_counts.size()) {
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, sizeof(int32_t), cudaHostAllocDefault) != cudaSuccess) return nullptr;
+    h->group_counts.push_back(static_cast<int32_t*>(p));
+  }
+  return h->group_counts[h->group_used++];
+}
+
 // accumulate stage durations from the events recorded since the last call
 void harvest_events(brx_handle* h) {
+  for (size_t i = 0; i < h->group_used; ++i) h->stage_groups += *h->group_counts[i];
+  h->group_used = 0;
   for (size_t i = 0; i + 5 < h->ev_used + 1 && i + 4 < h->ev_used; i += 5) {
     for (int k = 0; k < 4; ++k) {
       float ms = 0.f;
@@ -472,7 +486,10 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       p.MB = gather_pick_modes(p, h->vecs.store, h->vecs.cplx, smem_budget(h));
       h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h), cs);
     }
-    if (ev[4]) cudaEventRecord(ev[4], cs);
+    if (ev[4]) {
+      cudaEventRecord(ev[4], cs);
+      if (int32_t* slot = next_group_slot(h)) cudaMemcpyAsync(slot, s.n_groups, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+    }
     BRX_CUDA(h, cudaGetLastError());
     if (o_host) {
       BRX_CUDA(h, cudaMemcpyAsync(static_cast<char*>(vals_out) + vrow * (size_t)base, vdst, vrow * (size_t)m,
@@ -716,6 +733,7 @@ void brx_destroy(brx_handle* h) {
   }
   for (auto& b : h->tables) b.release();
   for (auto e : h->ev_pool) cudaEventDestroy(e);
+  for (auto p : h->group_counts) cudaFreeHost(p);
   h->vals.data.release();
   h->vecs.data.release();
   h->perm_keys.release();
@@ -862,13 +880,16 @@ brx_status brx_profile(brx_handle* h, int32_t enable) {
   h->ev_used = 0;
   for (double& x : h->stage_ms) x = 0;
   h->stage_q = 0;
+  h->stage_groups = 0;
+  h->group_used = 0;
   return BRX_OK;
 }
 
-brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count) {
+brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count, int64_t* groups) {
   if (!h || !ms || n < 0) return BRX_ERR_INVALID_ARGUMENT;
   for (int i = 0; i < n && i < 4; ++i) ms[i] = h->stage_ms[i];
   if (q_count) *q_count = h->stage_q;
+  if (groups) *groups = h->stage_groups;
   return BRX_OK;
 }
 

@@ -273,12 +273,14 @@ class _Grid:
         check(load().brx_profile(h, 1 if enable else 0), h)
 
     def stage_times(self):
-        """(ms per stage: locate, sort, values gather, vectors gather; q count)."""
+        """(ms per stage: locate, grouping, values gather, vectors gather;
+        q count; number of gather groups)."""
         ms = (C.c_double * 4)()
         q = C.c_int64()
+        ng = C.c_int64()
         h = self._handle()
-        check(load().brx_stage_times(h, ms, 4, C.byref(q)), h)
-        return list(ms), int(q.value)
+        check(load().brx_stage_times(h, ms, 4, C.byref(q), C.byref(ng)), h)
+        return list(ms), int(q.value), int(ng.value)
 
     def launch_count(self):
         return int(load().brx_launch_count(self._handle()))

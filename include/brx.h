@@ -203,9 +203,10 @@ int64_t brx_launch_count(const brx_handle* h);
  * disable (0); either call clears the accumulated times. */
 brx_status brx_profile(brx_handle* h, int32_t enable);
 
-/* Milliseconds spent, since brx_profile, in the stages locate, node sort,
- * values gather and vectors gather (ms[0..3]), and the q count they covered. */
-brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count);
+/* Milliseconds spent, since brx_profile, in the stages locate, grouping,
+ * values gather and vectors gather (ms[0..3]), the q count they covered and
+ * the number of gather work groups. */
+brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count, int64_t* groups);
 
 int32_t brx_abi_version(void);
 
