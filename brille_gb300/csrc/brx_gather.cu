@@ -154,7 +154,7 @@ __device__ __forceinline__ void cpY(St* dst, const St* src) {
 }
 
 struct GroupLayout {
-  size_t q, rot, ident, w, R, ph, e, Y, total;
+  size_t q, rot, ident, w, R, ph, M, de, e, Y, total;
 };
 
 template <typename Acc, typename St, bool CPLX>
@@ -168,10 +168,12 @@ __host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int n
   };
   L.q = take(sizeof(long long) * QM);
   L.rot = take(sizeof(int) * 2 * QM);
-  L.ident = take(sizeof(int) * QM);
+  L.ident = take(sizeof(int) * 2 * QM);
   L.w = take(sizeof(Acc) * 8 * QM);
   L.R = take(sizeof(Acc) * 18 * QM);
   L.ph = take(sizeof(Acc) * 2 * (size_t)na * QM);
+  L.M = take(sizeof(Acc) * 12 * QM);
+  L.de = take(sizeof(int) * (size_t)(na > 0 ? na : 1) * QM);
   L.e = take(sizeof(Acc) * 2 * 8 * (size_t)MB);
   L.Y = take(sizeof(St) * 2 * 8 * (size_t)MB * row_stride<St, CPLX>(s));
   L.total = (o + 15) & ~size_t(15);
@@ -385,6 +387,104 @@ __device__ __forceinline__ void issue_rows(const GatherParams& p, const GroupInf
   }
 }
 
+// FP32 output items of one block of modes.  Work unit = (mode, element
+// group) × a share of the group's q: the unit's rows of every slot, with
+// their antiphase, stay in registers while it loops over its q.  NS is the
+// number of vertex slots (8 for a cube node, 4 for a tetrahedron).
+template <int NS, typename Acc, typename St, bool CPLX, typename Out>
+__device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* s_Y, int rs, const Acc* s_e,
+                                               const Acc* s_w, const Acc* s_R, const int* s_id, const Acc* s_M,
+                                               const int* s_rotf, const Acc* s_ph, const int* s_de,
+                                               const long long* s_q, int count, int pivot, int MB, int b0, int mb,
+                                               int G, int na, Out* out) {
+  constexpr int comps = CPLX ? 2 : 1;
+  const int B = p.B, s = p.s;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int nitem = mb * G;
+  int qsplit = (2 * nth + nitem - 1) / nitem;
+  if (qsplit > count) qsplit = count;
+  if (qsplit < 1) qsplit = 1;
+  const bool gamma = p.rot_mode == ROT_GAMMA;
+  for (int it = tid; it < nitem * qsplit; it += nth) {
+    const int item = it % nitem, qs = it / nitem;
+    const int b = item / G, gi = item % G;
+    const int bb = b0 + b;
+    int e0, ne;
+    if (gi < p.nsc) { e0 = gi; ne = 1; }
+    else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
+    else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
+    if (ne == 9) {
+      for (int j = qs; j < count; j += qsplit)
+        matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w + 8 * j, s_R + 18 * j, s_id[j], false, pivot, NS, MB,
+                                        b, e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
+      continue;
+    }
+    Acc yr[NS][3], yi[NS][3];
+#pragma unroll
+    for (int x = 0; x < NS; ++x) {
+      const bool usex = x >= pivot;
+      const Acc er = usex ? s_e[2 * (x * MB + b)] : (Acc)0;
+      const Acc ei = usex ? s_e[2 * (x * MB + b) + 1] : (Acc)0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        Acc dr = 0, di = 0;
+        if (usex && k < ne) ldY<Acc, St, CPLX>(s_Y + (size_t)(x * MB + b) * rs + (e0 + k) * comps, dr, di);
+        yr[x][k] = er * dr - ei * di;
+        yi[x][k] = er * di + ei * dr;
+      }
+    }
+    const int k_atom = gi - p.nsc;
+    const size_t row_off = (size_t)bb * s * comps;
+    for (int j = qs; j < count; j += qsplit) {
+      Acc wv[8];
+      {
+        const float4 w0 = *reinterpret_cast<const float4*>(s_w + 8 * j);
+        wv[0] = w0.x; wv[1] = w0.y; wv[2] = w0.z; wv[3] = w0.w;
+        if (NS == 8) {
+          const float4 w1 = *reinterpret_cast<const float4*>(s_w + 8 * j + 4);
+          wv[4] = w1.x; wv[5] = w1.y; wv[6] = w1.z; wv[7] = w1.w;
+        }
+      }
+      Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+      for (int x = 0; x < NS; ++x) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          vr[k] += wv[x] * yr[x][k];
+          if (CPLX) vi[k] += wv[x] * yi[x][k];
+        }
+      }
+      Out* dst = out + (size_t)s_q[j] * B * s * comps + row_off;
+      int de = e0;
+      if (ne == 3 && s_rotf[j]) {
+        const float4 m0 = *reinterpret_cast<const float4*>(s_M + 12 * j);
+        const float4 m1 = *reinterpret_cast<const float4*>(s_M + 12 * j + 4);
+        const float m8 = s_M[12 * j + 8];
+        const Acc M[9] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w, m8};
+        Acc tr[3], ti[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          tr[a] = M[3 * a] * vr[0] + M[3 * a + 1] * vr[1] + M[3 * a + 2] * vr[2];
+          ti[a] = M[3 * a] * vi[0] + M[3 * a + 1] * vi[1] + M[3 * a + 2] * vi[2];
+        }
+        if (gamma) {
+          de = s_de[j * na + k_atom];
+          const float2 ph = *reinterpret_cast<const float2*>(s_ph + 2 * (j * na + k_atom));
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            vr[a] = ph.x * tr[a] - ph.y * ti[a];
+            vi[a] = ph.x * ti[a] + ph.y * tr[a];
+          }
+        } else {
+#pragma unroll
+          for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
+        }
+      }
+      store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
+    }
+  }
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
 __global__ void __launch_bounds__(kGatherThreads)
 group_gather_kernel(GatherParams p) {
@@ -406,6 +506,9 @@ group_gather_kernel(GatherParams p) {
   Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
   Acc* s_R = reinterpret_cast<Acc*>(sm + L.R);
   Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
+  Acc* s_M = reinterpret_cast<Acc*>(sm + L.M);
+  int* s_de = reinterpret_cast<int*>(sm + L.de);
+  int* s_rotf = s_id + QM;  // second half of the ident block
   Acc* s_e = reinterpret_cast<Acc*>(sm + L.e);
   St* const s_Y0 = reinterpret_cast<St*>(sm + L.Y);
   const size_t ybuf = (size_t)8 * MB * rs;
@@ -461,12 +564,31 @@ group_gather_kernel(GatherParams p) {
       s_rot[2 * j] = r0;
       s_rot[2 * j + 1] = r1;
       s_id[j] = ident;
+      // the matrix applied to 3-vectors (FP32 path), and whether to apply it
+      if constexpr (kRegTile) {
+        const Acc* R = s_R + 18 * j;
+        const Acc* Ri = R + 9;
+        Acc scale = 1;
+        if (p.rot_mode == ROT_AXIAL)
+          scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                  R[2] * (R[3] * R[7] - R[4] * R[6]);
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) {
+            Acc m;
+            if (p.rot_mode == ROT_RECIP) m = R[3 * c + a];
+            else if (gamma || p.rot_mode == ROT_AXIAL) m = scale * Ri[3 * a + c];
+            else m = R[3 * a + c];
+            s_M[12 * j + 3 * a + c] = m;
+          }
+        s_rotf[j] = (p.rot_mode != ROT_NONE && (gamma || !ident)) ? 1 : 0;
+      }
     }
     __syncthreads();
     if (gamma) {
       for (int it = tid; it < count * na; it += nth) {
         const int j = it / na, k = it % na;
         const long long qi = s_q[j];
+        s_de[it] = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + s_rot[2 * j + 1]);
         const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + s_rot[2 * j + 1]);
         double dq = 0.0;
         dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi], d[0]));
@@ -531,61 +653,13 @@ group_gather_kernel(GatherParams p) {
       }
       __syncthreads();
       const int nitem = mb * G;
-      if (kRegTile) {
-        int qsplit = (2 * nth + nitem - 1) / nitem;
-        if (qsplit > count) qsplit = count;
-        if (qsplit < 1) qsplit = 1;
-        for (int it = tid; it < nitem * qsplit; it += nth) {
-          const int item = it % nitem, qs = it / nitem;
-          const int b = item / G, gi = item % G;
-          const int bb = b0 + b;
-          int e0, ne;
-          if (gi < p.nsc) { e0 = gi; ne = 1; }
-          else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
-          else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
-          if (ne == 9) {
-            for (int j = qs; j < count; j += qsplit)
-              matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w + 8 * j, s_R + 18 * j, s_id[j], gamma, pivot,
-                                              nslot, MB, b, e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
-            continue;
-          }
-          // this (mode, element group)'s rows of every slot, antiphase applied
-          Acc yr[8][3], yi[8][3];
-#pragma unroll
-          for (int x = 0; x < 8; ++x) {
-            const bool usex = x >= pivot && x < nslot;
-            const Acc er = usex ? s_e[2 * (x * MB + b)] : (Acc)0;
-            const Acc ei = usex ? s_e[2 * (x * MB + b) + 1] : (Acc)0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              Acc dr = 0, di = 0;
-              if (usex && k < ne) ldY<Acc, St, CPLX>(s_Y + (size_t)(x * MB + b) * rs + (e0 + k) * comps, dr, di);
-              yr[x][k] = er * dr - ei * di;
-              yi[x][k] = er * di + ei * dr;
-            }
-          }
-          for (int j = qs; j < count; j += qsplit) {
-            const Acc* wj = s_w + 8 * j;
-            Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
-#pragma unroll
-            for (int x = 0; x < 8; ++x) {
-              const Acc wx = wj[x];
-#pragma unroll
-              for (int k = 0; k < 3; ++k) {
-                vr[k] += wx * yr[x][k];
-                if (CPLX) vi[k] += wx * yi[x][k];
-              }
-            }
-            Out* dst = out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps;
-            int de = e0;
-            if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
-              const int k = gi - p.nsc;
-              de = rotate_vector<Acc, CPLX>(p, gamma, s_R + 18 * j, s_ph + 2 * (j * na + k), k, s_rot[2 * j + 1],
-                                            e0, vr, vi);
-            }
-            store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
-          }
-        }
+      if constexpr (kRegTile) {
+        if (nslot == 4)
+          reg_tile_items<4, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q,
+                                                count, pivot, MB, b0, mb, G, na, out);
+        else
+          reg_tile_items<8, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q,
+                                                count, pivot, MB, b0, mb, G, na, out);
       } else {
         const int items = count * nitem;
         for (int it = tid; it < items; it += nth) {
