@@ -217,6 +217,7 @@ def main():
     dev = torch.device("cuda", local)
 
     from brille_gb300 import BZTrellisQdc
+    from brille_gb300.sharding import shard_range
 
     wl = build_workload(args.workload)
     B, na = wl["w"].shape[1], wl["v"].shape[2]
@@ -231,6 +232,9 @@ def main():
         log(f"[setup] {n} q per step do not fit in HBM; using {fit}")
         n = fit
     qr = wl["q_range"]
+    # weak scaling: a global batch of world·n q, each rank its own slice
+    q0, q1 = shard_range(world * n, rank, world)
+    n = q1 - q0
     gen = torch.Generator(device=dev)
     gen.manual_seed(1000 + rank)
     nbuf = 2
