@@ -47,6 +47,9 @@ def load(build_if_missing=True):
         f = getattr(lib, name)
         f.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
         f.restype = C.c_int
+    lib.brx_ir_interpolate_at_noalloc.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32,
+                                                  C.c_void_p]
+    lib.brx_ir_interpolate_at_noalloc.restype = C.c_int
     lib.brx_locate.argtypes = [h, C.c_void_p, C.c_int64, C.c_int32, C.c_uint32, C.POINTER(LocateOut), C.c_void_p]
     lib.brx_locate.restype = C.c_int
     lib.brx_sync.argtypes = [h, C.c_void_p]

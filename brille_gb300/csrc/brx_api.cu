@@ -25,96 +25,11 @@
 
 #include "../../include/brx.h"
 #include "brx_kernels.h"
+#include "brx_handle.h"
 
-using namespace brx;
+using namespace brx_detail;
 
-namespace {
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  cudaError_t ensure(size_t n) {
-    if (n <= bytes) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e == cudaSuccess) bytes = n;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
-};
-
-struct Interp {
-  bool present = false;
-  bool cplx = false;
-  int store = ST_F64;  // StoreKind of the device copy
-  int B = 0, s = 0;
-  int el[3] = {0, 0, 0};
-  int rotates_like = 0, length_unit = 0;
-  DevBuf data;
-};
-
-struct Scratch {
-  DevBuf rec;     // records
-  DevBuf sortbuf; // counts, offsets, cursors, block sums
-  DevBuf groupbuf;  // work descriptors + their count + queue cursors
-  DevBuf qbuf;    // staged Q
-  DevBuf vbuf, cbuf;  // staged outputs (host I/O)
-  Records r{};
-  int32_t* order = nullptr;
-  int32_t* sort_scratch = nullptr;
-  GroupDesc* groups = nullptr;
-  int32_t* n_groups = nullptr;
-  int32_t* counters = nullptr;  // one work-queue cursor per interpolator
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
-};
-
-}  // namespace
-
-struct brx_handle {
-  int device = 0;
-  int num_sms = 0;
-  size_t smem_optin = 0;
-  DevGeom g{};
-  std::vector<DevBuf> tables;
-  brx_geometry host_geom{};
-  std::vector<double> rot_cart;
-  Interp vals, vecs;
-  int storage = BRX_STORE_F64;
-  bool filled = false;
-  // permutation table
-  DevBuf perm_keys, perm_ids, perms;
-  long long n_keys = 0;
-  int n_perms = 0;
-  Scratch sc[2];
-  long long scratch_q = 0;
-  ErrorWord* err = nullptr;       // device
-  ErrorWord* err_host = nullptr;  // pinned
-  std::string message = "no error";
-  long long launches = 0;
-  // stage timing (brx_profile): events per chunk, accumulated after sync
-  bool profile = false;
-  std::vector<cudaEvent_t> ev_pool;
-  size_t ev_used = 0;
-  double stage_ms[5] = {0, 0, 0, 0, 0};
-  long long stage_q = 0;
-  long long stage_groups = 0;
-  std::vector<int32_t*> group_counts;  // pinned, one per profiled chunk
-  size_t group_used = 0;
-  bool async_pending = false;
-  cudaStream_t async_stream = nullptr;
-  int async_ir = 0;
-  const double* async_Q = nullptr;
-  long long async_n = 0;
-};
-
-namespace {
+namespace brx_detail {
 
 brx_status fail(brx_handle* h, brx_status st, const std::string& msg) {
   if (h) h->message = msg;
@@ -127,11 +42,6 @@ brx_status cuda_fail(brx_handle* h, cudaError_t e, const char* where) {
   return fail(h, BRX_ERR_CUDA, m);
 }
 
-#define BRX_CUDA(h, call)                               \
-  do {                                                  \
-    cudaError_t e_ = (call);                            \
-    if (e_ != cudaSuccess) return cuda_fail(h, e_, #call); \
-  } while (0)
 
 template <typename T>
 brx_status upload(brx_handle* h, const T* src, size_t count, const T** dst) {
@@ -519,7 +429,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   return collect_errors(h, ir, Q, n, q_host);
 }
 
-}  // namespace
+}  // namespace brx_detail
 
 extern "C" {
 

@@ -797,6 +797,54 @@ static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
   group_gather_kernel<Acc, St, CPLX, Out><<<(unsigned)grid, kGatherThreads, smem, s>>>(p);
 }
 
+template <typename Acc, typename St, bool CPLX, typename Out>
+static cudaError_t preload_t() {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, group_gather_kernel<Acc, St, CPLX, Out>);
+  if (e != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&a, scalar_gather_kernel<Acc, St, CPLX, Out>);
+}
+
+template <typename Acc, typename St>
+static cudaError_t preload_store() {
+  cudaError_t e;
+  if ((e = preload_t<Acc, St, true, float>()) != cudaSuccess) return e;
+  if ((e = preload_t<Acc, St, true, double>()) != cudaSuccess) return e;
+  if ((e = preload_t<Acc, St, false, float>()) != cudaSuccess) return e;
+  return preload_t<Acc, St, false, double>();
+}
+
+__global__ void key_hist_kernel(const int32_t* key, long long n, int32_t* counts);
+__global__ void scan_reduce_kernel(const int32_t* in, long long m, int32_t* block_sums);
+__global__ void scan_blocks_kernel(int32_t* block_sums, int nb);
+__global__ void scan_apply_kernel(const int32_t* in, long long m, const int32_t* block_sums, int32_t* out,
+                                  int32_t* out2);
+__global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cursor, int32_t* order);
+__global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
+                                   GroupDesc* groups, int32_t* n_groups);
+
+cudaError_t preload_grouping_kernels() {
+  cudaFuncAttributes a;
+  cudaError_t e;
+  if ((e = cudaFuncGetAttributes(&a, key_hist_kernel)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, scan_reduce_kernel)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, scan_blocks_kernel)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, scan_apply_kernel)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, key_scatter_kernel)) != cudaSuccess) return e;
+  return cudaFuncGetAttributes(&a, make_groups_kernel);
+}
+
+cudaError_t preload_locate_kernel();
+
+cudaError_t preload_query_kernels() {
+  cudaError_t e;
+  if ((e = preload_store<double, double>()) != cudaSuccess) return e;
+  if ((e = preload_store<float, float>()) != cudaSuccess) return e;
+  if ((e = preload_store<float, __nv_bfloat16>()) != cudaSuccess) return e;
+  if ((e = preload_grouping_kernels()) != cudaSuccess) return e;
+  return preload_locate_kernel();
+}
+
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms, size_t,
                   cudaStream_t s) {
   if (p.n <= 0) return 0;

@@ -80,6 +80,10 @@ size_t group_scratch_ints(long long n_keys);
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms,
                   size_t smem_budget, cudaStream_t s);
 size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB);
+
+// Load every query kernel of this library on the current device (module
+// loading is otherwise deferred to the first launch).
+cudaError_t preload_query_kernels();
 int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget);
 
 }  // namespace brx

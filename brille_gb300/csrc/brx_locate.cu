@@ -467,6 +467,11 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
   }
 }
 
+cudaError_t preload_locate_kernel() {
+  cudaFuncAttributes a;
+  return cudaFuncGetAttributes(&a, locate_kernel);
+}
+
 size_t locate_smem_bytes(const DevGeom& g) {
   return sizeof(float) * (5 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge * (g.n_ops + 1)) + 16 +
          sizeof(double) * (13 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge) +

@@ -190,6 +190,22 @@ brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n,
 brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir,
                       uint32_t flags, const brx_locate_out* out, void* stream);
 
+/* ir_interpolate_at for callers that may not allocate device memory while
+ * they run: work queued during CUDA stream capture (cudaMalloc cannot be
+ * captured), serving loops that cannot take cudaMalloc's device-wide
+ * synchronisation, and host frameworks whose own pool owns the device memory.
+ * No counterpart in the reference.  All per-q scratch lives in one fixed
+ * __device__ array of this library (about 12 MB on every device that loads
+ * it, kept until exit), so a call allocates nothing.  Limits: Q and outputs
+ * must be device pointers; n ≤ BRX_NOALLOC_MAX_Q (larger n is rejected with
+ * BRX_ERR_INVALID_ARGUMENT).  The first call on a device looks up the array
+ * and loads the kernels; make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised. */
+#define BRX_NOALLOC_MAX_Q 65536
+brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double* Q, int64_t n,
+                                         void* values_out, void* vectors_out,
+                                         uint32_t flags, void* stream);
+
 /* Wait for work queued with BRX_FLAG_ASYNC and report its status. */
 brx_status brx_sync(brx_handle* h, void* stream);
 
