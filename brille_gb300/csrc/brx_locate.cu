@@ -166,16 +166,23 @@ __device__ __forceinline__ bool wedge_candidate(const DevGeom& g, const float* m
 __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32_t rot[2]) {
   double x[3], qj[3];
   hkl_to_xyz(x, g.outer_B, q);
-  if (g.screen && g.n_wedge > 0) {
-    // exact tests for the screened-in operations only, in the reference's order
+  if (g.screen && g.n_wedge > 0 && g.n_ops <= 64) {
+    // FP32 screen of every operation first (the same work in every lane),
+    // then exact tests of the survivors in the reference's order; each lane
+    // walks its own candidate mask, so the exact tests run converged
     const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
     const float tol = screen_margin(fabsf(x0) + fabsf(x1) + fabsf(x2), 0.f) + g.wedge_band32;
-    if (wedge_candidate(g, z.wm + 3 * g.n_wedge * g.n_ops, x0, x1, x2, tol) && inside_wedge(g, z, x)) {
+    const bool id_cand = wedge_candidate(g, z.wm + 3 * g.n_wedge * g.n_ops, x0, x1, x2, tol);
+    unsigned long long mask = 0ull;
+    for (int j = 0; j < g.n_ops; ++j)
+      if (wedge_candidate(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, tol)) mask |= 1ull << j;
+    if (id_cand && inside_wedge(g, z, x)) {
       rot[0] = rot[1] = g.identity;
       return 0;
     }
-    for (int j = 0; j < g.n_ops; ++j) {
-      if (!wedge_candidate(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, tol)) continue;
+    while (mask) {
+      const int j = __ffsll((long long)mask) - 1;
+      mask &= mask - 1;
       const int32_t* W = z.ops + 9 * j;
       int32_t Wt[9] = {W[0], W[3], W[6], W[1], W[4], W[7], W[2], W[5], W[8]};
       matvec_i(qj, Wt, q);
