@@ -134,3 +134,42 @@ def grid_for(lat, max_volume_fraction, masses=None, time_reversal=False):
 
 def bvk_for(lat, masses):
     return BvKModel(lat, masses, cutoff=6.0, decay=1.5)
+
+
+def near_boundary_q(bz, tr, n, delta=1e-6, seed=0):
+    """q within `delta` r.l.u. of trellis faces (tetrahedron faces and knot
+    planes) and of high-symmetry lines (edges of the irreducible polyhedron),
+    carried to random symmetry images and zones so that every stage meets
+    them."""
+    from .trellis import _poly_edges
+
+    rng = np.random.default_rng(seed)
+    lat = bz.lattice
+    Binv = np.linalg.inv(lat.B)
+    parts = []
+    k = n // 3
+    # tetrahedron faces
+    t = tr.tet_vertices[rng.integers(0, len(tr.tet_vertices), k)]
+    bc = rng.dirichlet([1, 1, 1], size=k)
+    parts.append(np.einsum("nk,nkd->nd", bc, tr.vertices[t[:, :3]]))
+    # knot planes inside cube nodes
+    cv = tr.cube_vertices[rng.integers(0, max(len(tr.cube_vertices), 1), k)] if len(tr.cube_vertices) else None
+    if cv is not None:
+        lo, hi = tr.vertices[cv[:, 0]], tr.vertices[cv[:, 7]]
+        x = lo + rng.uniform(size=(k, 3)) * (hi - lo)
+        axis = rng.integers(0, 3, k)
+        x[np.arange(k), axis] = np.where(rng.uniform(size=(k, 1)) < 0.5, lo, hi)[np.arange(k), axis]
+        parts.append(x)
+    # edges of the irreducible polyhedron (high-symmetry lines)
+    edges = _poly_edges(bz.ir_vertices, bz.ir_halfspaces, 1e-9 * np.abs(bz.ir_vertices).max())
+    m = n - sum(len(p) for p in parts)
+    e = edges[rng.integers(0, len(edges), m)]
+    s = rng.uniform(size=(m, 1))
+    parts.append(bz.ir_vertices[e[:, 0]] * (1 - s) + bz.ir_vertices[e[:, 1]] * s)
+    q = np.concatenate(parts) @ Binv
+    q += rng.uniform(-delta, delta, size=q.shape)
+    W = bz.pointgroup.W[rng.integers(0, bz.pointgroup.size, len(q))]
+    q = np.einsum("nji,nj->ni", W, q)
+    P = lat.inv_P().T  # conventional components of primitive translations
+    G = rng.integers(-2, 3, size=(len(q), 3)) @ P.T
+    return q + G
