@@ -209,8 +209,11 @@ def run_precision(args):
         g.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage=st)
         grids[st] = g
     dev = torch.device("cuda")
-    chunk = 1 << 20
-    acc = {st: dict(vmax=0.0, vsq=0.0, omax=0.0, osum=0.0, cnt=0) for st in ("f32", "bf16")}
+    # chunks of at most ~4 GB of complex128 eigenvectors per storage
+    chunk = int(max(4096, min(1 << 20, (4 << 30) // (B * na * 3 * 16))))
+    acc = {st: dict(vmax=0.0, vsq=0.0, omax=0.0, osum=0.0, cnt=0, gmax=0.0, gsum=0.0, nbad=0)
+           for st in ("f32", "bf16")}
+    degen_tol = 1e-3  # meV: modes closer than this form one degenerate group
     for a in range(0, n, chunk):
         b_ = min(n, a + chunk)
         m = b_ - a
@@ -233,10 +236,34 @@ def run_precision(args):
             acc[st]["omax"] = max(acc[st]["omax"], float(e.max()))
             acc[st]["osum"] += float(e.sum())
             acc[st]["cnt"] += e.numel()
+            # degenerate-subspace overlap: 1 − sqrt(Σ_{j in G(b)} |<v̂_ref_b, v̂_j>|²)
+            # over the group G(b) of modes within degen_tol of each other (FP64 eigenvalues)
+            gid = torch.cat([torch.zeros((m, 1), dtype=torch.int64, device=dev),
+                             torch.cumsum((v64[:, 1:] - v64[:, :-1]).abs() >= degen_tol, dim=1)], dim=1)
+            r = c64 / torch.linalg.vector_norm(c64, dim=(2, 3), keepdim=True).clamp_min(1e-300)
+            u = c / torch.linalg.vector_norm(c, dim=(2, 3), keepdim=True).clamp_min(1e-300)
+            tot = torch.zeros((m, B), dtype=torch.float64, device=dev)
+            # groups are runs of consecutive modes: stop at the first distance
+            # with no pair inside one group
+            for d in range(B):
+                same = gid[:, :B - d] == gid[:, d:]
+                if not bool(same.any()):
+                    break
+                for a0, b0 in ((0, d), (d, 0)) if d else ((0, 0),):
+                    o = (torch.conj(r[:, a0:a0 + B - d]) * u[:, b0:b0 + B - d]).sum(dim=(2, 3)).abs() ** 2
+                    tot[:, a0:a0 + B - d] += torch.where(same, o, torch.zeros_like(o))
+            ge = 1 - torch.sqrt(tot)
+            acc[st]["gmax"] = max(acc[st]["gmax"], float(ge.max()))
+            acc[st]["gsum"] += float(ge.sum())
+            acc[st]["nbad"] += int((ge > 1e-3).sum())
     res = {}
     for st, a_ in acc.items():
         res[st] = dict(eig_max_abs_meV=a_["vmax"], eig_rms_meV=(a_["vsq"] / (n * B)) ** 0.5,
-                       overlap_loss_max=a_["omax"], overlap_loss_mean=a_["osum"] / max(a_["cnt"], 1))
+                       overlap_loss_max=a_["omax"], overlap_loss_mean=a_["osum"] / max(a_["cnt"], 1),
+                       subspace_overlap_loss_max=a_["gmax"],
+                       subspace_overlap_loss_mean=a_["gsum"] / max(a_["cnt"], 1),
+                       subspace_overlap_loss_above_0p001_fraction=a_["nbad"] / max(a_["cnt"], 1),
+                       degenerate_group_tol_meV=degen_tol)
     # the FP64 path against the exact model (interpolation error of the trellis itself)
     ns = 200_000
     Qs = Q[rng.integers(0, n, ns)]
@@ -254,6 +281,120 @@ def run_precision(args):
     print(json.dumps(out), flush=True)
 
 
+LEARNED_COARSE = (("bz/625", 1 / 625), ("bz/200", 1 / 200))
+
+
+def run_learned(args):
+    """Learned residual on coarse trellises of the 2-atom FCC crystal
+    (a = 4.96 Å, 28 amu, BZ/5000 for the fine trellis) against the plain
+    fine trellis: error against the exact BvK model on held-out uniform q in
+    [-1,1]³, and eigenvalue throughput of each path on device-resident q."""
+    import torch
+
+    from brille_gb300 import workloads as W
+    from brille_gb300.bz import BrillouinZone
+    from brille_gb300.grid import BZTrellisQdd
+    from brille_gb300.learned import ResidualModel
+    from brille_gb300.trellis import TrellisBuild
+
+    lat, masses = W.diamond_primitive()
+    bz = BrillouinZone(lat)
+    model = W.bvk_for(lat, masses)
+    B = model.n_modes
+    procs = min(16, os.cpu_count() or 1)
+    Binv = np.linalg.inv(lat.B)
+    dev = torch.device("cuda")
+
+    def grid_at(frac):
+        tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac)
+        g = BZTrellisQdd(bz, trellis=tr)
+        g.fill(model.frequencies(tr.vertices @ Binv)[:, :, None], [1, 0, 0, 0, 3], storage="f32")
+        return g
+
+    n_train = args.train_q or 1_000_000
+    n_eval = args.q_per_step or 10_000_000
+    t = time.time()
+    Qt = np.random.default_rng(11).uniform(-1, 1, (n_train, 3))
+    wt = model.frequencies(Qt, processes=procs)
+    Qe = np.random.default_rng(12).uniform(-1, 1, (n_eval, 3))
+    we = model.frequencies(Qe, processes=procs)
+    log(f"[learned] exact BvK for {n_train} + {n_eval} q in {time.time() - t:.1f}s ({procs} processes)")
+    Qd = torch.from_numpy(Qe).to(dev)
+    Wd = torch.from_numpy(we).to(dev)
+    out = torch.empty((n_eval, B), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+
+    def errors(g):
+        g.query_into(Qd, n_eval, out, None, out_f32=True, stream=sp)
+        torch.cuda.synchronize()
+        e = (out.double() - Wd).abs()
+        eh = e.cpu().numpy().ravel()
+        return dict(max_meV=float(eh.max()), rms_meV=float(np.sqrt(np.mean(eh ** 2))),
+                    p99_meV=float(np.quantile(eh, 0.99)), p9999_meV=float(np.quantile(eh, 0.9999)))
+
+    def throughput(g):
+        for _ in range(args.warmup):
+            g.query_into(Qd, n_eval, out, None, out_f32=True, async_=True, stream=sp)
+            g.sync(sp)
+        torch.cuda.synchronize()
+        g.profile(True)
+        l0 = g.launch_count()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            g.query_into(Qd, n_eval, out, None, out_f32=True, async_=True, stream=sp)
+        ev1.record(stream)
+        g.sync(sp)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / args.steps
+        st_ms, st_q, _ = g.stage_times()
+        g.profile(False)
+        return dict(q_per_s=n_eval / (ms / 1e3), ms_per_step=ms, gpu_launches=int(g.launch_count() - l0),
+                    stage_ms_per_step=dict(zip(["locate", "grouping", "values", "vectors"],
+                                               [round(x / args.steps, 3) for x in st_ms])))
+
+    fine = grid_at(1 / 5000)
+    res = dict(fine=dict(trellis="bz/5000", vertices=int(len(fine.trellis.vertices)), plain=errors(fine),
+                         speed=throughput(fine)))
+    peaks = measured_peaks()
+    for name, frac in LEARNED_COARSE:
+        g = grid_at(frac)
+        r = dict(vertices=int(len(g.trellis.vertices)), plain=errors(g), plain_speed=throughput(g))
+        m = ResidualModel(B, seed=0)
+        torch.cuda.synchronize()
+        t = time.time()
+        hist = m.train_on(g, Qt, wt, epochs=args.epochs, batch=4096, lr=2e-3, log=log)
+        torch.cuda.synchronize()
+        r["train"] = dict(samples=n_train, epochs=args.epochs, batch=4096, seconds=round(time.time() - t, 2),
+                          loss_first=hist[0], loss_last=hist[-1], params=m.n_params,
+                          res_scale_meV=m.res_scale, clip_meV=m.clip)
+        m.attach(g)
+        r["learned"] = errors(g)
+        r["learned_speed"] = sp_ = throughput(g)
+        # the residual kernel runs inside the values stage: its share is the
+        # difference to the plain coarse path
+        mlp_ms = sp_["stage_ms_per_step"]["values"] - r["plain_speed"]["stage_ms_per_step"]["values"]
+        flops_q = 2 * (m.d_in * 128 + 2 * 128 * 128 + 128 * m.n_out)
+        if mlp_ms > 0:
+            ach = flops_q * n_eval / (mlp_ms / 1e3) / 1e12
+            peak = float(peaks["bf16_tflops"]) if peaks else 1900.0
+            r["mlp_roofline"] = dict(bound="tensor", achieved=round(ach, 2), peak=peak, unit="TFLOP/s",
+                                     frac=round(ach / peak, 4), flops_per_q=flops_q, ms_per_step=round(mlp_ms, 3),
+                                     peak_source="measured" if peaks else "fallback")
+        r["speedup_vs_fine"] = sp_["q_per_s"] / res["fine"]["speed"]["q_per_s"]
+        res[name] = r
+        log(f"[learned] {name}: plain max {r['plain']['max_meV']:.3g} rms {r['plain']['rms_meV']:.3g}; "
+            f"learned max {r['learned']['max_meV']:.3g} rms {r['learned']['rms_meV']:.3g} meV; "
+            f"{sp_['q_per_s']:.3g} q/s vs fine {res['fine']['speed']['q_per_s']:.3g}")
+    out_line = dict(mode="learned", crystal="FCC Fd-3m a=4.96 A, 2-atom primitive basis, 28 amu, 6 modes",
+                    q_eval=n_eval, q_eval_set="uniform in [-1,1]^3 r.l.u., seed 12 (held out)",
+                    train_set="uniform in [-1,1]^3 r.l.u., seed 11, folded into the wedge by the locate",
+                    exact="BvK eigenvalues (FP64 eigvalsh) at each q", outputs="f32 eigenvalues, storage f32",
+                    target="<=1e-3 meV max error", steps=args.steps, warmup=args.warmup, results=res)
+    print(json.dumps(out_line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,8 +407,11 @@ def main():
     ap.add_argument("--out-f64", action="store_true", help="float64/complex128 outputs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "precision"],
-                    help="precision: FP32 and BF16 storage against the FP64 path")
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned"],
+                    help="precision: FP32 and BF16 storage against the FP64 path; learned: the learned residual "
+                         "on coarse trellises against the plain fine trellis")
+    ap.add_argument("--train-q", type=int, default=0, help="learned mode: training samples (default 1e6)")
+    ap.add_argument("--epochs", type=int, default=30, help="learned mode: training epochs")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -279,6 +423,8 @@ def main():
 
     if args.mode == "precision":
         return run_precision(args)
+    if args.mode == "learned":
+        return run_learned(args)
 
     import torch
 

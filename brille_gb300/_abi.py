@@ -56,6 +56,13 @@ class LocateOut(C.Structure):
     ]
 
 
+class MlpDims(C.Structure):
+    _fields_ = [("d_in", C.c_int32), ("n_out", C.c_int32), ("n_modes", C.c_int32), ("flags", C.c_int32)]
+
+
+BRX_MLP_FP32 = 0x1
+
+
 def _ptr(a, ctype):
     return a.ctypes.data_as(C.POINTER(ctype)) if a is not None and a.size else C.POINTER(ctype)()
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import Data, Geometry, LocateOut
+from ._abi import Data, Geometry, LocateOut, MlpDims
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbrx.so")
@@ -62,6 +62,20 @@ def load(build_if_missing=True):
     lib.brx_profile.restype = C.c_int
     lib.brx_stage_times.argtypes = [h, C.POINTER(C.c_double), C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     lib.brx_stage_times.restype = C.c_int
+    md = C.POINTER(MlpDims)
+    vp = C.c_void_p
+    lib.brx_mlp_param_count.argtypes = [md]
+    lib.brx_mlp_param_count.restype = C.c_int64
+    lib.brx_mlp_workspace_floats.argtypes = [md, C.c_int64]
+    lib.brx_mlp_workspace_floats.restype = C.c_int64
+    lib.brx_mlp_features.argtypes = [h, C.POINTER(LocateOut), C.c_int64, md, C.c_float, vp, vp, vp]
+    lib.brx_mlp_features.restype = C.c_int
+    lib.brx_mlp_train_step.argtypes = [md, vp, vp, vp, vp, C.c_int32, C.c_float, vp, vp, C.c_int64, vp, vp, vp]
+    lib.brx_mlp_train_step.restype = C.c_int
+    lib.brx_mlp_forward.argtypes = [md, vp, vp, C.c_int64, vp, vp, vp]
+    lib.brx_mlp_forward.restype = C.c_int
+    lib.brx_set_residual_model.argtypes = [h, md, vp, C.c_float, C.c_float, C.c_float]
+    lib.brx_set_residual_model.restype = C.c_int
     lib.brx_abi_version.argtypes = []
     lib.brx_abi_version.restype = C.c_int32
     _lib = lib

@@ -96,22 +96,21 @@ class BvKModel:
     def modes(self, q_rlu, chunk=4096, processes=0):
         """(ħω meV (N, 3n), eigenvectors (N, 3n, n, 3)) sorted by energy.
 
-        processes > 1 spreads the eigensolves over a spawn-started pool (safe
-        in a process that has already initialised CUDA)."""
+        processes > 1 spreads the eigensolves over a spawn-started process
+        pool (safe in a process that has already initialised CUDA; the caller's
+        __main__ must be importable, i.e. a file, not standard input)."""
         q = np.atleast_2d(np.asarray(q_rlu, float))
         N, n = q.shape[0], self.n_atoms
         w = np.empty((N, 3 * n))
         v = np.empty((N, 3 * n, n, 3), complex)
         parts = [(a, min(N, a + chunk)) for a in range(0, N, chunk)]
         if processes > 1 and len(parts) > 1:
-            import multiprocessing as mp
             from multiprocessing import shared_memory
 
             shm_w = shared_memory.SharedMemory(create=True, size=w.nbytes)
             shm_v = shared_memory.SharedMemory(create=True, size=v.nbytes)
             try:
-                with mp.get_context("spawn").Pool(processes) as pool:
-                    pool.starmap(_modes_worker, [(self, q[a:b], a, N, shm_w.name, shm_v.name) for a, b in parts])
+                _run_pool(processes, _modes_worker, [(self, q[a:b], a, N, shm_w.name, shm_v.name) for a, b in parts])
                 w[:] = np.ndarray(w.shape, w.dtype, buffer=shm_w.buf)
                 v[:] = np.ndarray(v.shape, v.dtype, buffer=shm_v.buf)
             finally:
@@ -122,6 +121,56 @@ class BvKModel:
             for a, b in parts:
                 w[a:b], v[a:b] = self._modes_serial(q[a:b])
         return w, v
+
+    def frequencies(self, q_rlu, chunk=8192, processes=0):
+        """ħω in meV (N, 3n), sorted, without eigenvectors (eigvalsh)."""
+        q = np.atleast_2d(np.asarray(q_rlu, float))
+        N = q.shape[0]
+        w = np.empty((N, self.n_modes))
+        parts = [(a, min(N, a + chunk)) for a in range(0, N, chunk)]
+        if processes > 1 and len(parts) > 1:
+            from multiprocessing import shared_memory
+
+            shm = shared_memory.SharedMemory(create=True, size=w.nbytes)
+            try:
+                _run_pool(processes, _freq_worker, [(self, q[a:b], a, N, shm.name) for a, b in parts])
+                w[:] = np.ndarray(w.shape, w.dtype, buffer=shm.buf)
+            finally:
+                shm.close()
+                shm.unlink()
+        else:
+            for a, b in parts:
+                w[a:b] = self._freq_serial(q[a:b])
+        return w
+
+    def _freq_serial(self, q):
+        D = self.dynamical_matrix(q)
+        D = 0.5 * (D + np.conj(np.swapaxes(D, 1, 2)))
+        lam = np.linalg.eigvalsh(D)
+        return np.sign(lam) * np.sqrt(np.abs(lam)) * HBAR_OMEGA_MEV
+
+
+def _run_pool(processes, fn, jobs):
+    """Run fn(*job) for every job on a spawn-started process pool.  A worker
+    that cannot start (e.g. a __main__ that spawn cannot re-import) raises
+    BrokenProcessPool here instead of being restarted forever."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
+        for f in [ex.submit(fn, *j) for j in jobs]:
+            f.result()
+
+
+def _freq_worker(model, q, a, N, name):
+    from multiprocessing import shared_memory
+
+    wa = model._freq_serial(q)
+    s = shared_memory.SharedMemory(name=name)
+    try:
+        np.ndarray((N, model.n_modes), float, buffer=s.buf)[a:a + len(q)] = wa
+    finally:
+        s.close()
 
 
 def _modes_worker(model, q, a, N, name_w, name_v):

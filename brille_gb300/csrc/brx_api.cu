@@ -386,6 +386,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       p.out = vdst;
       p.MB = gather_pick_modes(p, h->vals.store, h->vals.cplx, smem_budget(h));
       h->launches += launch_gather(p, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h), cs);
+      h->launches += launch_residual(h, s, m, vdst, f32, cs);
     }
     if (ev[3]) cudaEventRecord(ev[3], cs);
     char* cdst = nullptr;
@@ -649,6 +650,8 @@ void brx_destroy(brx_handle* h) {
   h->perm_keys.release();
   h->perm_ids.release();
   h->perms.release();
+  h->mlp_w.release();
+  h->mlp_b.release();
   if (h->err) cudaFree(h->err);
   if (h->err_host) cudaFreeHost(h->err_host);
   delete h;
@@ -707,6 +710,7 @@ brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vecto
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "The values and vectors must have matching number of points and branches");
   BRX_CUDA(h, cudaSetDevice(h->device));
   h->filled = false;
+  h->mlp_on = false;  // a residual model belongs to the data it was trained on
   // bfloat16 storage applies to the eigenvectors; eigenvalues keep float32
   brx_status st = fill_one(h, values, h->vals, storage == BRX_STORE_BF16 ? BRX_STORE_F32 : storage);
   if (st) return st;

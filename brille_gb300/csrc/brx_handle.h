@@ -96,6 +96,11 @@ struct brx_handle {
   long long stage_groups = 0;
   std::vector<int32_t*> group_counts;  // pinned, one per profiled chunk
   size_t group_used = 0;
+  // learned eigenvalue residual (brx_set_residual_model)
+  bool mlp_on = false;
+  brx_mlp_dims mlp_dims{};
+  float mlp_omega_scale = 1.f, mlp_res_scale = 1.f, mlp_clip = 0.f;
+  DevBuf mlp_w, mlp_b;
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;
@@ -115,6 +120,9 @@ size_t smem_budget(brx_handle* h);
 size_t out_elem_bytes(const Interp& d, bool f32);
 brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, bool q_host);
 brx_status reset_errors(brx_handle* h, cudaStream_t s);
+// Adds the learned residual to the eigenvalues just gathered for a chunk;
+// returns the number of kernels launched (0 without a model).
+int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_out, bool out_f32, cudaStream_t cs);
 
 }  // namespace brx_detail
 

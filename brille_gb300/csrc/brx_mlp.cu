@@ -1,0 +1,681 @@
+// Learned residual correction of interpolated eigenvalues.
+//
+// A small MLP (d_in → 128 → 128 → 128 → n_out, GELU) predicts, per mode, the
+// difference between the exact eigenvalue and the trellis interpolation at
+// q.  Its input row is built on the GPU from the locate record of q:
+//
+//   col 0-2    position of q in its node cell, (x − knot_lo)/(knot_hi − knot_lo)
+//   col 3-10   weights of the (up to) 8 vertex slots, 0 for unused slots
+//   col 11     1 for a tetrahedron, 0 for a cube node
+//   col 12 …   vertex eigenvalues, slot-major: 12 + slot·B + mode
+//   then       interpolated eigenvalues, B columns
+//   then       zero padding up to d_in
+//
+// eigenvalues divided by omega_scale.  Training runs on the FP32 CUDA-core
+// kernels of this file (a tiled GEMM with optional transposes, bias + GELU,
+// GELU derivative, bias sums, Adam).  Weights, biases and activations are
+// rounded to bfloat16 wherever inference rounds them, so training sees the
+// inference arithmetic; gradients pass straight through the rounding onto
+// FP32 master weights.  Inference is one fused kernel on the tensor cores
+// (mma m16n8k16, bf16 operands, FP32 accumulate): feature rows into a
+// shared-memory tile, four dense layers, and the residual added to the
+// eigenvalues the gather wrote, 128 q per tile.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/brx.h"
+#include "brx_handle.h"
+#include "brx_kernels.h"
+
+namespace brx {
+
+constexpr int kWidth = 128;
+
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+// Offsets of the parameter blocks in the flat FP32 parameter vector:
+// W0 (128 × d_in), b0, W1 (128 × 128), b1, W2, b2, W3 (n_out × 128), b3;
+// every W row-major [out][in].
+struct MlpLayout {
+  long long W[4], b[4], total;
+  int in[4], out[4];
+};
+
+__host__ __device__ inline MlpLayout mlp_layout(int d_in, int n_out) {
+  MlpLayout L;
+  L.in[0] = d_in;   L.out[0] = kWidth;
+  L.in[1] = kWidth; L.out[1] = kWidth;
+  L.in[2] = kWidth; L.out[2] = kWidth;
+  L.in[3] = kWidth; L.out[3] = n_out;
+  long long o = 0;
+  for (int l = 0; l < 4; ++l) {
+    L.W[l] = o; o += (long long)L.out[l] * L.in[l];
+    L.b[l] = o; o += L.out[l];
+  }
+  L.total = o;
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// feature rows
+// ---------------------------------------------------------------------------
+struct FeatureArgs {
+  const double* q_ir;
+  const int32_t* node;     // n × 2
+  const int32_t* nw;
+  const int32_t* vidx;     // n × 8
+  const double* w;         // n × 8
+  const int32_t* status;
+  long long n;
+  const void* values;      // n_vertices × B, float or double
+  int values_f64;
+  int B;
+  int d_in;
+  float inv_omega;         // 1 / omega_scale
+};
+
+__device__ __forceinline__ float vertex_value(const FeatureArgs& a, long long v, int b) {
+  return a.values_f64 ? (float)static_cast<const double*>(a.values)[v * a.B + b]
+                      : static_cast<const float*>(a.values)[v * a.B + b];
+}
+
+// Writes the non-zero columns of q i's row through put(col, value) (the
+// caller zeroes the row first) and returns through base the B interpolated
+// eigenvalues in the data's own unit (NaN for a q whose locate failed).
+template <class Put>
+__device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i, Put put, float* base) {
+  if (a.status[i]) {
+    if (base)
+      for (int b = 0; b < a.B; ++b) base[b] = __int_as_float(0x7fc00000);
+    return;
+  }
+  const long long node = a.node[2 * i];
+  const long long nx = g.n_knots[0] - 1, ny = g.n_knots[1] - 1;
+  const int sub[3] = {(int)(node % nx), (int)((node / nx) % ny), (int)(node / (nx * ny))};
+  double x[3];
+  hkl_to_xyz(x, g.outer_B, a.q_ir + 3 * i);
+  for (int d = 0; d < 3; ++d) {
+    const double lo = g.knots[d][sub[d]], hi = g.knots[d][sub[d] + 1];
+    put(d, (float)((x[d] - lo) / (hi - lo)));
+  }
+  const int nw = min(a.nw[i], 8);
+  for (int k = 0; k < nw; ++k) put(3 + k, (float)a.w[8 * i + k]);
+  put(11, a.node[2 * i + 1] >= 0 ? 1.f : 0.f);
+  for (int b = 0; b < a.B; ++b) {
+    double s = 0.0;
+    for (int k = 0; k < nw; ++k) {
+      const float ev = vertex_value(a, a.vidx[8 * i + k], b);
+      put(12 + k * a.B + b, ev * a.inv_omega);
+      s = dadd(s, dmul(a.w[8 * i + k], (double)ev));
+    }
+    if (base) base[b] = (float)s;
+    put(12 + 8 * a.B + b, (float)s * a.inv_omega);
+  }
+}
+
+__global__ void mlp_features_kernel(DevGeom g, FeatureArgs a, float* X, float* base) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x) {
+    float* row = X + i * a.d_in;
+    for (int k = 0; k < a.d_in; ++k) row[k] = 0.f;
+    feature_row(g, a, i, [row](int k, float v) { row[k] = v; }, base + i * a.B);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// training kernels (FP32 CUDA cores)
+// ---------------------------------------------------------------------------
+// C[M×N] = Σ_k A(m,k)·B(k,n);
+// A(m,k) = A[m·lda+k], or A[k·lda+m] when transA;
+// B(k,n) = B[k·ldb+n], or B[n·ldb+k] when transB.
+// Operands are rounded to bfloat16 on load when roundA / roundB.
+constexpr int kTile = 64, kTK = 16;
+
+__global__ void __launch_bounds__(256)
+gemm_f32_kernel(int M, int N, int K, const float* A, int lda, int transA, int roundA, const float* Bm, int ldb,
+                int transB, int roundB, float* C, int ldc) {
+  __shared__ float As[kTK][kTile + 1];
+  __shared__ float Bs[kTK][kTile + 1];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
+  float acc[4][4] = {};
+  for (int k0 = 0; k0 < K; k0 += kTK) {
+    for (int t = threadIdx.x; t < kTK * kTile; t += 256) {
+      // consecutive threads walk the operand's contiguous index
+      int kk, mm;
+      if (transA) { kk = t / kTile; mm = t % kTile; } else { kk = t % kTK; mm = t / kTK; }
+      const int m = m0 + mm, k = k0 + kk;
+      float v = 0.f;
+      if (m < M && k < K) v = transA ? A[(long long)k * lda + m] : A[(long long)m * lda + k];
+      As[kk][mm] = roundA ? bf16_round(v) : v;
+      int kb, nn;
+      if (transB) { kb = t % kTK; nn = t / kTK; } else { kb = t / kTile; nn = t % kTile; }
+      const int n = n0 + nn, kq = k0 + kb;
+      float u = 0.f;
+      if (n < N && kq < K) u = transB ? Bm[(long long)n * ldb + kq] : Bm[(long long)kq * ldb + n];
+      Bs[kb][nn] = roundB ? bf16_round(u) : u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTK; ++kk) {
+      float a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) { a[i] = As[kk][ty * 4 + i]; b[i] = Bs[kk][tx * 4 + i]; }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int m = m0 + ty * 4 + i, n = n0 + tx * 4 + j;
+      if (m < M && n < N) C[(long long)m * ldc + n] = acc[i][j];
+    }
+}
+
+static void gemm(int M, int N, int K, const float* A, int lda, int tA, int rA, const float* B, int ldb, int tB, int rB,
+                 float* C, int ldc, cudaStream_t s) {
+  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
+  gemm_f32_kernel<<<grid, 256, 0, s>>>(M, N, K, A, lda, tA, rA, B, ldb, tB, rB, C, ldc);
+}
+
+static unsigned elem_blocks(long long total, int threads) {
+  long long b = (total + threads - 1) / threads;
+  return (unsigned)(b > 8192 ? 8192 : (b < 1 ? 1 : b));
+}
+
+// Z += bf16(bias); H = bf16(GELU(Z)) for hidden layers, H = Z for the
+// output (no bf16 rounding when rnd is 0)
+__global__ void bias_act_kernel(float* Z, float* H, const float* bias, long long M, int N, int act, int rnd) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M * N; t += (long long)gridDim.x * blockDim.x) {
+    const float b = bias[t % N];
+    const float z = Z[t] + (rnd ? bf16_round(b) : b);
+    Z[t] = z;
+    if (act) {
+      const float h = gelu(z);
+      H[t] = rnd ? bf16_round(h) : h;
+    } else {
+      H[t] = z;
+    }
+  }
+}
+
+// Mean squared error over the first B outputs of each row: dY = 2(Y − T)/(M·B)
+// (0 on padding columns), loss += Σ(Y − T)²/(M·B).
+__global__ void mse_grad_kernel(const float* Y, const float* T, float* dY, long long M, int n_out, int B, float* loss) {
+  float part = 0.f;
+  const float scale = 1.f / ((float)M * B);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < M * n_out; t += (long long)gridDim.x * blockDim.x) {
+    const long long m = t / n_out;
+    const int b = (int)(t % n_out);
+    float d = 0.f;
+    if (b < B) {
+      const float e = Y[t] - T[m * B + b];
+      d = 2.f * e * scale;
+      part += e * e * scale;
+    }
+    dY[t] = d;
+  }
+  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, part);
+}
+
+__global__ void gelu_backward_kernel(float* dH, const float* Z, long long total) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x)
+    dH[t] *= gelu_grad(Z[t]);
+}
+
+// db[n] = Σ_m dZ[m][n], one block per column
+__global__ void __launch_bounds__(256) colsum_kernel(const float* dZ, long long M, int N, float* db) {
+  const int n = blockIdx.x;
+  float s = 0.f;
+  for (long long m = threadIdx.x; m < M; m += blockDim.x) s += dZ[m * N + n];
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if ((int)threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[n] = red[0];
+}
+
+__global__ void adam_kernel(float* p, const float* g, float* m, float* v, long long n, float lr, float b1, float b2,
+                            float eps, float c1, float c2) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+// Workspace: Z1..Z3 and H1..H3 (M × 128 each), Y and dY (M × n_out), two
+// M × 128 gradient buffers.
+size_t mlp_workspace_floats(long long M, int n_out) { return (size_t)M * (8 * kWidth + 2 * n_out); }
+
+struct Work {
+  float *Z[3], *H[3], *Y, *dY, *dA, *dB;
+};
+
+static Work carve(float* ws, long long M, int n_out) {
+  Work w;
+  for (int l = 0; l < 3; ++l) {
+    w.Z[l] = ws + (size_t)M * kWidth * l;
+    w.H[l] = ws + (size_t)M * kWidth * (3 + l);
+  }
+  w.Y = ws + (size_t)M * kWidth * 6;
+  w.dY = w.Y + (size_t)M * n_out;
+  w.dA = w.dY + (size_t)M * n_out;
+  w.dB = w.dA + (size_t)M * kWidth;
+  return w;
+}
+
+// Forward pass in training arithmetic; outputs land in w.Y.
+static void mlp_forward_train(int d_in, int n_out, int rnd, const float* P, const float* X, long long M,
+                              const Work& w, cudaStream_t s) {
+  const MlpLayout L = mlp_layout(d_in, n_out);
+  const float* Hin = X;
+  for (int l = 0; l < 4; ++l) {
+    float* Zl = l < 3 ? w.Z[l] : w.Y;
+    float* Hl = l < 3 ? w.H[l] : w.Y;
+    // Z = H_prev · Wᵀ: B(k,n) = W[n·in + k]
+    gemm((int)M, L.out[l], L.in[l], Hin, L.in[l], 0, rnd, P + L.W[l], L.in[l], 1, rnd, Zl, L.out[l], s);
+    bias_act_kernel<<<elem_blocks(M * L.out[l], 256), 256, 0, s>>>(Zl, Hl, P + L.b[l], M, L.out[l], l < 3, rnd);
+    Hin = Hl;
+  }
+}
+
+// Backward pass from w.dY into the gradient vector G (same layout as P).
+static void mlp_backward(int d_in, int n_out, int rnd, const float* P, float* G, const float* X, long long M,
+                         const Work& w, cudaStream_t s) {
+  const MlpLayout L = mlp_layout(d_in, n_out);
+  float* dZ = w.dY;
+  for (int l = 3; l >= 0; --l) {
+    const float* Hprev = l > 0 ? w.H[l - 1] : X;
+    // dW = dZᵀ · H_prev (out × in): A(m,k) = dZ[k·out + m]
+    gemm(L.out[l], L.in[l], (int)M, dZ, L.out[l], 1, 0, Hprev, L.in[l], 0, rnd, G + L.W[l], L.in[l], s);
+    colsum_kernel<<<L.out[l], 256, 0, s>>>(dZ, M, L.out[l], G + L.b[l]);
+    if (l == 0) break;
+    // dH_prev = dZ · bf16(W) (M × in), then through the GELU of layer l−1
+    float* dH = dZ == w.dA ? w.dB : w.dA;
+    gemm((int)M, L.in[l], L.out[l], dZ, L.out[l], 0, 0, P + L.W[l], L.in[l], 0, rnd, dH, L.in[l], s);
+    gelu_backward_kernel<<<elem_blocks(M * L.in[l], 256), 256, 0, s>>>(dH, w.Z[l - 1], M * (long long)L.in[l]);
+    dZ = dH;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// inference: features + four dense layers on the tensor cores + residual add
+// ---------------------------------------------------------------------------
+constexpr int kInferRows = 128;     // q per tile
+constexpr int kInferThreads = 256;  // 8 warps × 16 rows
+
+__device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+struct InferArgs {
+  FeatureArgs f;
+  const __nv_bfloat16* W;  // layers' [out][in] bf16, one after another
+  const float* bias;       // layers' biases (bf16-rounded values), one after another
+  int n_out;
+  float res_scale;         // network outputs are residuals in units of res_scale
+  float clip;              // |residual| above clip is dropped (plain interpolation kept); 0: no clip
+  void* values_out;        // n × B, float or double: += residual
+  int out_f64;
+};
+
+// bf16 elements per shared-memory row: 8 extra spread the rows over the banks
+__host__ __device__ inline int act_stride(int d_in) { return (d_in > kWidth ? d_in : kWidth) + 8; }
+
+// One warp computes its 16 rows × (8·NT) output columns of a layer with
+// K = in: A fragments from the activation tile, B fragments from the
+// layer's weight rows.  Hidden layers write bf16(GELU(acc + b)) back into
+// the warp's own rows of the tile; the output layer writes acc + b to out.
+template <int NT, bool kHidden>
+__device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int ws, const float* bl,
+                                           __nv_bfloat16* act, int as, int row0, int lane, float* out, int out_ld,
+                                           int n_valid) {
+  float acc[NT][4];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+  const int g = lane >> 2, tq = lane & 3;
+  for (int k0 = 0; k0 < in; k0 += 16) {
+    uint32_t a[4];
+    const __nv_bfloat16* r0 = act + (size_t)(row0 + g) * as + k0 + 2 * tq;
+    const __nv_bfloat16* r1 = r0 + (size_t)8 * as;
+    a[0] = *reinterpret_cast<const uint32_t*>(r0);
+    a[1] = *reinterpret_cast<const uint32_t*>(r1);
+    a[2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
+    a[3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+      const __nv_bfloat16* wr = Wl + (size_t)(t * 8 + g) * ws + k0 + 2 * tq;
+      uint32_t b[2];
+      b[0] = *reinterpret_cast<const uint32_t*>(wr);
+      b[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
+      mma_bf16(acc[t], a, b);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    const int c0 = t * 8 + 2 * tq;
+    if (kHidden) {
+      const float b0 = bl[c0], b1 = bl[c0 + 1];
+      *reinterpret_cast<uint32_t*>(act + (size_t)(row0 + g) * as + c0) =
+          pack_bf16(gelu(acc[t][0] + b0), gelu(acc[t][1] + b1));
+      *reinterpret_cast<uint32_t*>(act + (size_t)(row0 + g + 8) * as + c0) =
+          pack_bf16(gelu(acc[t][2] + b0), gelu(acc[t][3] + b1));
+    } else {
+      if (c0 < n_valid) {
+        out[(row0 + g) * out_ld + c0] = acc[t][0] + bl[c0];
+        out[(row0 + g + 8) * out_ld + c0] = acc[t][2] + bl[c0];
+      }
+      if (c0 + 1 < n_valid) {
+        out[(row0 + g) * out_ld + c0 + 1] = acc[t][1] + bl[c0 + 1];
+        out[(row0 + g + 8) * out_ld + c0 + 1] = acc[t][3] + bl[c0 + 1];
+      }
+    }
+  }
+  __syncwarp();
+}
+
+struct InferSmem {
+  size_t woff[4];
+  int wstride[4];
+  size_t bias_off, act_off, out_off, total;
+};
+
+__host__ __device__ inline InferSmem infer_smem(int d_in, int n_out) {
+  const MlpLayout L = mlp_layout(d_in, n_out);
+  InferSmem s;
+  size_t o = 0;
+  for (int l = 0; l < 4; ++l) {
+    s.wstride[l] = L.in[l] + 8;
+    s.woff[l] = o;
+    o += (size_t)L.out[l] * s.wstride[l] * 2;
+  }
+  o = (o + 15) & ~size_t(15);
+  s.bias_off = o;
+  o += (size_t)(L.out[0] + L.out[1] + L.out[2] + L.out[3]) * 4;
+  o = (o + 15) & ~size_t(15);
+  s.act_off = o;
+  o += (size_t)kInferRows * act_stride(d_in) * 2;
+  o = (o + 15) & ~size_t(15);
+  s.out_off = o;
+  o += (size_t)kInferRows * n_out * 4;
+  s.total = o;
+  return s;
+}
+
+__global__ void __launch_bounds__(kInferThreads)
+mlp_infer_kernel(DevGeom g, InferArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int d_in = a.f.d_in, n_out = a.n_out, B = a.f.B;
+  const MlpLayout L = mlp_layout(d_in, n_out);
+  const InferSmem S = infer_smem(d_in, n_out);
+  float* sb = reinterpret_cast<float*>(sm + S.bias_off);
+  __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(sm + S.act_off);
+  float* out_tile = reinterpret_cast<float*>(sm + S.out_off);
+  const int as = act_stride(d_in);
+  // weights and biases once per CTA
+  {
+    long long src = 0;
+    int bo = 0;
+    for (int l = 0; l < 4; ++l) {
+      __nv_bfloat16* dst = reinterpret_cast<__nv_bfloat16*>(sm + S.woff[l]);
+      for (int t = threadIdx.x; t < L.out[l] * L.in[l]; t += blockDim.x)
+        dst[(size_t)(t / L.in[l]) * S.wstride[l] + t % L.in[l]] = a.W[src + t];
+      for (int t = threadIdx.x; t < L.out[l]; t += blockDim.x) sb[bo + t] = a.bias[bo + t];
+      src += (long long)L.out[l] * L.in[l];
+      bo += L.out[l];
+    }
+  }
+  const __nv_bfloat16* W0 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[0]);
+  const __nv_bfloat16* W1 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[1]);
+  const __nv_bfloat16* W2 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[2]);
+  const __nv_bfloat16* W3 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[3]);
+  const float* b1 = sb + L.out[0];
+  const float* b2 = b1 + L.out[1];
+  const float* b3 = b2 + L.out[2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * 16;
+  const int half_in = d_in / 2;
+  const long long n_tiles = (a.f.n + kInferRows - 1) / kInferRows;
+  for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
+    __syncthreads();  // weights staged; the previous tile's outputs consumed
+    for (int t = threadIdx.x; t < kInferRows * half_in; t += blockDim.x)
+      reinterpret_cast<uint32_t*>(act + (size_t)(t / half_in) * as)[t % half_in] = 0u;
+    __syncthreads();
+    for (int r = threadIdx.x; r < kInferRows; r += blockDim.x) {
+      const long long i = tile * kInferRows + r;
+      if (i >= a.f.n) continue;
+      __nv_bfloat16* arow = act + (size_t)r * as;
+      feature_row(g, a.f, i, [arow](int k, float v) { arow[k] = __float2bfloat16_rn(v); }, nullptr);
+    }
+    __syncthreads();
+    // each warp owns its 16 rows through all four layers
+    warp_layer<16, true>(W0, L.in[0], S.wstride[0], sb, act, as, row0, lane, nullptr, 0, 0);
+    warp_layer<16, true>(W1, L.in[1], S.wstride[1], b1, act, as, row0, lane, nullptr, 0, 0);
+    warp_layer<16, true>(W2, L.in[2], S.wstride[2], b2, act, as, row0, lane, nullptr, 0, 0);
+    for (int c = 0; c < n_out; c += 8)
+      warp_layer<1, false>(W3 + (size_t)c * S.wstride[3], L.in[3], S.wstride[3], b3 + c, act, as, row0, lane,
+                           out_tile + c, n_out, n_out - c);
+    __syncthreads();
+    for (int t = threadIdx.x; t < kInferRows * B; t += blockDim.x) {
+      const int r = t / B, b = t % B;
+      const long long i = tile * kInferRows + r;
+      if (i >= a.f.n || a.f.status[i]) continue;
+      const float res = out_tile[r * n_out + b] * a.res_scale;
+      if (a.clip > 0.f && !(fabsf(res) <= a.clip)) continue;
+      if (a.out_f64) static_cast<double*>(a.values_out)[i * B + b] += (double)res;
+      else static_cast<float*>(a.values_out)[i * B + b] += res;
+    }
+  }
+}
+
+}  // namespace brx
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+using namespace brx_detail;
+
+namespace {
+
+bool mlp_dims_ok(const brx_mlp_dims* d) {
+  return d && d->d_in >= 16 && d->d_in % 16 == 0 && d->d_in <= 512 && d->n_out >= 8 && d->n_out % 8 == 0 &&
+         d->n_out <= 64 && d->n_modes >= 1 && d->n_modes <= d->n_out && (d->flags & ~BRX_MLP_FP32) == 0;
+}
+
+int feature_cols(int B) { return 12 + 9 * B; }
+
+brx::FeatureArgs feature_args(const brx_handle* h, const double* q_ir, const int32_t* node, const int32_t* nw,
+                              const int32_t* vidx, const double* w, const int32_t* status, long long n, int d_in,
+                              float omega_scale) {
+  brx::FeatureArgs a{};
+  a.q_ir = q_ir;
+  a.node = node;
+  a.nw = nw;
+  a.vidx = vidx;
+  a.w = w;
+  a.status = status;
+  a.n = n;
+  a.values = h->vals.data.p;
+  a.values_f64 = h->vals.store == brx::ST_F64;
+  a.B = h->vals.B;
+  a.d_in = d_in;
+  a.inv_omega = 1.f / omega_scale;
+  return a;
+}
+
+brx_status check_model_fits(brx_handle* h, const brx_mlp_dims* d) {
+  if (!mlp_dims_ok(d)) return fail(h, BRX_ERR_INVALID_ARGUMENT, "invalid residual model dimensions");
+  if (!h->filled) return fail(h, BRX_ERR_NOT_FILLED, "The interpolation data must be filled before interpolating.");
+  if (h->vals.s != 1 || h->vals.cplx || h->vals.B != d->n_modes)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "the residual model needs one real eigenvalue per mode");
+  if (d->d_in < feature_cols(h->vals.B))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "d_in is too small for the feature row");
+  if (brx::infer_smem(d->d_in, d->n_out).total > h->smem_optin)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "the residual model does not fit in shared memory");
+  return BRX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t brx_mlp_param_count(const brx_mlp_dims* d) {
+  if (!mlp_dims_ok(d)) return -1;
+  return brx::mlp_layout(d->d_in, d->n_out).total;
+}
+
+int64_t brx_mlp_workspace_floats(const brx_mlp_dims* d, int64_t batch) {
+  if (!mlp_dims_ok(d) || batch < 1) return -1;
+  return (int64_t)brx::mlp_workspace_floats(batch, d->n_out);
+}
+
+brx_status brx_mlp_features(brx_handle* h, const brx_locate_out* records, int64_t n, const brx_mlp_dims* d,
+                            float omega_scale, float* X, float* base, void* stream) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!records || !X || !base || n < 0 || !(omega_scale > 0.f))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "features need records, X, base and a positive omega_scale");
+  if (!records->q_ir || !records->node || !records->n_weights || !records->vertex || !records->weight ||
+      !records->status)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "every locate record array is needed for features");
+  brx_status st = check_model_fits(h, d);
+  if (st) return st;
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->sc[0].stream;
+  if (n == 0) return BRX_OK;
+  brx::FeatureArgs a = feature_args(h, records->q_ir, records->node, records->n_weights, records->vertex,
+                                    records->weight, records->status, n, d->d_in, omega_scale);
+  long long blocks = (n + 127) / 128;
+  if (blocks > (long long)h->num_sms * 16) blocks = (long long)h->num_sms * 16;
+  brx::mlp_features_kernel<<<(unsigned)blocks, 128, 0, s>>>(h->g, a, X, base);
+  ++h->launches;
+  BRX_CUDA(h, cudaGetLastError());
+  if (!stream) BRX_CUDA(h, cudaStreamSynchronize(s));
+  return BRX_OK;
+}
+
+brx_status brx_mlp_train_step(const brx_mlp_dims* d, float* params, float* grads, float* adam_m, float* adam_v,
+                              int32_t step, float lr, const float* X, const float* T, int64_t batch, float* workspace,
+                              float* loss, void* stream) {
+  if (!mlp_dims_ok(d) || !params || !grads || !X || !T || !workspace || !loss || batch < 1 || batch > (1LL << 24))
+    return BRX_ERR_INVALID_ARGUMENT;
+  if ((adam_m == nullptr) != (adam_v == nullptr) || (adam_m && step < 1)) return BRX_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const brx::Work w = brx::carve(workspace, batch, d->n_out);
+  const int rnd = (d->flags & BRX_MLP_FP32) ? 0 : 1;
+  brx::mlp_forward_train(d->d_in, d->n_out, rnd, params, X, batch, w, s);
+  if (cudaMemsetAsync(loss, 0, sizeof(float), s) != cudaSuccess) return BRX_ERR_CUDA;
+  brx::mse_grad_kernel<<<brx::elem_blocks(batch * d->n_out, 256), 256, 0, s>>>(w.Y, T, w.dY, batch, d->n_out,
+                                                                              d->n_modes, loss);
+  brx::mlp_backward(d->d_in, d->n_out, rnd, params, grads, X, batch, w, s);
+  if (adam_m) {
+    const long long np = brx::mlp_layout(d->d_in, d->n_out).total;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)step), c2 = 1.f - std::pow(b2, (float)step);
+    brx::adam_kernel<<<brx::elem_blocks(np, 256), 256, 0, s>>>(params, grads, adam_m, adam_v, np, lr, b1, b2, 1e-8f,
+                                                               c1, c2);
+  }
+  return cudaGetLastError() == cudaSuccess ? BRX_OK : BRX_ERR_CUDA;
+}
+
+brx_status brx_mlp_forward(const brx_mlp_dims* d, const float* params, const float* X, int64_t batch, float* Y,
+                           float* workspace, void* stream) {
+  if (!mlp_dims_ok(d) || !params || !X || !Y || !workspace || batch < 1 || batch > (1LL << 24))
+    return BRX_ERR_INVALID_ARGUMENT;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const brx::Work w = brx::carve(workspace, batch, d->n_out);
+  brx::mlp_forward_train(d->d_in, d->n_out, (d->flags & BRX_MLP_FP32) ? 0 : 1, params, X, batch, w, s);
+  if (cudaMemcpyAsync(Y, w.Y, sizeof(float) * batch * d->n_out, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return BRX_ERR_CUDA;
+  return cudaGetLastError() == cudaSuccess ? BRX_OK : BRX_ERR_CUDA;
+}
+
+brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const float* params, float omega_scale,
+                                  float res_scale, float clip) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!params) {
+    h->mlp_on = false;
+    return BRX_OK;
+  }
+  if (!(omega_scale > 0.f) || !(res_scale > 0.f) || !(clip >= 0.f))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "residual model scales must be positive");
+  brx_status st = check_model_fits(h, d);
+  if (st) return st;
+  const brx::MlpLayout L = brx::mlp_layout(d->d_in, d->n_out);
+  std::vector<__nv_bfloat16> W;
+  std::vector<float> b;
+  for (int l = 0; l < 4; ++l) {
+    for (long long t = 0; t < (long long)L.out[l] * L.in[l]; ++t) W.push_back(__float2bfloat16_rn(params[L.W[l] + t]));
+    for (int t = 0; t < L.out[l]; ++t) b.push_back(__bfloat162float(__float2bfloat16_rn(params[L.b[l] + t])));
+  }
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  BRX_CUDA(h, h->mlp_w.ensure(W.size() * sizeof(__nv_bfloat16)));
+  BRX_CUDA(h, h->mlp_b.ensure(b.size() * sizeof(float)));
+  BRX_CUDA(h, cudaMemcpy(h->mlp_w.p, W.data(), W.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
+  BRX_CUDA(h, cudaMemcpy(h->mlp_b.p, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice));
+  const size_t smem = brx::infer_smem(d->d_in, d->n_out).total;
+  BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  h->mlp_dims = *d;
+  h->mlp_omega_scale = omega_scale;
+  h->mlp_res_scale = res_scale;
+  h->mlp_clip = clip;
+  h->mlp_on = true;
+  return BRX_OK;
+}
+
+}  // extern "C"
+
+namespace brx_detail {
+
+int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_out, bool out_f32, cudaStream_t cs) {
+  if (!h->mlp_on || n <= 0) return 0;
+  brx::InferArgs a{};
+  a.f = feature_args(h, s.r.q_ir, s.r.node, s.r.nw, s.r.vidx, s.r.w, s.r.status, n, h->mlp_dims.d_in,
+                     h->mlp_omega_scale);
+  a.W = static_cast<const __nv_bfloat16*>(h->mlp_w.p);
+  a.bias = static_cast<const float*>(h->mlp_b.p);
+  a.n_out = h->mlp_dims.n_out;
+  a.res_scale = h->mlp_res_scale;
+  a.clip = h->mlp_clip;
+  a.values_out = values_out;
+  a.out_f64 = !out_f32;
+  const size_t smem = brx::infer_smem(a.f.d_in, a.n_out).total;
+  const long long tiles = (n + brx::kInferRows - 1) / brx::kInferRows;
+  const long long grid = std::min<long long>(tiles, (long long)h->num_sms);
+  brx::mlp_infer_kernel<<<(unsigned)grid, brx::kInferThreads, smem, cs>>>(h->g, a);
+  return 1;
+}
+
+}  // namespace brx_detail

@@ -206,6 +206,59 @@ brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double* Q, int64_t
                                          void* values_out, void* vectors_out,
                                          uint32_t flags, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Learned eigenvalue residual.  No counterpart in the reference: a small
+ * MLP (d_in → 128 → 128 → 128 → n_out, GELU, bf16 weights, FP32
+ * accumulation) predicts per mode the exact eigenvalue minus its trellis
+ * interpolation, so that a coarser trellis serves the accuracy of a finer
+ * one.  Feature rows are built on the GPU from locate records:
+ *   0-2 position of q in its node cell; 3-10 the weights of the vertex
+ *   slots; 11 tetrahedron flag; 12 + slot·B + mode the vertex eigenvalues;
+ *   12 + 8B + mode the interpolated eigenvalues; zeros up to d_in;
+ * eigenvalues divided by omega_scale.  d_in ≥ 12 + 9B, a multiple of 16,
+ * ≤ 512; n_out a multiple of 8, ≤ 64, ≥ n_modes = B.  Parameters are one
+ * FP32 vector: W0 (128×d_in, row-major [out][in]), b0, W1, b1, W2, b2,
+ * W3 (n_out×128), b3.  Every pointer below except the host params of
+ * brx_set_residual_model is a device pointer. */
+typedef struct brx_mlp_dims {
+  int32_t d_in;
+  int32_t n_out;
+  int32_t n_modes;
+  int32_t flags;  /* BRX_MLP_FP32: training kernels skip the bf16 rounding */
+} brx_mlp_dims;
+#define BRX_MLP_FP32 0x1
+
+/* Length of the parameter vector, or −1 for invalid dimensions. */
+int64_t brx_mlp_param_count(const brx_mlp_dims* d);
+/* Floats of workspace that brx_mlp_train_step / brx_mlp_forward need. */
+int64_t brx_mlp_workspace_floats(const brx_mlp_dims* d, int64_t batch);
+
+/* Feature rows X (n × d_in) and plain interpolated eigenvalues base (n × B,
+ * NaN where the locate failed) from device locate records (every array of
+ * `records` set).  stream NULL: the handle's stream, synchronised. */
+brx_status brx_mlp_features(brx_handle* h, const brx_locate_out* records, int64_t n, const brx_mlp_dims* d,
+                            float omega_scale, float* X, float* base, void* stream);
+
+/* One training step on a batch: forward (weights and activations rounded
+ * to bf16 as inference rounds them), mean squared error against T
+ * (batch × n_modes) written to *loss, gradients into grads (same layout as
+ * params), then, when adam_m/adam_v are given, an Adam update (β 0.9/0.999,
+ * ε 1e-8, bias correction with step ≥ 1) of params. */
+brx_status brx_mlp_train_step(const brx_mlp_dims* d, float* params, float* grads, float* adam_m, float* adam_v,
+                              int32_t step, float lr, const float* X, const float* T, int64_t batch,
+                              float* workspace, float* loss, void* stream);
+
+/* Network outputs Y (batch × n_out) in training arithmetic. */
+brx_status brx_mlp_forward(const brx_mlp_dims* d, const float* params, const float* X, int64_t batch, float* Y,
+                           float* workspace, void* stream);
+
+/* Attach a trained model (host params) to the handle: from now on every
+ * query adds res_scale × output to the interpolated eigenvalues, except
+ * where that correction exceeds clip in magnitude (clip 0: never), which
+ * keeps the plain interpolation.  params NULL detaches the model. */
+brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const float* params, float omega_scale,
+                                  float res_scale, float clip);
+
 /* Wait for work queued with BRX_FLAG_ASYNC and report its status. */
 brx_status brx_sync(brx_handle* h, void* stream);
 

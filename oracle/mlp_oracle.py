@@ -1,0 +1,187 @@
+"""CPU oracle for the learned eigenvalue residual: feature rows, the MLP's
+forward pass, its gradients and one Adam update, in numpy.
+
+Test infrastructure only.  This file is imported by tests/, by the package's
+smoke check and by bench.py's CPU baseline, never by the product path.
+
+The reference has no learned part, so there is no reference code to follow.
+This file restates the network that include/brx.h defines (d_in → 128 → 128
+→ 128 → n_out, exact-erf GELU, mean squared error over the first n_modes
+outputs).  It is pinned two ways: its analytic gradients agree with central
+finite differences in FP64 (tests/test_mlp_oracle.py), and its feature base
+column equals the C oracle's own interpolated eigenvalues.
+
+bfloat16 rounding is round-to-nearest-even on the top 16 bits of the float32
+pattern, which is what __float2bfloat16_rn does for finite values.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+WIDTH = 128
+
+
+def bf16(x):
+    """Round float32 values to the nearest bfloat16 (ties to even), as float32."""
+    a = np.ascontiguousarray(np.asarray(x, np.float32))
+    u = a.view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32).reshape(a.shape)
+
+
+def feature_width(n_modes):
+    """Smallest legal d_in (a multiple of 16) for n_modes eigenvalues."""
+    need = 12 + 9 * n_modes
+    return (need + 15) // 16 * 16
+
+
+def layout(d_in, n_out):
+    """[(W offset, b offset, in, out)] of the four layers in the flat vector."""
+    dims = [(d_in, WIDTH), (WIDTH, WIDTH), (WIDTH, WIDTH), (WIDTH, n_out)]
+    out, o = [], 0
+    for i, n in dims:
+        out.append((o, o + n * i, i, n))
+        o += n * i + n
+    return out, o
+
+
+def unpack(params, d_in, n_out):
+    lay, total = layout(d_in, n_out)
+    p = np.asarray(params)
+    assert p.size == total
+    return [(p[w:w + n * i].reshape(n, i), p[b:b + n]) for w, b, i, n in lay]
+
+
+def init_params(d_in, n_out, seed=0):
+    """Uniform ±1/√fan_in weights, zero biases (float32)."""
+    rng = np.random.default_rng(seed)
+    lay, total = layout(d_in, n_out)
+    p = np.zeros(total, np.float32)
+    for w, b, i, n in lay:
+        lim = 1.0 / np.sqrt(i)
+        p[w:w + n * i] = rng.uniform(-lim, lim, n * i).astype(np.float32)
+    return p
+
+
+def _erf(x):
+    try:
+        from scipy.special import erf
+        return erf(x)
+    except ImportError:  # pragma: no cover
+        import math
+        return np.vectorize(math.erf)(x)
+
+
+def gelu(x):
+    return 0.5 * x * (1.0 + _erf(x / np.sqrt(2.0)))
+
+
+def gelu_grad(x):
+    return 0.5 * (1.0 + _erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
+
+
+def forward(params, X, d_in, n_out, rounding=True):
+    """FP64 forward pass on bf16-rounded operands (rounding=True, the GPU's
+    arithmetic up to FP32 accumulation order) or on the FP64 values as given
+    (rounding=False, for finite differences and the FP32 training mode).
+
+    Returns (Z list, H list, Y): Z the pre-activations of the three hidden
+    layers, H their activations (rounded like the GPU's), Y the outputs."""
+    layers = unpack(np.asarray(params, np.float32 if rounding else np.float64), d_in, n_out)
+    r = bf16 if rounding else (lambda a: np.asarray(a, np.float64))
+    H = r(X).astype(np.float64)
+    Zs, Hs = [], []
+    for l, (W, b) in enumerate(layers):
+        Z = H @ r(W).astype(np.float64).T + r(b).astype(np.float64)
+        if l < 3:
+            Zs.append(Z)
+            Hn = gelu(Z)
+            H = r(Hn.astype(np.float32)).astype(np.float64) if rounding else Hn
+            Hs.append(H)
+        else:
+            Y = Z
+    return Zs, Hs, Y
+
+
+def loss_and_grads(params, X, T, d_in, n_out, n_modes, rounding=True):
+    """Mean squared error over the first n_modes outputs and its gradient
+    (straight through the bf16 rounding), both FP64."""
+    layers = unpack(np.asarray(params, np.float32 if rounding else np.float64), d_in, n_out)
+    r = bf16 if rounding else (lambda a: np.asarray(a, np.float64))
+    Zs, Hs, Y = forward(params, X, d_in, n_out, rounding)
+    M = X.shape[0]
+    E = Y[:, :n_modes] - T
+    loss = float(np.sum(E * E) / (M * n_modes))
+    dZ = np.zeros_like(Y)
+    dZ[:, :n_modes] = 2.0 * E / (M * n_modes)
+    grads = []
+    X64 = r(X).astype(np.float64)
+    for l in range(3, -1, -1):
+        Hprev = Hs[l - 1] if l > 0 else X64
+        gW = dZ.T @ Hprev
+        gb = dZ.sum(axis=0)
+        grads.append((gW, gb))
+        if l == 0:
+            break
+        W = r(layers[l][0]).astype(np.float64)
+        dZ = (dZ @ W) * gelu_grad(Zs[l - 1])
+    grads.reverse()
+    flat = np.concatenate([np.concatenate([gW.ravel(), gb]) for gW, gb in grads])
+    return loss, flat
+
+
+def adam(params, grads, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
+    """One Adam update in float32 (returns new params, m, v)."""
+    p = np.asarray(params, np.float32)
+    g = np.asarray(grads, np.float32)
+    m = (np.float32(b1) * m + np.float32(1 - b1) * g).astype(np.float32)
+    v = (np.float32(b2) * v + np.float32(1 - b2) * g * g).astype(np.float32)
+    c1 = np.float32(1 - b1 ** step)
+    c2 = np.float32(1 - b2 ** step)
+    p = (p - np.float32(lr) * (m / c1) / (np.sqrt(v / c2) + np.float32(eps))).astype(np.float32)
+    return p, m, v
+
+
+def features(records, values, knots, outer_B, n_modes, d_in, omega_scale):
+    """Feature rows (n × d_in float32) and plain interpolated eigenvalues
+    (n × n_modes float32, NaN where the locate failed) from locate records
+    (dict of q_ir, node, n_weights, vertex, weight, status), vertex
+    eigenvalues (n_vertices × n_modes) and the trellis knots."""
+    q = np.asarray(records["q_ir"], np.float64)
+    n = q.shape[0]
+    B = n_modes
+    X = np.zeros((n, d_in), np.float32)
+    base = np.full((n, B), np.nan, np.float32)
+    ok = np.asarray(records["status"]) == 0
+    vals32 = np.asarray(values).reshape(-1, B).astype(np.float32)
+    inv = np.float32(1.0) / np.float32(omega_scale)
+    Bm = np.asarray(outer_B, np.float64).reshape(3, 3)
+    # xyz_i = ((0 + B0i h0) + B1i h1) + B2i h2, unfused like the device code
+    x = np.zeros((n, 3))
+    for i in range(3):
+        s = np.zeros(n)
+        for k in range(3):
+            s = s + Bm[k, i] * q[:, k]
+        x[:, i] = s
+    node = np.asarray(records["node"]).reshape(n, 2)
+    nx = len(knots[0]) - 1
+    ny = len(knots[1]) - 1
+    sub = np.stack([node[:, 0] % nx, (node[:, 0] // nx) % ny, node[:, 0] // (nx * ny)], axis=1)
+    nw = np.minimum(np.asarray(records["n_weights"]), 8)
+    vid = np.asarray(records["vertex"]).reshape(n, 8)
+    w = np.asarray(records["weight"]).reshape(n, 8)
+    for i in np.nonzero(ok)[0]:
+        for d in range(3):
+            lo, hi = knots[d][sub[i, d]], knots[d][sub[i, d] + 1]
+            X[i, d] = np.float32((x[i, d] - lo) / (hi - lo))
+        X[i, 3:3 + nw[i]] = w[i, :nw[i]].astype(np.float32)
+        X[i, 11] = 1.0 if node[i, 1] >= 0 else 0.0
+        for b in range(B):
+            s = 0.0
+            for k in range(nw[i]):
+                ev = vals32[vid[i, k], b]
+                X[i, 12 + k * B + b] = ev * inv
+                s = s + float(w[i, k]) * float(ev)
+            base[i, b] = np.float32(s)
+            X[i, 12 + 8 * B + b] = np.float32(s) * inv
+    return X, base
