@@ -9,6 +9,7 @@
 //   col 11     1 for a tetrahedron, 0 for a cube node
 //   col 12 …   vertex eigenvalues, slot-major: 12 + slot·B + mode
 //   then       interpolated eigenvalues, B columns
+//   then       position of q in the trellis box, (x − knot_first)/(knot_last − knot_first), 3 columns
 //   then       zero padding up to d_in
 //
 // eigenvalues divided by omega_scale.  Training runs on the FP32 CUDA-core
@@ -122,6 +123,10 @@ __device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i,
     }
     if (base) base[b] = (float)s;
     put(12 + 8 * a.B + b, (float)s * a.inv_omega);
+  }
+  for (int d = 0; d < 3; ++d) {
+    const double lo = g.knots[d][0], hi = g.knots[d][g.n_knots[d] - 1];
+    put(12 + 9 * a.B + d, (float)((x[d] - lo) / (hi - lo)));
   }
 }
 
@@ -515,7 +520,7 @@ bool mlp_dims_ok(const brx_mlp_dims* d) {
          d->n_out <= 64 && d->n_modes >= 1 && d->n_modes <= d->n_out && (d->flags & ~BRX_MLP_FP32) == 0;
 }
 
-int feature_cols(int B) { return 12 + 9 * B; }
+int feature_cols(int B) { return 15 + 9 * B; }
 
 brx::FeatureArgs feature_args(const brx_handle* h, const double* q_ir, const int32_t* node, const int32_t* nw,
                               const int32_t* vidx, const double* w, const int32_t* status, long long n, int d_in,

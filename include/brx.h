@@ -214,8 +214,9 @@ brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double* Q, int64_t
  * one.  Feature rows are built on the GPU from locate records:
  *   0-2 position of q in its node cell; 3-10 the weights of the vertex
  *   slots; 11 tetrahedron flag; 12 + slot·B + mode the vertex eigenvalues;
- *   12 + 8B + mode the interpolated eigenvalues; zeros up to d_in;
- * eigenvalues divided by omega_scale.  d_in ≥ 12 + 9B, a multiple of 16,
+ *   12 + 8B + mode the interpolated eigenvalues; 12 + 9B + 0..2 the
+ *   position of q in the trellis's bounding box; zeros up to d_in;
+ * eigenvalues divided by omega_scale.  d_in ≥ 15 + 9B, a multiple of 16,
  * ≤ 512; n_out a multiple of 8, ≤ 64, ≥ n_modes = B.  Parameters are one
  * FP32 vector: W0 (128×d_in, row-major [out][in]), b0, W1, b1, W2, b2,
  * W3 (n_out×128), b3.  Every pointer below except the host params of

@@ -31,7 +31,7 @@ def bf16(x):
 
 def feature_width(n_modes):
     """Smallest legal d_in (a multiple of 16) for n_modes eigenvalues."""
-    need = 12 + 9 * n_modes
+    need = 15 + 9 * n_modes
     return (need + 15) // 16 * 16
 
 
@@ -184,4 +184,7 @@ def features(records, values, knots, outer_B, n_modes, d_in, omega_scale):
                 s = s + float(w[i, k]) * float(ev)
             base[i, b] = np.float32(s)
             X[i, 12 + 8 * B + b] = np.float32(s) * inv
+        for d in range(3):
+            lo, hi = knots[d][0], knots[d][-1]
+            X[i, 12 + 9 * B + d] = np.float32((x[i, d] - lo) / (hi - lo))
     return X, base

@@ -58,7 +58,7 @@ def _grad_case(seed, fp32, n=3000):
     m = ResidualModel(6, fp32_training=fp32, seed=seed)
     m.params = (m.params + rng.normal(scale=0.02, size=m.n_params)).astype(np.float32)
     X = rng.normal(size=(n, m.d_in)).astype(np.float32)
-    X[:, 70:] = 0.0
+    X[:, 72:] = 0.0
     T = rng.normal(size=(n, 6)).astype(np.float32)
     return m, X, T
 
@@ -181,7 +181,7 @@ def test_training_beats_plain_coarse_interpolation(coarse):
     Qt = rng.uniform(-1, 1, (200_000, 3))
     wt, _ = model.modes(Qt, chunk=8192)
     m = ResidualModel(B, seed=0)
-    hist = m.train_on(g, Qt, wt, epochs=6, batch=2048, lr=2e-3)
+    hist = m.train_on(g, Qt, wt, epochs=10, batch=1024, lr=2e-3)
     assert hist[-1] < 0.5 * hist[0]
     Qe = rng.uniform(-1, 1, (20_000, 3))
     we, _ = model.modes(Qe, chunk=8192)

@@ -22,7 +22,7 @@ def test_layout_counts():
     lay, total = M.layout(80, 8)
     assert total == 128 * 80 + 128 + 2 * (128 * 128 + 128) + 8 * 128 + 8
     assert lay[3][2:] == (128, 8)
-    assert M.feature_width(6) == 80 and M.feature_width(48) == 448
+    assert M.feature_width(6) == 80 and M.feature_width(48) == 448 and M.feature_width(49) == 464
 
 
 def test_gradients_match_finite_differences():
@@ -77,3 +77,5 @@ def test_feature_base_equals_oracle_interpolation():
     assert np.all((X[:, 0:3] >= -1e-6) & (X[:, 0:3] <= 1 + 1e-6))
     assert np.allclose(X[:, 3:11].sum(axis=1), 1.0, atol=1e-5)
     assert np.allclose(X[:, 12 + 8 * B:12 + 9 * B] * 50.0, base, rtol=1e-6)
+    box = X[:, 12 + 9 * B:15 + 9 * B]
+    assert np.all((box >= -1e-6) & (box <= 1 + 1e-6))
