@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <new>
 #include <string>
 #include <vector>
@@ -75,6 +76,10 @@ bool host_ptr(const void* p) {
 }
 
 int span(const Interp& d) { return d.el[0] + d.el[1] + d.el[2]; }
+
+// whether the gather of d takes the group-ordered kernel (launch_t in
+// brx_gather.cu): anything but scalars without a phase factor
+bool uses_groups(const Interp& d, bool phase) { return d.el[1] / 3 != 0 || d.el[2] / 9 != 0 || phase; }
 
 // rotation support, mirroring Interpolator::rotate_in_place (src/interpolator.hpp:387-428)
 brx_status rotation_mode(const Interp& d, int* mode, std::string* msg) {
@@ -377,8 +382,12 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       BRX_CUDA(h, cp(lout->status ? lout->status + base : nullptr, s.r.status, 4 * (size_t)m));
       continue;
     }
-    h->launches += launch_grouping(s.r.key, m, n_group_keys(h->g.n_cube, h->g.n_tets), kGroupQ, s.sort_scratch,
-                                   s.order, s.groups, s.n_groups, cs);
+    // the group-ordered gather serves vector and matrix data; scalar-only
+    // data (eigenvalues) is gathered per q and needs no grouping
+    const bool grouped = uses_groups(h->vals, false) || (h->vecs.present && uses_groups(h->vecs, h->vecs.cplx));
+    if (grouped)
+      h->launches += launch_grouping(s.r.key, m, n_group_keys(h->g.n_cube, h->g.n_tets), kGroupQ, s.sort_scratch,
+                                     s.order, s.groups, s.n_groups, cs);
     if (ev[2]) cudaEventRecord(ev[2], cs);
     char* vdst = o_host ? static_cast<char*>(s.vbuf.p) : static_cast<char*>(vals_out) + vrow * (size_t)base;
     {
@@ -399,6 +408,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     }
     if (ev[4]) {
       cudaEventRecord(ev[4], cs);
+      if (!grouped) cudaMemsetAsync(s.n_groups, 0, sizeof(int32_t), cs);
       if (int32_t* slot = next_group_slot(h)) cudaMemcpyAsync(slot, s.n_groups, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
     }
     BRX_CUDA(h, cudaGetLastError());
@@ -607,6 +617,51 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
     UP(plane.data(), plane.size(), g.face_plane32);
     UP(band.data(), band.size(), g.face_band32);
     UP(wm.data(), wm.size(), g.wedge_m32);
+    // Barycentric planes of every tetrahedron, w_j(x) = a_j·x + c_j with
+    // w_j = orient3d(…x…)/(6V) as tet_contains forms them: (x−d)·n_j/(6V) for
+    // j < 3 and (x−a)·n_3/(6V).  A tetrahedron whose planes do not reproduce
+    // w_j(v_k) = δ_jk gets NaN offsets and is never screened out.
+    std::vector<float> tp(16 * (size_t)G.n_tets);
+    for (long long t = 0; t < G.n_tets; ++t) {
+      const double* P[4];
+      for (int k = 0; k < 4; ++k) P[k] = G.vertex_xyz + 3 * (long long)G.tet_vertices[4 * t + k];
+      const double* A = P[0];
+      const double* Bv = P[1];
+      const double* Cv = P[2];
+      const double* D = P[3];
+      auto cross = [](const double* u0, const double* u1, const double* v0, const double* v1, double* o) {
+        const double u[3] = {u1[0] - u0[0], u1[1] - u0[1], u1[2] - u0[2]};
+        const double v[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+        o[0] = u[1] * v[2] - u[2] * v[1];
+        o[1] = u[2] * v[0] - u[0] * v[2];
+        o[2] = u[0] * v[1] - u[1] * v[0];
+      };
+      double n[4][3], c[4];
+      cross(D, Bv, D, Cv, n[0]);   // (b−d)×(c−d)
+      cross(D, Cv, D, A, n[1]);    // (c−d)×(a−d)
+      cross(D, A, D, Bv, n[2]);    // (a−d)×(b−d)
+      cross(A, Bv, A, Cv, n[3]);   // (b−a)×(c−a), negated below
+      for (int i = 0; i < 3; ++i) n[3][i] = -n[3][i];
+      const double vol6 = G.tet_volume[t] * 6.0;
+      for (int j = 0; j < 4; ++j) {
+        const double* o = j < 3 ? D : A;
+        for (int i = 0; i < 3; ++i) n[j][i] /= vol6;
+        c[j] = -(o[0] * n[j][0] + o[1] * n[j][1] + o[2] * n[j][2]);
+      }
+      bool good = std::isfinite(vol6) && vol6 != 0.0;
+      for (int j = 0; j < 4 && good; ++j)
+        for (int k = 0; k < 4; ++k) {
+          const double wv = n[j][0] * P[k][0] + n[j][1] * P[k][1] + n[j][2] * P[k][2] + c[j];
+          const double scale = std::fabs(n[j][0] * P[k][0]) + std::fabs(n[j][1] * P[k][1]) +
+                               std::fabs(n[j][2] * P[k][2]) + std::fabs(c[j]) + 1.0;
+          if (!(std::fabs(wv - (j == k ? 1.0 : 0.0)) <= 1e-9 * scale)) good = false;
+        }
+      for (int j = 0; j < 4; ++j) {
+        for (int i = 0; i < 3; ++i) tp[16 * t + 4 * j + i] = good ? (float)n[j][i] : 0.f;
+        tp[16 * t + 4 * j + 3] = good ? (float)c[j] : std::numeric_limits<float>::quiet_NaN();
+      }
+    }
+    UP(tp.data(), tp.size(), g.tet_plane32);
   }
 #undef UP
   // the host copy keeps only counts: no pointer into caller memory survives

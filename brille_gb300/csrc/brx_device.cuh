@@ -125,6 +125,7 @@ struct DevGeom {
   const float* face_band32;    // n_faces: width of the tolerance band in distance
   const float* wedge_m32;      // (n_ops + 1) × n_wedge × 3 (last block: identity)
   float wedge_band32;          // width of the wedge tolerance band
+  const float* tet_plane32;    // n_tets × 4 × (a_x, a_y, a_z, c): barycentric w_j(x) = a_j·x + c_j
   int32_t screen;              // 0 disables the screens (exact FP64 everywhere)
   Tol t_main;               // (float_tolerance, digit)
   Tol t_def;                // (0, 1): the reference's default comparisons

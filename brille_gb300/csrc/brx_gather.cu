@@ -872,9 +872,15 @@ int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32
 // grouping: counting sort of q by group key, then one work descriptor per
 // group (at most kGroupQ q each)
 // ---------------------------------------------------------------------------
+// Lanes of a warp holding the same key add once, through their lowest lane:
+// trellises with few tetrahedra put millions of q on a handful of keys.
 __global__ void key_hist_kernel(const int32_t* key, long long n, int32_t* counts) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    atomicAdd(counts + key[i], 1);
+  const int lane = threadIdx.x & 31;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int32_t k = key[i];
+    const unsigned peers = __match_any_sync(__activemask(), k);
+    if (lane == __ffs(peers) - 1) atomicAdd(counts + k, __popc(peers));
+  }
 }
 
 constexpr int kScanThreads = 1024, kScanPer = 8;
@@ -941,8 +947,14 @@ __global__ void scan_apply_kernel(const int32_t* in, long long m, const int32_t*
 }
 
 __global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cursor, int32_t* order) {
+  const int lane = threadIdx.x & 31;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    int pos = atomicAdd(cursor + key[i], 1);
+    const int32_t k = key[i];
+    const unsigned peers = __match_any_sync(__activemask(), k);
+    const int leader = __ffs(peers) - 1;
+    int pos = 0;
+    if (lane == leader) pos = atomicAdd(cursor + k, __popc(peers));
+    pos = __shfl_sync(peers, pos, leader) + __popc(peers & ((1u << lane) - 1u));
     order[pos] = (int32_t)i;
   }
 }

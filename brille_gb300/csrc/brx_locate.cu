@@ -319,6 +319,23 @@ __device__ double tet_contains(const DevGeom& g, long long t, const double x[3],
   return any_neg ? mn : 0.0;
 }
 
+// FP32 screen of one tetrahedron: true only when some barycentric weight is
+// negative by more than a margin of 1e-5 of its magnitude scale (25× the FP32
+// evaluation error), so that the exact test of tet_contains would find it
+// negative beyond the default tolerance too.  NaN planes never screen out.
+__device__ __forceinline__ bool tet_screened_out(const DevGeom& g, long long t, float x0, float x1, float x2,
+                                                 float ax) {
+  const float4* P = reinterpret_cast<const float4*>(g.tet_plane32) + 4 * t;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float4 p = __ldg(P + j);
+    const float w = fmaf(p.x, x0, fmaf(p.y, x1, fmaf(p.z, x2, p.w)));
+    const float m = 1e-5f * ((fabsf(p.x) + fabsf(p.y) + fabsf(p.z)) * ax + fabsf(p.w)) + 1e-12f;
+    if (w < -m) return true;
+  }
+  return false;
+}
+
 // Returns the number of (vertex, weight) pairs, or −status.
 __device__ int node_weights(const DevGeom& g, long long node, const double x[3], int32_t* tet_out,
                             int32_t vidx[8], double w8[8]) {
@@ -348,6 +365,23 @@ __device__ int node_weights(const DevGeom& g, long long node, const double x[3],
   if (type == BRX_NODE_POLY) {
     const int32_t tb = __ldg(g.poly_tet_offset + ni), te = __ldg(g.poly_tet_offset + ni + 1);
     double w[4] = {0, 0, 0, 0};
+    if (g.screen) {
+      // first containing tetrahedron in order, skipping those the FP32
+      // screen rules out; none found: the exact loop below (with its
+      // fallback) decides
+      const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+      const float ax = fabsf(x0) + fabsf(x1) + fabsf(x2);
+      for (int32_t t = tb; t < te; ++t) {
+        if (tet_screened_out(g, t, x0, x1, x2, ax)) continue;
+        if (tet_contains(g, t, x, w, true) >= 0.0) {
+          int n = 0;
+          for (int j = 0; j < 4; ++j)
+            if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
+          *tet_out = t;
+          return n;
+        }
+      }
+    }
     double best = 0.0;
     int32_t best_i = -1;
     for (int32_t t = tb; t < te; ++t) {

@@ -92,16 +92,11 @@ __device__ __forceinline__ float vertex_value(const FeatureArgs& a, long long v,
                       : static_cast<const float*>(a.values)[v * a.B + b];
 }
 
-// Writes the non-zero columns of q i's row through put(col, value) (the
-// caller zeroes the row first) and returns through base the B interpolated
-// eigenvalues in the data's own unit (NaN for a q whose locate failed).
+// Columns of q i's row that do not depend on the mode: position in the node
+// cell (0-2), slot weights (3-10), tetrahedron flag (11), position in the
+// trellis box (12 + 9B + 0..2).  The caller has checked status[i] == 0.
 template <class Put>
-__device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i, Put put, float* base) {
-  if (a.status[i]) {
-    if (base)
-      for (int b = 0; b < a.B; ++b) base[b] = __int_as_float(0x7fc00000);
-    return;
-  }
+__device__ void feature_head(const DevGeom& g, const FeatureArgs& a, long long i, Put put) {
   const long long node = a.node[2 * i];
   const long long nx = g.n_knots[0] - 1, ny = g.n_knots[1] - 1;
   const int sub[3] = {(int)(node % nx), (int)((node / nx) % ny), (int)(node / (nx * ny))};
@@ -114,20 +109,38 @@ __device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i,
   const int nw = min(a.nw[i], 8);
   for (int k = 0; k < nw; ++k) put(3 + k, (float)a.w[8 * i + k]);
   put(11, a.node[2 * i + 1] >= 0 ? 1.f : 0.f);
-  for (int b = 0; b < a.B; ++b) {
-    double s = 0.0;
-    for (int k = 0; k < nw; ++k) {
-      const float ev = vertex_value(a, a.vidx[8 * i + k], b);
-      put(12 + k * a.B + b, ev * a.inv_omega);
-      s = dadd(s, dmul(a.w[8 * i + k], (double)ev));
-    }
-    if (base) base[b] = (float)s;
-    put(12 + 8 * a.B + b, (float)s * a.inv_omega);
-  }
   for (int d = 0; d < 3; ++d) {
     const double lo = g.knots[d][0], hi = g.knots[d][g.n_knots[d] - 1];
     put(12 + 9 * a.B + d, (float)((x[d] - lo) / (hi - lo)));
   }
+}
+
+// Columns of mode b: its vertex eigenvalues (12 + slot·B + b) and its
+// interpolated eigenvalue (12 + 8B + b), which is also returned unscaled.
+template <class Put>
+__device__ float feature_mode(const FeatureArgs& a, long long i, int b, Put put) {
+  const int nw = min(a.nw[i], 8);
+  double s = 0.0;
+  for (int k = 0; k < nw; ++k) {
+    const float ev = vertex_value(a, a.vidx[8 * i + k], b);
+    put(12 + k * a.B + b, ev * a.inv_omega);
+    s = dadd(s, dmul(a.w[8 * i + k], (double)ev));
+  }
+  put(12 + 8 * a.B + b, (float)s * a.inv_omega);
+  return (float)s;
+}
+
+// The whole row through put(col, value) (the caller zeroes the row first),
+// and through base the B interpolated eigenvalues in the data's own unit
+// (NaN for a q whose locate failed).
+template <class Put>
+__device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i, Put put, float* base) {
+  if (a.status[i]) {
+    for (int b = 0; b < a.B; ++b) base[b] = __int_as_float(0x7fc00000);
+    return;
+  }
+  feature_head(g, a, i, put);
+  for (int b = 0; b < a.B; ++b) base[b] = feature_mode(a, i, b, put);
 }
 
 __global__ void mlp_features_kernel(DevGeom g, FeatureArgs a, float* X, float* base) {
@@ -330,8 +343,9 @@ static void mlp_backward(int d_in, int n_out, int rnd, const float* P, float* G,
 // ---------------------------------------------------------------------------
 // inference: features + four dense layers on the tensor cores + residual add
 // ---------------------------------------------------------------------------
-constexpr int kInferRows = 128;     // q per tile
-constexpr int kInferThreads = 256;  // 8 warps × 16 rows
+constexpr int kInferRows = 128;        // q per tile, one tile per warp group at a time
+constexpr int kGroupThreads = 256;     // a warp group: 8 warps × 16 rows
+constexpr int kMaxGroups = 2;          // warp groups per CTA
 
 __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint32_t* b) {
   asm volatile(
@@ -339,6 +353,27 @@ __device__ __forceinline__ void mma_bf16(float* c, const uint32_t* a, const uint
       "{%0,%1,%2,%3};\n"
       : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t* r, uint32_t addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr)
+               : "memory");
+}
+
+__device__ __forceinline__ void ldsm_x2(uint32_t* r, uint32_t addr) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];\n"
+               : "=r"(r[0]), "=r"(r[1])
+               : "r"(addr)
+               : "memory");
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// named barrier of one warp group (id 1 + group; 0 is __syncthreads)
+__device__ __forceinline__ void group_sync(int group) {
+  asm volatile("bar.sync %0, %1;\n" ::"r"(1 + group), "n"(kGroupThreads) : "memory");
 }
 
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
@@ -357,13 +392,16 @@ struct InferArgs {
   int out_f64;
 };
 
-// bf16 elements per shared-memory row: 8 extra spread the rows over the banks
+// bf16 elements per shared-memory row: 8 extra spread the rows over the
+// banks (row strides of 176 or 272 bytes put the 8 rows of an ldmatrix
+// phase on disjoint banks) and keep every row 16-byte aligned
 __host__ __device__ inline int act_stride(int d_in) { return (d_in > kWidth ? d_in : kWidth) + 8; }
 
 // One warp computes its 16 rows × (8·NT) output columns of a layer with
-// K = in: A fragments from the activation tile, B fragments from the
-// layer's weight rows.  Hidden layers write bf16(GELU(acc + b)) back into
-// the warp's own rows of the tile; the output layer writes acc + b to out.
+// K = in: A fragments (ldmatrix.x4) from the activation tile, B fragments
+// (ldmatrix.x4 for two n-tiles, .x2 for one) from the layer's weight rows
+// W[n][k].  Hidden layers write bf16(GELU(acc + b)) back into the warp's own
+// rows of the tile; the output layer writes acc + b to out.
 template <int NT, bool kHidden>
 __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int ws, const float* bl,
                                            __nv_bfloat16* act, int as, int row0, int lane, float* out, int out_ld,
@@ -371,25 +409,31 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
   float acc[NT][4];
 #pragma unroll
   for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-  const int g = lane >> 2, tq = lane & 3;
+  const int mat = lane >> 3, r8 = lane & 7;
+  // A: matrices (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
+  const uint32_t a_addr = smem_u32(act + (size_t)(row0 + r8 + ((mat & 1) << 3)) * as + ((mat >> 1) << 3));
+  // B, two n-tiles: (tile 0, k 0-7), (tile 0, k 8-15), (tile 1, k 0-7), (tile 1, k 8-15)
+  const uint32_t b_addr = NT == 1 ? smem_u32(Wl + (size_t)r8 * ws + ((mat & 1) << 3))
+                                  : smem_u32(Wl + (size_t)(((mat >> 1) << 3) + r8) * ws + ((mat & 1) << 3));
   for (int k0 = 0; k0 < in; k0 += 16) {
     uint32_t a[4];
-    const __nv_bfloat16* r0 = act + (size_t)(row0 + g) * as + k0 + 2 * tq;
-    const __nv_bfloat16* r1 = r0 + (size_t)8 * as;
-    a[0] = *reinterpret_cast<const uint32_t*>(r0);
-    a[1] = *reinterpret_cast<const uint32_t*>(r1);
-    a[2] = *reinterpret_cast<const uint32_t*>(r0 + 8);
-    a[3] = *reinterpret_cast<const uint32_t*>(r1 + 8);
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const __nv_bfloat16* wr = Wl + (size_t)(t * 8 + g) * ws + k0 + 2 * tq;
+    ldsm_x4(a, a_addr + 2 * k0);
+    if (NT == 1) {
       uint32_t b[2];
-      b[0] = *reinterpret_cast<const uint32_t*>(wr);
-      b[1] = *reinterpret_cast<const uint32_t*>(wr + 8);
-      mma_bf16(acc[t], a, b);
+      ldsm_x2(b, b_addr + 2 * k0);
+      mma_bf16(acc[0], a, b);
+    } else {
+#pragma unroll
+      for (int p = 0; p < NT / 2; ++p) {
+        uint32_t b[4];
+        ldsm_x4(b, b_addr + 2 * (p * 16 * ws + k0));
+        mma_bf16(acc[2 * p], a, b);
+        mma_bf16(acc[2 * p + 1], a, b + 2);
+      }
     }
   }
   __syncwarp();
+  const int g = lane >> 2, tq = lane & 3;
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
     const int c0 = t * 8 + 2 * tq;
@@ -416,10 +460,10 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
 struct InferSmem {
   size_t woff[4];
   int wstride[4];
-  size_t bias_off, act_off, out_off, total;
+  size_t bias_off, act_off, act_bytes, out_off, out_bytes, total;
 };
 
-__host__ __device__ inline InferSmem infer_smem(int d_in, int n_out) {
+__host__ __device__ inline InferSmem infer_smem(int d_in, int n_out, int groups) {
   const MlpLayout L = mlp_layout(d_in, n_out);
   InferSmem s;
   size_t o = 0;
@@ -433,25 +477,28 @@ __host__ __device__ inline InferSmem infer_smem(int d_in, int n_out) {
   o += (size_t)(L.out[0] + L.out[1] + L.out[2] + L.out[3]) * 4;
   o = (o + 15) & ~size_t(15);
   s.act_off = o;
-  o += (size_t)kInferRows * act_stride(d_in) * 2;
-  o = (o + 15) & ~size_t(15);
+  s.act_bytes = ((size_t)kInferRows * act_stride(d_in) * 2 + 15) & ~size_t(15);
+  o += s.act_bytes * groups;
   s.out_off = o;
-  o += (size_t)kInferRows * n_out * 4;
+  s.out_bytes = ((size_t)kInferRows * n_out * 4 + 15) & ~size_t(15);
+  o += s.out_bytes * groups;
   s.total = o;
   return s;
 }
 
-__global__ void __launch_bounds__(kInferThreads)
+// One CTA per SM, blockDim = 256 × groups.  The weights are staged once per
+// CTA; each warp group then takes 128-q tiles on its own (own activation and
+// output tiles, own named barrier), so one group's feature gathers overlap
+// the other group's tensor-core layers.
+__global__ void __launch_bounds__(kGroupThreads * kMaxGroups, 1)
 mlp_infer_kernel(DevGeom g, InferArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int d_in = a.f.d_in, n_out = a.n_out, B = a.f.B;
+  const int groups = blockDim.x / kGroupThreads;
   const MlpLayout L = mlp_layout(d_in, n_out);
-  const InferSmem S = infer_smem(d_in, n_out);
+  const InferSmem S = infer_smem(d_in, n_out, groups);
   float* sb = reinterpret_cast<float*>(sm + S.bias_off);
-  __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(sm + S.act_off);
-  float* out_tile = reinterpret_cast<float*>(sm + S.out_off);
   const int as = act_stride(d_in);
-  // weights and biases once per CTA
   {
     long long src = 0;
     int bo = 0;
@@ -464,6 +511,7 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
       bo += L.out[l];
     }
   }
+  __syncthreads();
   const __nv_bfloat16* W0 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[0]);
   const __nv_bfloat16* W1 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[1]);
   const __nv_bfloat16* W2 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[2]);
@@ -471,21 +519,27 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
   const float* b1 = sb + L.out[0];
   const float* b2 = b1 + L.out[1];
   const float* b3 = b2 + L.out[2];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row0 = warp * 16;
+  const int grp = threadIdx.x / kGroupThreads, gt = threadIdx.x % kGroupThreads;
+  const int lane = gt & 31, row0 = (gt >> 5) * 16;
+  __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(sm + S.act_off + S.act_bytes * grp);
+  float* out_tile = reinterpret_cast<float*>(sm + S.out_off + S.out_bytes * grp);
   const int half_in = d_in / 2;
+  const int items = 1 + B;  // per row: the mode-independent columns, then one item per mode
   const long long n_tiles = (a.f.n + kInferRows - 1) / kInferRows;
-  for (long long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
-    __syncthreads();  // weights staged; the previous tile's outputs consumed
-    for (int t = threadIdx.x; t < kInferRows * half_in; t += blockDim.x)
+  for (long long tile = (long long)blockIdx.x * groups + grp; tile < n_tiles; tile += (long long)gridDim.x * groups) {
+    for (int t = gt; t < kInferRows * half_in; t += kGroupThreads)
       reinterpret_cast<uint32_t*>(act + (size_t)(t / half_in) * as)[t % half_in] = 0u;
-    __syncthreads();
-    for (int r = threadIdx.x; r < kInferRows; r += blockDim.x) {
+    group_sync(grp);
+    for (int t = gt; t < kInferRows * items; t += kGroupThreads) {
+      const int r = t / items, j = t % items;
       const long long i = tile * kInferRows + r;
-      if (i >= a.f.n) continue;
+      if (i >= a.f.n || a.f.status[i]) continue;
       __nv_bfloat16* arow = act + (size_t)r * as;
-      feature_row(g, a.f, i, [arow](int k, float v) { arow[k] = __float2bfloat16_rn(v); }, nullptr);
+      auto put = [arow](int k, float v) { arow[k] = __float2bfloat16_rn(v); };
+      if (j == 0) feature_head(g, a.f, i, put);
+      else feature_mode(a.f, i, j - 1, put);
     }
-    __syncthreads();
+    group_sync(grp);
     // each warp owns its 16 rows through all four layers
     warp_layer<16, true>(W0, L.in[0], S.wstride[0], sb, act, as, row0, lane, nullptr, 0, 0);
     warp_layer<16, true>(W1, L.in[1], S.wstride[1], b1, act, as, row0, lane, nullptr, 0, 0);
@@ -493,8 +547,8 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
     for (int c = 0; c < n_out; c += 8)
       warp_layer<1, false>(W3 + (size_t)c * S.wstride[3], L.in[3], S.wstride[3], b3 + c, act, as, row0, lane,
                            out_tile + c, n_out, n_out - c);
-    __syncthreads();
-    for (int t = threadIdx.x; t < kInferRows * B; t += blockDim.x) {
+    group_sync(grp);
+    for (int t = gt; t < kInferRows * B; t += kGroupThreads) {
       const int r = t / B, b = t % B;
       const long long i = tile * kInferRows + r;
       if (i >= a.f.n || a.f.status[i]) continue;
@@ -503,6 +557,7 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
       if (a.out_f64) static_cast<double*>(a.values_out)[i * B + b] += (double)res;
       else static_cast<float*>(a.values_out)[i * B + b] += res;
     }
+    group_sync(grp);  // the tiles are rewritten by the next iteration
   }
 }
 
@@ -548,7 +603,7 @@ brx_status check_model_fits(brx_handle* h, const brx_mlp_dims* d) {
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "the residual model needs one real eigenvalue per mode");
   if (d->d_in < feature_cols(h->vals.B))
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "d_in is too small for the feature row");
-  if (brx::infer_smem(d->d_in, d->n_out).total > h->smem_optin)
+  if (brx::infer_smem(d->d_in, d->n_out, 1).total > h->smem_optin)
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "the residual model does not fit in shared memory");
   return BRX_OK;
 }
@@ -650,8 +705,10 @@ brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const fl
   BRX_CUDA(h, h->mlp_b.ensure(b.size() * sizeof(float)));
   BRX_CUDA(h, cudaMemcpy(h->mlp_w.p, W.data(), W.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
   BRX_CUDA(h, cudaMemcpy(h->mlp_b.p, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice));
-  const size_t smem = brx::infer_smem(d->d_in, d->n_out).total;
+  const int groups = brx::infer_smem(d->d_in, d->n_out, 2).total <= h->smem_optin ? 2 : 1;
+  const size_t smem = brx::infer_smem(d->d_in, d->n_out, groups).total;
   BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  h->mlp_groups = groups;
   h->mlp_dims = *d;
   h->mlp_omega_scale = omega_scale;
   h->mlp_res_scale = res_scale;
@@ -676,10 +733,11 @@ int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_o
   a.clip = h->mlp_clip;
   a.values_out = values_out;
   a.out_f64 = !out_f32;
-  const size_t smem = brx::infer_smem(a.f.d_in, a.n_out).total;
+  const int groups = h->mlp_groups;
+  const size_t smem = brx::infer_smem(a.f.d_in, a.n_out, groups).total;
   const long long tiles = (n + brx::kInferRows - 1) / brx::kInferRows;
-  const long long grid = std::min<long long>(tiles, (long long)h->num_sms);
-  brx::mlp_infer_kernel<<<(unsigned)grid, brx::kInferThreads, smem, cs>>>(h->g, a);
+  const long long grid = std::min<long long>((tiles + groups - 1) / groups, (long long)h->num_sms);
+  brx::mlp_infer_kernel<<<(unsigned)grid, brx::kGroupThreads * groups, smem, cs>>>(h->g, a);
   return 1;
 }
 
