@@ -707,6 +707,7 @@ void brx_destroy(brx_handle* h) {
   h->perms.release();
   h->mlp_w.release();
   h->mlp_b.release();
+  h->mlp_x.release();
   if (h->err) cudaFree(h->err);
   if (h->err_host) cudaFreeHost(h->err_host);
   delete h;

@@ -101,7 +101,7 @@ struct brx_handle {
   brx_mlp_dims mlp_dims{};
   float mlp_omega_scale = 1.f, mlp_res_scale = 1.f, mlp_clip = 0.f;
   int mlp_groups = 1;  // warp groups per CTA of the inference kernel
-  DevBuf mlp_w, mlp_b;
+  DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;

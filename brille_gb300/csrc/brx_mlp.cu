@@ -92,6 +92,10 @@ __device__ __forceinline__ float vertex_value(const FeatureArgs& a, long long v,
                       : static_cast<const float*>(a.values)[v * a.B + b];
 }
 
+// Feature arithmetic is FP32 with explicit rounding (no contraction), so
+// that the oracle repeats it bit for bit; the rows are rounded to bf16 for
+// the network anyway.
+
 // Columns of q i's row that do not depend on the mode: position in the node
 // cell (0-2), slot weights (3-10), tetrahedron flag (11), position in the
 // trellis box (12 + 9B + 0..2).  The caller has checked status[i] == 0.
@@ -100,34 +104,38 @@ __device__ void feature_head(const DevGeom& g, const FeatureArgs& a, long long i
   const long long node = a.node[2 * i];
   const long long nx = g.n_knots[0] - 1, ny = g.n_knots[1] - 1;
   const int sub[3] = {(int)(node % nx), (int)((node / nx) % ny), (int)(node / (nx * ny))};
-  double x[3];
-  hkl_to_xyz(x, g.outer_B, a.q_ir + 3 * i);
+  const float q0 = (float)a.q_ir[3 * i], q1 = (float)a.q_ir[3 * i + 1], q2 = (float)a.q_ir[3 * i + 2];
+  float x[3];
+  for (int d = 0; d < 3; ++d)
+    x[d] = __fadd_rn(__fadd_rn(__fmul_rn((float)g.outer_B[d], q0), __fmul_rn((float)g.outer_B[3 + d], q1)),
+                     __fmul_rn((float)g.outer_B[6 + d], q2));
   for (int d = 0; d < 3; ++d) {
-    const double lo = g.knots[d][sub[d]], hi = g.knots[d][sub[d] + 1];
-    put(d, (float)((x[d] - lo) / (hi - lo)));
+    const float lo = (float)g.knots[d][sub[d]], hi = (float)g.knots[d][sub[d] + 1];
+    put(d, __fdiv_rn(__fsub_rn(x[d], lo), __fsub_rn(hi, lo)));
   }
   const int nw = min(a.nw[i], 8);
   for (int k = 0; k < nw; ++k) put(3 + k, (float)a.w[8 * i + k]);
   put(11, a.node[2 * i + 1] >= 0 ? 1.f : 0.f);
   for (int d = 0; d < 3; ++d) {
-    const double lo = g.knots[d][0], hi = g.knots[d][g.n_knots[d] - 1];
-    put(12 + 9 * a.B + d, (float)((x[d] - lo) / (hi - lo)));
+    const float lo = (float)g.knots[d][0], hi = (float)g.knots[d][g.n_knots[d] - 1];
+    put(12 + 9 * a.B + d, __fdiv_rn(__fsub_rn(x[d], lo), __fsub_rn(hi, lo)));
   }
 }
 
 // Columns of mode b: its vertex eigenvalues (12 + slot·B + b) and its
-// interpolated eigenvalue (12 + 8B + b), which is also returned unscaled.
+// interpolated eigenvalue Σ w·v in slot order (12 + 8B + b), which is also
+// returned unscaled (the FP32 gather's own result for FP32 storage).
 template <class Put>
 __device__ float feature_mode(const FeatureArgs& a, long long i, int b, Put put) {
   const int nw = min(a.nw[i], 8);
-  double s = 0.0;
+  float s = 0.f;
   for (int k = 0; k < nw; ++k) {
     const float ev = vertex_value(a, a.vidx[8 * i + k], b);
-    put(12 + k * a.B + b, ev * a.inv_omega);
-    s = dadd(s, dmul(a.w[8 * i + k], (double)ev));
+    put(12 + k * a.B + b, __fmul_rn(ev, a.inv_omega));
+    s = __fadd_rn(s, __fmul_rn((float)a.w[8 * i + k], ev));
   }
-  put(12 + 8 * a.B + b, (float)s * a.inv_omega);
-  return (float)s;
+  put(12 + 8 * a.B + b, __fmul_rn(s, a.inv_omega));
+  return s;
 }
 
 // The whole row through put(col, value) (the caller zeroes the row first),
@@ -381,37 +389,35 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<uint32_t*>(&v);
 }
 
-struct InferArgs {
-  FeatureArgs f;
-  const __nv_bfloat16* W;  // layers' [out][in] bf16, one after another
-  const float* bias;       // layers' biases (bf16-rounded values), one after another
-  int n_out;
-  float res_scale;         // network outputs are residuals in units of res_scale
-  float clip;              // |residual| above clip is dropped (plain interpolation kept); 0: no clip
-  void* values_out;        // n × B, float or double: += residual
-  int out_f64;
-};
 
-// bf16 elements per shared-memory row: 8 extra spread the rows over the
-// banks (row strides of 176 or 272 bytes put the 8 rows of an ldmatrix
-// phase on disjoint banks) and keep every row 16-byte aligned
-__host__ __device__ inline int act_stride(int d_in) { return (d_in > kWidth ? d_in : kWidth) + 8; }
+// bf16 elements per shared-memory row of the hidden activations and of the
+// staged feature rows: 8 extra spread the rows over the banks (strides of
+// 2·cols + 16 bytes put the 8 rows of an ldmatrix phase on disjoint banks)
+// and keep every row 16-byte aligned
+__host__ __device__ inline int act_stride() { return kWidth + 8; }
+__host__ __device__ inline int stage_stride(int d_in) { return d_in + 8; }
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* gaddr) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr), "l"(gaddr) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // One warp computes its 16 rows × (8·NT) output columns of a layer with
-// K = in: A fragments (ldmatrix.x4) from the activation tile, B fragments
+// K = in: A fragments (ldmatrix.x4) from src (row stride ss), B fragments
 // (ldmatrix.x4 for two n-tiles, .x2 for one) from the layer's weight rows
-// W[n][k].  Hidden layers write bf16(GELU(acc + b)) back into the warp's own
-// rows of the tile; the output layer writes acc + b to out.
+// W[n][k].  Hidden layers write bf16(GELU(acc + b)) to the warp's rows of
+// dst (row stride ds); the output layer writes acc + b to out.
 template <int NT, bool kHidden>
 __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int ws, const float* bl,
-                                           __nv_bfloat16* act, int as, int row0, int lane, float* out, int out_ld,
-                                           int n_valid) {
+                                           const __nv_bfloat16* src, int ss, __nv_bfloat16* dst, int ds, int row0,
+                                           int lane, float* out, int out_ld, int n_valid) {
   float acc[NT][4];
 #pragma unroll
   for (int t = 0; t < NT; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
   const int mat = lane >> 3, r8 = lane & 7;
   // A: matrices (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
-  const uint32_t a_addr = smem_u32(act + (size_t)(row0 + r8 + ((mat & 1) << 3)) * as + ((mat >> 1) << 3));
+  const uint32_t a_addr = smem_u32(src + (size_t)(row0 + r8 + ((mat & 1) << 3)) * ss + ((mat >> 1) << 3));
   // B, two n-tiles: (tile 0, k 0-7), (tile 0, k 8-15), (tile 1, k 0-7), (tile 1, k 8-15)
   const uint32_t b_addr = NT == 1 ? smem_u32(Wl + (size_t)r8 * ws + ((mat & 1) << 3))
                                   : smem_u32(Wl + (size_t)(((mat >> 1) << 3) + r8) * ws + ((mat & 1) << 3));
@@ -439,9 +445,9 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
     const int c0 = t * 8 + 2 * tq;
     if (kHidden) {
       const float b0 = bl[c0], b1 = bl[c0 + 1];
-      *reinterpret_cast<uint32_t*>(act + (size_t)(row0 + g) * as + c0) =
+      *reinterpret_cast<uint32_t*>(dst + (size_t)(row0 + g) * ds + c0) =
           pack_bf16(gelu(acc[t][0] + b0), gelu(acc[t][1] + b1));
-      *reinterpret_cast<uint32_t*>(act + (size_t)(row0 + g + 8) * as + c0) =
+      *reinterpret_cast<uint32_t*>(dst + (size_t)(row0 + g + 8) * ds + c0) =
           pack_bf16(gelu(acc[t][2] + b0), gelu(acc[t][3] + b1));
     } else {
       if (c0 < n_valid) {
@@ -457,12 +463,59 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
   __syncwarp();
 }
 
+// bf16 feature rows X (n × d_in, contiguous) of one sub-chunk: each thread
+// builds one row in shared memory, then the block writes its 128 rows as
+// 16-byte stores.
+constexpr int kRowsPerBlock = 128;
+
+__global__ void __launch_bounds__(kRowsPerBlock) mlp_xrows_kernel(DevGeom g, FeatureArgs a, __nv_bfloat16* X) {
+  extern __shared__ __align__(16) unsigned char xs[];
+  const int d_in = a.d_in, ss = stage_stride(d_in);
+  __nv_bfloat16* rows = reinterpret_cast<__nv_bfloat16*>(xs);
+  for (long long r0 = (long long)blockIdx.x * kRowsPerBlock; r0 < a.n; r0 += (long long)gridDim.x * kRowsPerBlock) {
+    __nv_bfloat16* row = rows + (size_t)threadIdx.x * ss;
+    for (int k = 0; k < d_in / 2; ++k) reinterpret_cast<uint32_t*>(row)[k] = 0u;
+    const long long i = r0 + threadIdx.x;
+    if (i < a.n && !a.status[i]) {
+      auto put = [row](int k, float v) { row[k] = __float2bfloat16_rn(v); };
+      feature_head(g, a, i, put);
+      for (int b = 0; b < a.B; ++b) feature_mode(a, i, b, put);
+    }
+    __syncthreads();
+    const int rows_here = (int)(a.n - r0 < kRowsPerBlock ? a.n - r0 : kRowsPerBlock);
+    const int chunks = d_in / 8;  // 16-byte pieces per row
+    for (int t = threadIdx.x; t < rows_here * chunks; t += kRowsPerBlock) {
+      const int r = t / chunks, c = t % chunks;
+      reinterpret_cast<uint4*>(X + (size_t)(r0 + r) * d_in)[c] = reinterpret_cast<const uint4*>(rows + (size_t)r * ss)[c];
+    }
+    __syncthreads();
+  }
+}
+
+size_t xrows_smem(int d_in) { return (size_t)kRowsPerBlock * stage_stride(d_in) * 2; }
+
+struct InferArgs {
+  const __nv_bfloat16* X;  // n × d_in feature rows
+  const int32_t* status;   // n
+  long long n;
+  int d_in, B;
+  const __nv_bfloat16* W;  // layers' [out][in] bf16, one after another
+  const float* bias;       // layers' biases (bf16-rounded values), one after another
+  int n_out;
+  float res_scale;         // network outputs are residuals in units of res_scale
+  float clip;              // |residual| above clip is dropped (plain interpolation kept); 0: no clip
+  void* values_out;        // n × B, float or double: += residual
+  int out_f64;
+};
+
 struct InferSmem {
   size_t woff[4];
   int wstride[4];
-  size_t bias_off, act_off, act_bytes, out_off, out_bytes, total;
+  size_t bias_off, grp_off, grp_bytes, stage_off, act_off, out_off, total;
 };
 
+// weights and biases once per CTA, then per warp group: a staged tile of
+// feature rows, the hidden activations and the output tile
 __host__ __device__ inline InferSmem infer_smem(int d_in, int n_out, int groups) {
   const MlpLayout L = mlp_layout(d_in, n_out);
   InferSmem s;
@@ -476,29 +529,28 @@ __host__ __device__ inline InferSmem infer_smem(int d_in, int n_out, int groups)
   s.bias_off = o;
   o += (size_t)(L.out[0] + L.out[1] + L.out[2] + L.out[3]) * 4;
   o = (o + 15) & ~size_t(15);
-  s.act_off = o;
-  s.act_bytes = ((size_t)kInferRows * act_stride(d_in) * 2 + 15) & ~size_t(15);
-  o += s.act_bytes * groups;
-  s.out_off = o;
-  s.out_bytes = ((size_t)kInferRows * n_out * 4 + 15) & ~size_t(15);
-  o += s.out_bytes * groups;
+  s.grp_off = o;
+  s.stage_off = 0;
+  s.act_off = ((size_t)kInferRows * stage_stride(d_in) * 2 + 15) & ~size_t(15);
+  s.out_off = s.act_off + (((size_t)kInferRows * act_stride() * 2 + 15) & ~size_t(15));
+  s.grp_bytes = s.out_off + (((size_t)kInferRows * n_out * 4 + 15) & ~size_t(15));
+  o += s.grp_bytes * groups;
   s.total = o;
   return s;
 }
 
-// One CTA per SM, blockDim = 256 × groups.  The weights are staged once per
-// CTA; each warp group then takes 128-q tiles on its own (own activation and
-// output tiles, own named barrier), so one group's feature gathers overlap
-// the other group's tensor-core layers.
+// One CTA per SM, blockDim = 256 × groups.  Each warp group streams 128-row
+// tiles of X: layer 0 reads the staged tile, after which the group's
+// cp.async prefetch of its next tile overlaps layers 1-3 and the residual
+// add; the other group interleaves on the same SM.
 __global__ void __launch_bounds__(kGroupThreads * kMaxGroups, 1)
-mlp_infer_kernel(DevGeom g, InferArgs a) {
+mlp_infer_kernel(InferArgs a) {
   extern __shared__ __align__(16) unsigned char sm[];
-  const int d_in = a.f.d_in, n_out = a.n_out, B = a.f.B;
+  const int d_in = a.d_in, n_out = a.n_out, B = a.B;
   const int groups = blockDim.x / kGroupThreads;
   const MlpLayout L = mlp_layout(d_in, n_out);
   const InferSmem S = infer_smem(d_in, n_out, groups);
   float* sb = reinterpret_cast<float*>(sm + S.bias_off);
-  const int as = act_stride(d_in);
   {
     long long src = 0;
     int bo = 0;
@@ -511,7 +563,6 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
       bo += L.out[l];
     }
   }
-  __syncthreads();
   const __nv_bfloat16* W0 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[0]);
   const __nv_bfloat16* W1 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[1]);
   const __nv_bfloat16* W2 = reinterpret_cast<const __nv_bfloat16*>(sm + S.woff[2]);
@@ -521,44 +572,51 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
   const float* b3 = b2 + L.out[2];
   const int grp = threadIdx.x / kGroupThreads, gt = threadIdx.x % kGroupThreads;
   const int lane = gt & 31, row0 = (gt >> 5) * 16;
-  __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(sm + S.act_off + S.act_bytes * grp);
-  float* out_tile = reinterpret_cast<float*>(sm + S.out_off + S.out_bytes * grp);
-  const int half_in = d_in / 2;
-  const int items = 1 + B;  // per row: the mode-independent columns, then one item per mode
-  const long long n_tiles = (a.f.n + kInferRows - 1) / kInferRows;
-  for (long long tile = (long long)blockIdx.x * groups + grp; tile < n_tiles; tile += (long long)gridDim.x * groups) {
-    for (int t = gt; t < kInferRows * half_in; t += kGroupThreads)
-      reinterpret_cast<uint32_t*>(act + (size_t)(t / half_in) * as)[t % half_in] = 0u;
-    group_sync(grp);
-    for (int t = gt; t < kInferRows * items; t += kGroupThreads) {
-      const int r = t / items, j = t % items;
+  unsigned char* gbase = sm + S.grp_off + S.grp_bytes * grp;
+  __nv_bfloat16* stage = reinterpret_cast<__nv_bfloat16*>(gbase + S.stage_off);
+  __nv_bfloat16* act = reinterpret_cast<__nv_bfloat16*>(gbase + S.act_off);
+  float* out_tile = reinterpret_cast<float*>(gbase + S.out_off);
+  const int ss = stage_stride(d_in), as = act_stride(), chunks = d_in / 8;
+  const long long n_tiles = (a.n + kInferRows - 1) / kInferRows;
+  const long long step = (long long)gridDim.x * groups;
+  // rows past n are zero-filled with plain stores, the rest copied by cp.async
+  auto stage_tile = [&](long long tile) {
+    for (int t = gt; t < kInferRows * chunks; t += kGroupThreads) {
+      const int r = t / chunks, c = t % chunks;
       const long long i = tile * kInferRows + r;
-      if (i >= a.f.n || a.f.status[i]) continue;
-      __nv_bfloat16* arow = act + (size_t)r * as;
-      auto put = [arow](int k, float v) { arow[k] = __float2bfloat16_rn(v); };
-      if (j == 0) feature_head(g, a.f, i, put);
-      else feature_mode(a.f, i, j - 1, put);
+      __nv_bfloat16* d = stage + (size_t)r * ss + 8 * c;
+      if (i < a.n) cp_async16(smem_u32(d), a.X + (size_t)i * d_in + 8 * c);
+      else *reinterpret_cast<uint4*>(d) = make_uint4(0u, 0u, 0u, 0u);
     }
-    group_sync(grp);
-    // each warp owns its 16 rows through all four layers
-    warp_layer<16, true>(W0, L.in[0], S.wstride[0], sb, act, as, row0, lane, nullptr, 0, 0);
-    warp_layer<16, true>(W1, L.in[1], S.wstride[1], b1, act, as, row0, lane, nullptr, 0, 0);
-    warp_layer<16, true>(W2, L.in[2], S.wstride[2], b2, act, as, row0, lane, nullptr, 0, 0);
+    cp_async_commit();
+  };
+  long long tile = (long long)blockIdx.x * groups + grp;
+  if (tile < n_tiles) stage_tile(tile);
+  __syncthreads();  // weights and biases staged
+  for (; tile < n_tiles; tile += step) {
+    cp_async_wait_all();
+    group_sync(grp);  // the whole staged tile is visible
+    warp_layer<16, true>(W0, L.in[0], S.wstride[0], sb, stage, ss, act, as, row0, lane, nullptr, 0, 0);
+    group_sync(grp);  // every warp is done with the staged tile
+    if (tile + step < n_tiles) stage_tile(tile + step);
+    warp_layer<16, true>(W1, L.in[1], S.wstride[1], b1, act, as, act, as, row0, lane, nullptr, 0, 0);
+    warp_layer<16, true>(W2, L.in[2], S.wstride[2], b2, act, as, act, as, row0, lane, nullptr, 0, 0);
     for (int c = 0; c < n_out; c += 8)
-      warp_layer<1, false>(W3 + (size_t)c * S.wstride[3], L.in[3], S.wstride[3], b3 + c, act, as, row0, lane,
-                           out_tile + c, n_out, n_out - c);
-    group_sync(grp);
-    for (int t = gt; t < kInferRows * B; t += kGroupThreads) {
-      const int r = t / B, b = t % B;
+      warp_layer<1, false>(W3 + (size_t)c * S.wstride[3], L.in[3], S.wstride[3], b3 + c, act, as, nullptr, 0, row0,
+                           lane, out_tile + c, n_out, n_out - c);
+    // each warp adds the residuals of its own 16 rows
+    for (int t = lane; t < 16 * B; t += 32) {
+      const int r = row0 + t / B, b = t % B;
       const long long i = tile * kInferRows + r;
-      if (i >= a.f.n || a.f.status[i]) continue;
+      if (i >= a.n || a.status[i]) continue;
       const float res = out_tile[r * n_out + b] * a.res_scale;
       if (a.clip > 0.f && !(fabsf(res) <= a.clip)) continue;
       if (a.out_f64) static_cast<double*>(a.values_out)[i * B + b] += (double)res;
       else static_cast<float*>(a.values_out)[i * B + b] += res;
     }
-    group_sync(grp);  // the tiles are rewritten by the next iteration
+    __syncwarp();
   }
+  cp_async_wait_all();
 }
 
 }  // namespace brx
@@ -569,6 +627,10 @@ mlp_infer_kernel(DevGeom g, InferArgs a) {
 using namespace brx_detail;
 
 namespace {
+
+// q per sub-chunk of the residual: 2^19 feature rows of ≤ 160 bytes stay in
+// the 129 MB L2 between the feature and network kernels
+constexpr long long kResidualSub = 1LL << 19;
 
 bool mlp_dims_ok(const brx_mlp_dims* d) {
   return d && d->d_in >= 16 && d->d_in % 16 == 0 && d->d_in <= 512 && d->n_out >= 8 && d->n_out % 8 == 0 &&
@@ -708,6 +770,9 @@ brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const fl
   const int groups = brx::infer_smem(d->d_in, d->n_out, 2).total <= h->smem_optin ? 2 : 1;
   const size_t smem = brx::infer_smem(d->d_in, d->n_out, groups).total;
   BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_xrows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)brx::xrows_smem(d->d_in)));
+  BRX_CUDA(h, h->mlp_x.ensure((size_t)kResidualSub * d->d_in * sizeof(__nv_bfloat16)));
   h->mlp_groups = groups;
   h->mlp_dims = *d;
   h->mlp_omega_scale = omega_scale;
@@ -723,22 +788,39 @@ namespace brx_detail {
 
 int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_out, bool out_f32, cudaStream_t cs) {
   if (!h->mlp_on || n <= 0) return 0;
-  brx::InferArgs a{};
-  a.f = feature_args(h, s.r.q_ir, s.r.node, s.r.nw, s.r.vidx, s.r.w, s.r.status, n, h->mlp_dims.d_in,
-                     h->mlp_omega_scale);
-  a.W = static_cast<const __nv_bfloat16*>(h->mlp_w.p);
-  a.bias = static_cast<const float*>(h->mlp_b.p);
-  a.n_out = h->mlp_dims.n_out;
-  a.res_scale = h->mlp_res_scale;
-  a.clip = h->mlp_clip;
-  a.values_out = values_out;
-  a.out_f64 = !out_f32;
-  const int groups = h->mlp_groups;
-  const size_t smem = brx::infer_smem(a.f.d_in, a.n_out, groups).total;
-  const long long tiles = (n + brx::kInferRows - 1) / brx::kInferRows;
-  const long long grid = std::min<long long>((tiles + groups - 1) / groups, (long long)h->num_sms);
-  brx::mlp_infer_kernel<<<(unsigned)grid, brx::kGroupThreads * groups, smem, cs>>>(h->g, a);
-  return 1;
+  const int d_in = h->mlp_dims.d_in, B = h->vals.B, groups = h->mlp_groups;
+  const size_t smem = brx::infer_smem(d_in, h->mlp_dims.n_out, groups).total;
+  const size_t out_row = (size_t)B * (out_f32 ? 4 : 8);
+  __nv_bfloat16* X = static_cast<__nv_bfloat16*>(h->mlp_x.p);
+  int launches = 0;
+  // sub-chunks whose feature rows stay in L2 between the two kernels
+  for (long long off = 0; off < n; off += kResidualSub) {
+    const long long m = std::min<long long>(kResidualSub, n - off);
+    const brx::FeatureArgs f = feature_args(h, s.r.q_ir + 3 * off, s.r.node + 2 * off, s.r.nw + off,
+                                            s.r.vidx + 8 * off, s.r.w + 8 * off, s.r.status + off, m, d_in,
+                                            h->mlp_omega_scale);
+    const long long blocks = std::min<long long>((m + brx::kRowsPerBlock - 1) / brx::kRowsPerBlock,
+                                                 (long long)h->num_sms * 8);
+    brx::mlp_xrows_kernel<<<(unsigned)blocks, brx::kRowsPerBlock, brx::xrows_smem(d_in), cs>>>(h->g, f, X);
+    brx::InferArgs a{};
+    a.X = X;
+    a.status = s.r.status + off;
+    a.n = m;
+    a.d_in = d_in;
+    a.B = B;
+    a.W = static_cast<const __nv_bfloat16*>(h->mlp_w.p);
+    a.bias = static_cast<const float*>(h->mlp_b.p);
+    a.n_out = h->mlp_dims.n_out;
+    a.res_scale = h->mlp_res_scale;
+    a.clip = h->mlp_clip;
+    a.values_out = static_cast<char*>(values_out) + out_row * (size_t)off;
+    a.out_f64 = !out_f32;
+    const long long tiles = (m + brx::kInferRows - 1) / brx::kInferRows;
+    const long long grid = std::min<long long>((tiles + groups - 1) / groups, (long long)h->num_sms);
+    brx::mlp_infer_kernel<<<(unsigned)grid, brx::kGroupThreads * groups, smem, cs>>>(a);
+    launches += 2;
+  }
+  return launches;
 }
 
 }  // namespace brx_detail

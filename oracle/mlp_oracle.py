@@ -146,45 +146,41 @@ def features(records, values, knots, outer_B, n_modes, d_in, omega_scale):
     """Feature rows (n × d_in float32) and plain interpolated eigenvalues
     (n × n_modes float32, NaN where the locate failed) from locate records
     (dict of q_ir, node, n_weights, vertex, weight, status), vertex
-    eigenvalues (n_vertices × n_modes) and the trellis knots."""
-    q = np.asarray(records["q_ir"], np.float64)
+    eigenvalues (n_vertices × n_modes) and the trellis knots.  Every step is
+    one IEEE float32 operation in the device code's order."""
+    f32 = np.float32
+    q = np.asarray(records["q_ir"], np.float64).astype(f32)
     n = q.shape[0]
     B = n_modes
-    X = np.zeros((n, d_in), np.float32)
-    base = np.full((n, B), np.nan, np.float32)
+    X = np.zeros((n, d_in), f32)
+    base = np.full((n, B), np.nan, f32)
     ok = np.asarray(records["status"]) == 0
-    vals32 = np.asarray(values).reshape(-1, B).astype(np.float32)
-    inv = np.float32(1.0) / np.float32(omega_scale)
-    Bm = np.asarray(outer_B, np.float64).reshape(3, 3)
-    # xyz_i = ((0 + B0i h0) + B1i h1) + B2i h2, unfused like the device code
-    x = np.zeros((n, 3))
-    for i in range(3):
-        s = np.zeros(n)
-        for k in range(3):
-            s = s + Bm[k, i] * q[:, k]
-        x[:, i] = s
+    vals32 = np.asarray(values).reshape(-1, B).astype(f32)
+    inv = f32(1.0) / f32(omega_scale)
+    Bm = np.asarray(outer_B, np.float64).reshape(3, 3).astype(f32)
+    # x_d = (B0d q0 + B1d q1) + B2d q2
+    x = np.stack([(Bm[0, d] * q[:, 0] + Bm[1, d] * q[:, 1]) + Bm[2, d] * q[:, 2] for d in range(3)], axis=1)
     node = np.asarray(records["node"]).reshape(n, 2)
     nx = len(knots[0]) - 1
     ny = len(knots[1]) - 1
     sub = np.stack([node[:, 0] % nx, (node[:, 0] // nx) % ny, node[:, 0] // (nx * ny)], axis=1)
     nw = np.minimum(np.asarray(records["n_weights"]), 8)
     vid = np.asarray(records["vertex"]).reshape(n, 8)
-    w = np.asarray(records["weight"]).reshape(n, 8)
+    w = np.asarray(records["weight"]).reshape(n, 8).astype(f32)
+    kn = [np.asarray(k, np.float64).astype(f32) for k in knots]
     for i in np.nonzero(ok)[0]:
         for d in range(3):
-            lo, hi = knots[d][sub[i, d]], knots[d][sub[i, d] + 1]
-            X[i, d] = np.float32((x[i, d] - lo) / (hi - lo))
-        X[i, 3:3 + nw[i]] = w[i, :nw[i]].astype(np.float32)
+            lo, hi = kn[d][sub[i, d]], kn[d][sub[i, d] + 1]
+            X[i, d] = (x[i, d] - lo) / (hi - lo)
+            X[i, 12 + 9 * B + d] = (x[i, d] - kn[d][0]) / (kn[d][-1] - kn[d][0])
+        X[i, 3:3 + nw[i]] = w[i, :nw[i]]
         X[i, 11] = 1.0 if node[i, 1] >= 0 else 0.0
         for b in range(B):
-            s = 0.0
+            s = f32(0.0)
             for k in range(nw[i]):
                 ev = vals32[vid[i, k], b]
                 X[i, 12 + k * B + b] = ev * inv
-                s = s + float(w[i, k]) * float(ev)
-            base[i, b] = np.float32(s)
-            X[i, 12 + 8 * B + b] = np.float32(s) * inv
-        for d in range(3):
-            lo, hi = knots[d][0], knots[d][-1]
-            X[i, 12 + 9 * B + d] = np.float32((x[i, d] - lo) / (hi - lo))
+                s = f32(s + w[i, k] * ev)
+            base[i, b] = s
+            X[i, 12 + 8 * B + b] = s * inv
     return X, base
