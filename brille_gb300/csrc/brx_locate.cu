@@ -32,6 +32,8 @@ struct SmemZone {
   float* plane;     // n_faces × 4
   float* band;      // n_faces
   float* wm;        // (n_ops + 1) × n_wedge × 3
+  float* n32;       // n_faces × 3: face normals rounded to FP32
+  float* tl32;      // n_faces: |τ| rounded to FP32
   double* abc;      // n_faces × 9
   double* normal;   // n_faces × 3
   double* tau_len;  // n_faces
@@ -75,6 +77,50 @@ __device__ bool inside_all_faces(const DevGeom& g, const SmemZone& z, const doub
   return inside_all_faces_exact(g, z, x);
 }
 
+// One step of part_moveinto_prim's shift choice (src/bz_move.cpp:28-46) in
+// FP32: n_j = round(n̂_j·x / |τ_j|) for every face, and the face of largest
+// positive n_j, ties going to a later face only when it does not undo the
+// last shift and lies further out.  Returns false, leaving the choice to the
+// exact loop, whenever a quotient lies within its error bound of a rounding
+// boundary or two candidate distances are too close to order; otherwise the
+// choice is the FP64 one.  With unit normals |n̂·x|'s FP32 error is below
+// 3e-7·|x|₁, so the 3e-6 margin of screen_margin covers it tenfold.
+__device__ bool shift_screen(const DevGeom& g, const SmemZone& z, const double x[3], const int32_t last[3],
+                             int* max_nm_out, int* max_at_out, int* any_pos_out) {
+  const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
+  const float ed = screen_margin(fabsf(x0) + fabsf(x1) + fabsf(x2), 0.f);
+  int max_nm = 0, max_at = 0, any_pos = 0;
+  float dmax = 0.f;
+  for (int j = 0; j < g.n_faces; ++j) {
+    const float* n = z.n32 + 3 * j;
+    const float d = n[0] * x0 + n[1] * x1 + n[2] * x2;
+    const float tl = z.tl32[j];
+    const float r = d / tl;
+    const float mr = ed / tl + 1e-6f * fabsf(r) + 1e-30f;
+    if (fabsf((r - floorf(r)) - 0.5f) <= mr) return false;
+    const int nj = (int)roundf(r);
+    if (nj > 0) any_pos = 1;
+    const int32_t* tj = z.tau + 3 * j;
+    const bool back = (tj[0] + last[0]) != 0 || (tj[1] + last[1]) != 0 || (tj[2] + last[2]) != 0;
+    if (nj > 0 && nj >= max_nm) {
+      bool take = max_nm == 0;
+      if (!take && back) {
+        if (fabsf(d - dmax) <= 2.f * ed) return false;
+        take = d > dmax;
+      }
+      if (take) {
+        max_at = j;
+        max_nm = nj;
+        dmax = d;
+      }
+    }
+  }
+  *max_nm_out = max_nm;
+  *max_at_out = max_at;
+  *any_pos_out = any_pos;
+  return true;
+}
+
 // Returns 0 or BRX_ERR_MOVE_FAILED; q_out in conventional r.l.u.
 __device__ int moveinto_one(const DevGeom& g, const SmemZone& z, const double Q[3], double q_out[3],
                             int32_t tau_out[3]) {
@@ -99,7 +145,8 @@ __device__ int moveinto_one(const DevGeom& g, const SmemZone& z, const double Q[
     if (inside_all_faces(g, z, x)) break;
     int max_nm = 0, max_at = 0, any_pos = 0;
     double dmax = 0.0;
-    for (int j = 0; j < g.n_faces; ++j) {
+    const bool screened = g.screen && shift_screen(g, z, x, last, &max_nm, &max_at, &any_pos);
+    for (int j = 0; !screened && j < g.n_faces; ++j) {
       double dj = dot3(x, z.normal + 3 * j);
       int nj = (int)round(__ddiv_rn(dj, z.tau_len[j]));
       if (nj > 0) any_pos = 1;
@@ -425,6 +472,8 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
   z.plane = fp; fp += 4 * g.n_faces;
   z.band = fp; fp += g.n_faces;
   z.wm = fp; fp += 3 * g.n_wedge * (g.n_ops + 1);
+  z.n32 = fp; fp += 3 * g.n_faces;
+  z.tl32 = fp; fp += g.n_faces;
   p = reinterpret_cast<double*>(((uintptr_t)fp + 15) & ~uintptr_t(15));
   z.abc = p; p += 9 * g.n_faces;
   z.normal = p; p += 3 * g.n_faces;
@@ -447,6 +496,8 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
     for (int i = threadIdx.x; i < 4 * g.n_faces; i += blockDim.x) z.plane[i] = g.face_plane32[i];
     for (int i = threadIdx.x; i < g.n_faces; i += blockDim.x) z.band[i] = g.face_band32[i];
     for (int i = threadIdx.x; i < 3 * g.n_wedge * (g.n_ops + 1); i += blockDim.x) z.wm[i] = g.wedge_m32[i];
+    for (int i = threadIdx.x; i < 3 * g.n_faces; i += blockDim.x) z.n32[i] = (float)g.face_normal[i];
+    for (int i = threadIdx.x; i < g.n_faces; i += blockDim.x) z.tl32[i] = (float)g.face_tau_len[i];
   }
   __syncthreads();
 
@@ -514,7 +565,7 @@ cudaError_t preload_locate_kernel() {
 }
 
 size_t locate_smem_bytes(const DevGeom& g) {
-  return sizeof(float) * (5 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge * (g.n_ops + 1)) + 16 +
+  return sizeof(float) * (9 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge * (g.n_ops + 1)) + 16 +
          sizeof(double) * (13 * (size_t)g.n_faces + 3 * (size_t)g.n_wedge) +
          sizeof(int32_t) * (3 * (size_t)g.n_faces + 10 * (size_t)g.n_ops) + 16;
 }
