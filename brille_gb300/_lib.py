@@ -76,6 +76,27 @@ def load(build_if_missing=True):
     lib.brx_mlp_forward.restype = C.c_int
     lib.brx_set_residual_model.argtypes = [h, md, vp, C.c_float, C.c_float, C.c_float]
     lib.brx_set_residual_model.restype = C.c_int
+    bp = C.c_void_p
+    lib.brx_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int64), C.c_int32, C.c_uint32,
+                                     C.POINTER(C.c_void_p)]
+    lib.brx_batch_create.restype = C.c_int
+    lib.brx_batch_destroy.argtypes = [bp]
+    lib.brx_batch_destroy.restype = None
+    lib.brx_batch_set_io.argtypes = [bp, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    lib.brx_batch_set_io.restype = C.c_int
+    for name in ("brx_batch_run", "brx_batch_capture", "brx_batch_launch"):
+        getattr(lib, name).argtypes = [bp, C.c_void_p]
+        getattr(lib, name).restype = C.c_int
+    lib.brx_batch_sync.argtypes = [bp, C.c_void_p, C.POINTER(C.c_int32)]
+    lib.brx_batch_sync.restype = C.c_int
+    lib.brx_batch_tune.argtypes = [bp, C.c_void_p, C.c_int32]
+    lib.brx_batch_tune.restype = C.c_int
+    lib.brx_batch_config.argtypes = [bp, C.POINTER(C.c_int32), C.c_int32]
+    lib.brx_batch_config.restype = C.c_int
+    lib.brx_batch_launch_count.argtypes = [bp]
+    lib.brx_batch_launch_count.restype = C.c_int64
+    lib.brx_batch_last_error.argtypes = [bp]
+    lib.brx_batch_last_error.restype = C.c_char_p
     lib.brx_abi_version.argtypes = []
     lib.brx_abi_version.restype = C.c_int32
     _lib = lib

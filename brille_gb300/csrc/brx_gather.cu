@@ -157,8 +157,10 @@ struct GroupLayout {
   size_t q, rot, ident, w, R, ph, M, de, e, Y, total;
 };
 
-template <typename Acc, typename St, bool CPLX>
-__host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int na) {
+// e_modes: antiphase entries per slot; ybuf: elements of one of the two
+// staging buffers of vertex rows
+template <typename Acc, typename St>
+__host__ __device__ inline GroupLayout group_layout_dims(int QM, int e_modes, int na, long long ybuf) {
   GroupLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -174,10 +176,15 @@ __host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int n
   L.ph = take(sizeof(Acc) * 2 * (size_t)na * QM);
   L.M = take(sizeof(Acc) * 12 * QM);
   L.de = take(sizeof(int) * (size_t)(na > 0 ? na : 1) * QM);
-  L.e = take(sizeof(Acc) * 2 * 8 * (size_t)MB);
-  L.Y = take(sizeof(St) * 2 * 8 * (size_t)MB * row_stride<St, CPLX>(s));
+  L.e = take(sizeof(Acc) * 2 * 8 * (size_t)e_modes);
+  L.Y = take(sizeof(St) * 2 * (size_t)ybuf);
   L.total = (o + 15) & ~size_t(15);
   return L;
+}
+
+template <typename Acc, typename St, bool CPLX>
+__host__ __device__ inline GroupLayout group_layout(int QM, int MB, int s, int na) {
+  return group_layout_dims<Acc, St>(QM, MB, na, 8LL * MB * row_stride<St, CPLX>(s));
 }
 
 // Store ne (1 or 3) interpolated elements; complex values as 2-wide vectors.
@@ -333,24 +340,47 @@ struct GroupInfo {
   int pid[8];
 };
 
-// Warp 0 takes the next work descriptor and decodes its vertex slots.
-__device__ __forceinline__ void fetch_group(const GatherParams& p, int n_groups, GroupInfo* gi, int lane) {
+// Warp 0 takes the next work descriptor and decodes its vertex slots.  In a
+// batch (gb.items set) it also finds the descriptor's interpolator and
+// copies that item's parameters into *slot.
+__device__ __forceinline__ void fetch_group(const GatherBatch& gb, int n_groups, GatherParams* slot, GroupInfo* gi,
+                                            int lane) {
   int g = 0;
-  if (lane == 0) g = atomicAdd(p.counter, 1);
+  if (lane == 0) g = atomicAdd(gb.counter, 1);
   g = __shfl_sync(0xffffffffu, g, 0);
   if (g >= n_groups) {
     if (lane == 0) gi->count = -1;
     return;
   }
-  const GroupDesc d = p.groups[g];
+  const GroupDesc d = gb.groups[g];
+  int key = d.key;
+  if (gb.items) {
+    int item = 0;
+    if (lane == 0) {
+      int lo = 0, hi = gb.n_items - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(gb.key_off + mid) <= key) lo = mid;
+        else hi = mid - 1;
+      }
+      item = lo;
+    }
+    item = __shfl_sync(0xffffffffu, item, 0);
+    const int* src = reinterpret_cast<const int*>(gb.items + item);
+    int* dst = reinterpret_cast<int*>(slot);
+    for (int w = lane; w < (int)(sizeof(GatherParams) / sizeof(int)); w += 32) dst[w] = __ldg(src + w);
+    __syncwarp();
+    key -= slot->key_base;
+  }
+  const GatherParams& p = *slot;
   int nslot, pivot, vid = 0;
-  if (d.key < 8 * p.n_cube) {
-    pivot = d.key & 7;
+  if (key < 8 * p.n_cube) {
+    pivot = key & 7;
     nslot = 8;
-    if (lane < 8) vid = __ldg(p.cube_vertices + 8 * (long long)(d.key >> 3) + 7 - lane);
+    if (lane < 8) vid = __ldg(p.cube_vertices + 8 * (long long)(key >> 3) + 7 - lane);
   } else {
-    const long long t = (d.key - 8LL * p.n_cube) >> 2;
-    pivot = (int)((d.key - 8LL * p.n_cube) & 3);
+    const long long t = (key - 8LL * p.n_cube) >> 2;
+    pivot = (int)((key - 8LL * p.n_cube) & 3);
     nslot = 4;
     if (lane < 4) vid = __ldg(p.tet_vertices + 4 * t + lane);
   }
@@ -360,7 +390,7 @@ __device__ __forceinline__ void fetch_group(const GatherParams& p, int n_groups,
     gi->pid[lane] = lane < nslot ? perm_lookup(p, pv, vid) : -1;
   }
   if (lane == 0) {
-    gi->key = d.key;
+    gi->key = key;
     gi->start = d.start;
     gi->count = d.count;
     gi->nslot = nslot;
@@ -395,8 +425,8 @@ template <int NS, typename Acc, typename St, bool CPLX, typename Out>
 __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* s_Y, int rs, const Acc* s_e,
                                                const Acc* s_w, const Acc* s_R, const int* s_id, const Acc* s_M,
                                                const int* s_rotf, const Acc* s_ph, const int* s_de,
-                                               const long long* s_q, int count, int pivot, int MB, int b0, int mb,
-                                               int G, int na, Out* out) {
+                                               const long long* s_q, long long qb, int count, int pivot, int MB,
+                                               int b0, int mb, int G, int na, Out* out) {
   constexpr int comps = CPLX ? 2 : 1;
   const int B = p.B, s = p.s;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -416,7 +446,7 @@ __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* 
     if (ne == 9) {
       for (int j = qs; j < count; j += qsplit)
         matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w + 8 * j, s_R + 18 * j, s_id[j], false, pivot, NS, MB,
-                                        b, e0, out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps);
+                                        b, e0, out + ((size_t)(s_q[j] - qb) * B + bb) * (size_t)s * comps);
       continue;
     }
     Acc yr[NS][3], yi[NS][3];
@@ -454,7 +484,7 @@ __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* 
           if (CPLX) vi[k] += wv[x] * yi[x][k];
         }
       }
-      Out* dst = out + (size_t)s_q[j] * B * s * comps + row_off;
+      Out* dst = out + (size_t)(s_q[j] - qb) * B * s * comps + row_off;
       int de = e0;
       if (ne == 3 && s_rotf[j]) {
         const float4 m0 = *reinterpret_cast<const float4*>(s_M + 12 * j);
@@ -485,9 +515,12 @@ __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* 
   }
 }
 
+// Persistent gather over work descriptors.  With single set, every group
+// belongs to that interpolator; otherwise gb.items describes a batch and
+// each group's item parameters are fetched with it.  The parameters of the
+// current and of the next group live in s_p[cur] and s_p[cur ^ 1].
 template <typename Acc, typename St, bool CPLX, typename Out>
-__global__ void __launch_bounds__(kGatherThreads)
-group_gather_kernel(GatherParams p) {
+__device__ __forceinline__ void gather_groups(const GatherParams* single, const GatherBatch& gb) {
   using A = Ar<Acc>;
   // FP32 arithmetic: rows held in registers across the q of a group.
   // FP64: the reference's operation order, rows read from shared memory.
@@ -495,11 +528,9 @@ group_gather_kernel(GatherParams p) {
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ GroupInfo s_g[2];
-  const int B = p.B, s = p.s, MB = p.MB, QM = p.qmax;
-  const int rs = row_stride<St, CPLX>(s);
-  const bool gamma = p.rot_mode == ROT_GAMMA;
-  const int na = gamma ? p.nvec : 0;
-  const GroupLayout L = group_layout<Acc, St, CPLX>(QM, MB, s, na);
+  __shared__ GatherParams s_p[2];
+  const int QM = gb.qmax;
+  const GroupLayout L = group_layout_dims<Acc, St>(QM, gb.e_modes, gb.ph_atoms, gb.ybuf);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
   int* s_rot = reinterpret_cast<int*>(sm + L.rot);
   int* s_id = reinterpret_cast<int*>(sm + L.ident);
@@ -511,25 +542,43 @@ group_gather_kernel(GatherParams p) {
   int* s_rotf = s_id + QM;  // second half of the ident block
   Acc* s_e = reinterpret_cast<Acc*>(sm + L.e);
   St* const s_Y0 = reinterpret_cast<St*>(sm + L.Y);
-  const size_t ybuf = (size_t)8 * MB * rs;
-  const int G = p.nsc + p.nvec + p.nmat;
-  const int n_groups = *p.n_groups;
-  Out* out = reinterpret_cast<Out*>(p.out);
+  const size_t ybuf = (size_t)gb.ybuf;
+  const int n_groups = *gb.n_groups;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int warp = tid >> 5, lane = tid & 31, nwarp = nth >> 5;
-  const int nblk = (B + MB - 1) / MB;
+  if (single) {
+    const int* src = reinterpret_cast<const int*>(single);
+    for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth) {
+      reinterpret_cast<int*>(&s_p[0])[w] = src[w];
+      reinterpret_cast<int*>(&s_p[1])[w] = src[w];
+    }
+    __syncthreads();
+  }
 
-  if (warp == 0) fetch_group(p, n_groups, &s_g[0], lane);
+  if (warp == 0) fetch_group(gb, n_groups, &s_p[0], &s_g[0], lane);
   __syncthreads();
   if (s_g[0].count < 0) return;
-  issue_rows<St, CPLX>(p, s_g[0], 0, min(MB, B), MB, rs, s_Y0, warp, lane, nwarp);
+  {
+    const GatherParams& pn = s_p[0];
+    issue_rows<St, CPLX>(pn, s_g[0], 0, min(pn.MB, pn.B), pn.MB, row_stride<St, CPLX>(pn.s), s_Y0, warp, lane,
+                         nwarp);
+  }
   cp_async_commit();
   int cur = 0, buf = 0;
 
   for (;;) {
     const GroupInfo& gc = s_g[cur];
+    const GatherParams& p = s_p[cur];
+    const int B = p.B, s = p.s, MB = p.MB;
+    const int rs = row_stride<St, CPLX>(s);
+    const bool gamma = p.rot_mode == ROT_GAMMA;
+    const int na = gamma ? p.nvec : 0;
+    const int G = p.nsc + p.nvec + p.nmat;
+    const int nblk = (B + MB - 1) / MB;
+    const long long qb = p.q_base;
+    Out* out = reinterpret_cast<Out*>(p.out);
     // the next group is taken now so that its first rows can load early
-    if (warp == 0) fetch_group(p, n_groups, &s_g[cur ^ 1], lane);
+    if (warp == 0) fetch_group(gb, n_groups, &s_p[cur ^ 1], &s_g[cur ^ 1], lane);
     const int count = gc.count, start = gc.start, nslot = gc.nslot, pivot = gc.pivot;
     // per-q records: weights by slot, R and R⁻¹
     for (int j = tid; j < count; j += nth) {
@@ -619,10 +668,13 @@ group_gather_kernel(GatherParams p) {
         // rows for the following block: this group's next block, or the
         // first block of the next group
         const GroupInfo& gn = s_g[cur ^ 1];
-        if (bi + 1 < nblk)
+        if (bi + 1 < nblk) {
           issue_rows<St, CPLX>(p, gc, b0 + MB, min(MB, B - b0 - MB), MB, rs, (s_Y0 + (buf ^ 1) * ybuf), warp, lane, nwarp);
-        else if (gn.count >= 0)
-          issue_rows<St, CPLX>(p, gn, 0, min(MB, B), MB, rs, (s_Y0 + (buf ^ 1) * ybuf), warp, lane, nwarp);
+        } else if (gn.count >= 0) {
+          const GatherParams& pn = s_p[cur ^ 1];
+          issue_rows<St, CPLX>(pn, gn, 0, min(pn.MB, pn.B), pn.MB, row_stride<St, CPLX>(pn.s),
+                               (s_Y0 + (buf ^ 1) * ybuf), warp, lane, nwarp);
+        }
         cp_async_commit();
       }
       const St* s_Y = s_Y0 + buf * ybuf;
@@ -655,10 +707,10 @@ group_gather_kernel(GatherParams p) {
       const int nitem = mb * G;
       if constexpr (kRegTile) {
         if (nslot == 4)
-          reg_tile_items<4, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q,
+          reg_tile_items<4, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, qb,
                                                 count, pivot, MB, b0, mb, G, na, out);
         else
-          reg_tile_items<8, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q,
+          reg_tile_items<8, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, qb,
                                                 count, pivot, MB, b0, mb, G, na, out);
       } else {
         const int items = count * nitem;
@@ -668,7 +720,7 @@ group_gather_kernel(GatherParams p) {
           const int b = jb % mb, j = jb / mb;
           const int bb = b0 + b;
           const Acc* wj = s_w + 8 * j;
-          Out* dst = out + ((size_t)s_q[j] * B + bb) * (size_t)s * comps;
+          Out* dst = out + ((size_t)(s_q[j] - qb) * B + bb) * (size_t)s * comps;
           int e0, ne;
           if (gi < p.nsc) { e0 = gi; ne = 1; }
           else if (gi < p.nsc + p.nvec) { e0 = p.nsc + 3 * (gi - p.nsc); ne = 3; }
@@ -715,40 +767,85 @@ group_gather_kernel(GatherParams p) {
   cp_async_wait_all();
 }
 
+template <typename Acc, typename St, bool CPLX, typename Out>
+__global__ void __launch_bounds__(kGatherThreads) group_gather_kernel(GatherParams p) {
+  GatherBatch gb{};
+  gb.groups = p.groups;
+  gb.n_groups = p.n_groups;
+  gb.counter = p.counter;
+  gb.qmax = p.qmax;
+  gb.e_modes = p.MB;
+  gb.ph_atoms = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
+  gb.ybuf = 8LL * p.MB * row_stride<St, CPLX>(p.s);
+  gather_groups<Acc, St, CPLX, Out>(&p, gb);
+}
+
+template <typename Acc, typename St, bool CPLX, typename Out>
+__global__ void __launch_bounds__(kGatherThreads) group_gather_batch_kernel(GatherBatch gb) {
+  gather_groups<Acc, St, CPLX, Out>(nullptr, gb);
+}
+
 // Scalar-only interpolators (eigenvalues): one thread per (q, branch),
 // out = Σ_x w_x d[v_x][perm_x(b)] in the reference's order.  The rows are
 // small enough to stay in L2, so no grouping is needed.
+// Interpolated values of branch b for q at record index qi (batch-wide),
+// written at output row qo.
 template <typename Acc, typename St, bool CPLX, typename Out>
-__global__ void scalar_gather_kernel(GatherParams p) {
+__device__ __forceinline__ void scalar_one(const GatherParams& p, long long qi, long long qo, int b) {
   using A = Ar<Acc>;
   constexpr int comps = CPLX ? 2 : 1;
   const St* data = reinterpret_cast<const St*>(p.data);
   Out* out = reinterpret_cast<Out*>(p.out);
   const int B = p.B, s = p.s;
+  if (p.status[qi]) return;
+  const int nw = p.nw[qi];
+  const int piv = p.vidx[8 * qi];
+  for (int e = 0; e < s; ++e) {
+    Acc vr = 0, vi = 0;
+    for (int x = 0; x < nw; ++x) {
+      const int v = p.vidx[8 * qi + x];
+      const int pid = perm_lookup(p, piv, v);
+      const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b) : b;
+      Acc dr, di;
+      Ld<St, CPLX>::get(data, ((long long)v * B + row) * s + e, dr, di);
+      const Acc w = (Acc)p.w[8 * qi + x];
+      vr = A::add(vr, A::mul(w, dr));
+      if (CPLX) vi = A::add(vi, A::mul(w, di));
+    }
+    Out* dst = out + ((size_t)qo * B + b) * (size_t)s * comps + (size_t)e * comps;
+    dst[0] = (Out)vr;
+    if (CPLX) dst[1] = (Out)vi;
+  }
+}
+
+template <typename Acc, typename St, bool CPLX, typename Out>
+__global__ void scalar_gather_kernel(GatherParams p) {
+  const int B = p.B;
   const long long total = p.n * (long long)B;
   for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
        it += (long long)gridDim.x * blockDim.x) {
     const long long qi = it / B;
-    const int b = (int)(it % B);
-    if (p.status[qi]) continue;
-    const int nw = p.nw[qi];
-    const int piv = p.vidx[8 * qi];
-    for (int e = 0; e < s; ++e) {
-      Acc vr = 0, vi = 0;
-      for (int x = 0; x < nw; ++x) {
-        const int v = p.vidx[8 * qi + x];
-        const int pid = perm_lookup(p, piv, v);
-        const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b) : b;
-        Acc dr, di;
-        Ld<St, CPLX>::get(data, ((long long)v * B + row) * s + e, dr, di);
-        const Acc w = (Acc)p.w[8 * qi + x];
-        vr = A::add(vr, A::mul(w, dr));
-        if (CPLX) vi = A::add(vi, A::mul(w, di));
-      }
-      Out* dst = out + ((size_t)qi * B + b) * (size_t)s * comps + (size_t)e * comps;
-      dst[0] = (Out)vr;
-      if (CPLX) dst[1] = (Out)vi;
+    scalar_one<Acc, St, CPLX, Out>(p, qi, qi, (int)(it % B));
+  }
+}
+
+// Scalar-only items of a batch: one thread per (item, q, branch); qb_off[i]
+// is the first pair of item i.
+template <typename Acc, typename St, bool CPLX, typename Out>
+__global__ void scalar_gather_batch_kernel(const GatherParams* items, const long long* qb_off, int n_items,
+                                           long long total) {
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(qb_off + mid) <= it) lo = mid;
+      else hi = mid - 1;
     }
+    const GatherParams& p = items[lo];
+    const long long local = it - __ldg(qb_off + lo);
+    const long long qo = local / p.B;
+    scalar_one<Acc, St, CPLX, Out>(p, p.q_base + qo, qo, (int)(local % p.B));
   }
 }
 
@@ -867,6 +964,88 @@ int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32
 #undef BRX_DISPATCH
   return 1;
 }
+
+// ---------------------------------------------------------------------------
+// batched launches
+// ---------------------------------------------------------------------------
+#define BRX_STORE_TYPES(STORE, ...)                                                      \
+  do {                                                                                   \
+    if ((STORE) == ST_F64) { using Acc = double; using St = double; __VA_ARGS__; }       \
+    else if ((STORE) == ST_F32) { using Acc = float; using St = float; __VA_ARGS__; }    \
+    else { using Acc = float; using St = __nv_bfloat16; __VA_ARGS__; }                   \
+  } while (0)
+
+size_t gather_batch_smem(int store_kind, bool cplx, int qmax, int e_modes, int ph_atoms, long long ybuf) {
+  size_t r = 0;
+  (void)cplx;
+  BRX_STORE_TYPES(store_kind, r = group_layout_dims<Acc, St>(qmax, e_modes, ph_atoms, ybuf).total);
+  return r;
+}
+
+long long gather_ybuf(int store_kind, bool cplx, int MB, int s) {
+  long long r = 0;
+  BRX_STORE_TYPES(store_kind, r = cplx ? 8LL * MB * row_stride<St, true>(s) : 8LL * MB * row_stride<St, false>(s));
+  return r;
+}
+
+template <typename Acc, typename St, bool CPLX, typename Out>
+static int batch_ctas(size_t smem) {
+  cudaFuncSetAttribute(group_gather_batch_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, group_gather_batch_kernel<Acc, St, CPLX, Out>,
+                                                kGatherThreads, smem);
+  return per_sm;
+}
+
+int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem) {
+  int r = 0;
+  BRX_STORE_TYPES(store_kind, {
+    if (cplx) r = out_f32 ? batch_ctas<Acc, St, true, float>(smem) : batch_ctas<Acc, St, true, double>(smem);
+    else r = out_f32 ? batch_ctas<Acc, St, false, float>(smem) : batch_ctas<Acc, St, false, double>(smem);
+  });
+  return r;
+}
+
+// ctas: CTAs per SM, from gather_max_ctas (which also raises the kernel's
+// shared-memory limit); nothing here but the launch, so that a stream
+// capture can record it
+template <typename Acc, typename St, bool CPLX, typename Out>
+static void batch_launch_t(const GatherBatch& gb, int num_sms, size_t smem, int ctas, cudaStream_t s) {
+  if (ctas < 1) ctas = 1;
+  group_gather_batch_kernel<Acc, St, CPLX, Out><<<(unsigned)(num_sms * ctas), kGatherThreads, smem, s>>>(gb);
+}
+
+void launch_gather_batch(const GatherBatch& gb, int store_kind, bool cplx, bool out_f32, int num_sms, size_t smem,
+                         int ctas_per_sm, cudaStream_t s) {
+  cudaMemsetAsync(gb.counter, 0, sizeof(int32_t), s);
+  BRX_STORE_TYPES(store_kind, {
+    if (cplx) {
+      if (out_f32) batch_launch_t<Acc, St, true, float>(gb, num_sms, smem, ctas_per_sm, s);
+      else batch_launch_t<Acc, St, true, double>(gb, num_sms, smem, ctas_per_sm, s);
+    } else {
+      if (out_f32) batch_launch_t<Acc, St, false, float>(gb, num_sms, smem, ctas_per_sm, s);
+      else batch_launch_t<Acc, St, false, double>(gb, num_sms, smem, ctas_per_sm, s);
+    }
+  });
+}
+
+void launch_scalar_batch(const GatherParams* items, const long long* qb_off, int n_items, long long total,
+                         int store_kind, bool cplx, bool out_f32, int num_sms, cudaStream_t s) {
+  if (total <= 0) return;
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)num_sms * 16) blocks = (long long)num_sms * 16;
+  BRX_STORE_TYPES(store_kind, {
+    if (cplx) {
+      if (out_f32) scalar_gather_batch_kernel<Acc, St, true, float><<<(unsigned)blocks, 256, 0, s>>>(items, qb_off, n_items, total);
+      else scalar_gather_batch_kernel<Acc, St, true, double><<<(unsigned)blocks, 256, 0, s>>>(items, qb_off, n_items, total);
+    } else {
+      if (out_f32) scalar_gather_batch_kernel<Acc, St, false, float><<<(unsigned)blocks, 256, 0, s>>>(items, qb_off, n_items, total);
+      else scalar_gather_batch_kernel<Acc, St, false, double><<<(unsigned)blocks, 256, 0, s>>>(items, qb_off, n_items, total);
+    }
+  });
+}
+#undef BRX_STORE_TYPES
 
 // ---------------------------------------------------------------------------
 // grouping: counting sort of q by group key, then one work descriptor per

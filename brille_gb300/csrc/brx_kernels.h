@@ -64,11 +64,38 @@ struct GatherParams {
   void* out;                 // n × B × s, double or float (complex: pairs)
   int MB;                    // modes staged per block
   int qmax;                  // q per work descriptor
+  // batches: records are indexed by batch-wide q, the output by q − q_base;
+  // group keys are batch-wide, the trellis's own by key − key_base
+  long long q_base;
+  int key_base;
+};
+
+// One persistent gather launch over the groups of many interpolators that
+// share storage, complex-ness and output type.  Shared memory is laid out
+// for the largest item: e_modes entries of antiphase per slot, ph_atoms Γ
+// phases per q, and two staging buffers of ybuf elements.
+struct GatherBatch {
+  const GatherParams* items;  // n_items, device
+  const int32_t* key_off;     // n_items: first batch-wide group key of each item
+  int n_items;
+  const GroupDesc* groups;
+  const int32_t* n_groups;
+  int32_t* counter;
+  int qmax;
+  int e_modes;
+  int ph_atoms;
+  long long ybuf;
 };
 
 size_t locate_smem_bytes(const DevGeom& g);
 void launch_locate(const DevGeom& g, const double* Q, long long n, long long base, int mode, const Records& r,
                    ErrorWord* err, int num_sms, cudaStream_t s);
+size_t locate_smem_bytes(const DevGeom& g);
+// Locate for many trellises in one launch: tiles (item, first q, count),
+// block size 64, 128 or 256.
+void launch_locate_batch(const DevGeom* geoms, const long long* q_off, const int32_t* key_off, int key_fail,
+                         const int4* tiles, int n_tiles, const double* const* Qptr, int mode, const Records& r,
+                         ErrorWord* err, size_t smem, int threads, int grid, cudaStream_t s);
 
 // Counting sort of q by group key and the work descriptors of the groups.
 // Returns the number of kernel launches.
@@ -80,6 +107,19 @@ size_t group_scratch_ints(long long n_keys);
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms,
                   size_t smem_budget, cudaStream_t s);
 size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB);
+
+// Batched gather: group-ordered items (vector/matrix data) in one persistent
+// launch; scalar-only items in one launch over all (q, branch) pairs with
+// qb_off[i] = Σ_{k<i} n_k·B_k.  grid 0: one CTA per SM times occupancy.
+void launch_gather_batch(const GatherBatch& gb, int store_kind, bool cplx, bool out_f32, int num_sms, size_t smem,
+                         int ctas_per_sm, cudaStream_t s);
+void launch_scalar_batch(const GatherParams* items, const long long* qb_off, int n_items, long long total,
+                         int store_kind, bool cplx, bool out_f32, int num_sms, cudaStream_t s);
+// shared memory of a batch launch from its largest item dimensions
+size_t gather_batch_smem(int store_kind, bool cplx, int qmax, int e_modes, int ph_atoms, long long ybuf);
+// staging elements of one block of MB modes of an item with s elements per mode
+long long gather_ybuf(int store_kind, bool cplx, int MB, int s);
+int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem);
 
 // Load every query kernel of this library on the current device (module
 // loading is otherwise deferred to the first launch).

@@ -460,12 +460,8 @@ __device__ __forceinline__ void report(ErrorWord* err, long long i, int st) {
   atomicMin(&err->first_bad, i + 0LL);
 }
 
-// mode: 0 interpolate_at (moveinto), 1 ir_interpolate_at (ir_moveinto),
-// 2 no move (Q already in the trellis domain)
-__global__ void __launch_bounds__(kLocateThreads)
-locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long base, int mode,
-              Records r, ErrorWord* err) {
-  extern __shared__ double smem_d[];
+// Tables of one zone in shared memory (smem_d: locate_smem_bytes(g)).
+__device__ __forceinline__ SmemZone stage_zone(const DevGeom& g, double* smem_d) {
   SmemZone z;
   double* p = smem_d;
   float* fp = reinterpret_cast<float*>(p);
@@ -499,69 +495,143 @@ locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long ba
     for (int i = threadIdx.x; i < 3 * g.n_faces; i += blockDim.x) z.n32[i] = (float)g.face_normal[i];
     for (int i = threadIdx.x; i < g.n_faces; i += blockDim.x) z.tl32[i] = (float)g.face_tau_len[i];
   }
-  __syncthreads();
+  return z;
+}
 
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double Qi[3] = {Q[3 * i], Q[3 * i + 1], Q[3 * i + 2]};
-    double q[3];
-    int32_t tau[3] = {0, 0, 0}, rot[2] = {g.identity, g.identity};
-    int st = 0;
-    if (mode == 2) {
-      q[0] = Qi[0]; q[1] = Qi[1]; q[2] = Qi[2];
+// Move, wedge search and trellis locate of the q at Qq; writes its records
+// at index i and returns its status.  key_base/key_fail: the batch-wide group
+// key of the trellis's first key and of every failed q.
+__device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, const double* Qq, long long i, int mode,
+                                          const Records& r, int key_base, int key_fail) {
+  double Qi[3] = {Qq[0], Qq[1], Qq[2]};
+  double q[3];
+  int32_t tau[3] = {0, 0, 0}, rot[2] = {g.identity, g.identity};
+  int st = 0;
+  if (mode == 2) {
+    q[0] = Qi[0]; q[1] = Qi[1]; q[2] = Qi[2];
+  } else {
+    st = moveinto_one(g, z, Qi, q, tau);
+    if (!st && mode == 1) st = wedge_one(g, z, q, rot);
+  }
+  int32_t nt[2] = {-1, -1}, vi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  int nw = 0;
+  if (!st) {
+    double x[3];
+    hkl_to_xyz(x, g.outer_B, q);
+    long long node = node_subscript(g, x);
+    nt[0] = (int32_t)node;
+    if (node < 0) {
+      st = BRX_ERR_NOT_FOUND;
     } else {
-      st = moveinto_one(g, z, Qi, q, tau);
-      if (!st && mode == 1) st = wedge_one(g, z, q, rot);
+      int k = node_weights(g, node, x, &nt[1], vi, w);
+      if (k > 0) nw = k;
+      else st = (k == 0) ? BRX_ERR_NOT_FOUND : -k;
     }
-    int32_t nt[2] = {-1, -1}, vi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    int nw = 0;
-    if (!st) {
-      double x[3];
-      hkl_to_xyz(x, g.outer_B, q);
-      long long node = node_subscript(g, x);
-      nt[0] = (int32_t)node;
-      if (node < 0) {
-        st = BRX_ERR_NOT_FOUND;
-      } else {
-        int k = node_weights(g, node, x, &nt[1], vi, w);
-        if (k > 0) nw = k;
-        else st = (k == 0) ? BRX_ERR_NOT_FOUND : -k;
-      }
-    }
-    r.q_ir[3 * i] = q[0]; r.q_ir[3 * i + 1] = q[1]; r.q_ir[3 * i + 2] = q[2];
-    if (r.tau) { r.tau[3 * i] = tau[0]; r.tau[3 * i + 1] = tau[1]; r.tau[3 * i + 2] = tau[2]; }
-    r.rot[2 * i] = rot[0]; r.rot[2 * i + 1] = rot[1];
-    r.node[2 * i] = nt[0]; r.node[2 * i + 1] = nt[1];
-    r.nw[i] = nw;
+  }
+  r.q_ir[3 * i] = q[0]; r.q_ir[3 * i + 1] = q[1]; r.q_ir[3 * i + 2] = q[2];
+  if (r.tau) { r.tau[3 * i] = tau[0]; r.tau[3 * i + 1] = tau[1]; r.tau[3 * i + 2] = tau[2]; }
+  r.rot[2 * i] = rot[0]; r.rot[2 * i + 1] = rot[1];
+  r.node[2 * i] = nt[0]; r.node[2 * i + 1] = nt[1];
+  r.nw[i] = nw;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = vi[k]; r.w[8 * i + k] = w[k]; }
-    r.status[i] = st;
-    int32_t key = (int32_t)n_group_keys(g.n_cube, g.n_tets);  // failed q: last bucket
-    if (!st) {
-      const long long node = nt[0];
-      if (nt[1] < 0) {
-        const int32_t ni = __ldg(g.node_index + node);
-        const int32_t* cv = g.cube_vertices + 8 * (long long)ni;
-        int slot = 0;
-        for (int j = 0; j < 8; ++j)
-          if (__ldg(cv + 7 - j) == vi[0]) { slot = j; break; }
-        key = 8 * ni + slot;
-      } else {
-        const int32_t* tv = g.tet_vertices + 4 * (long long)nt[1];
-        int slot = 0;
-        for (int j = 0; j < 4; ++j)
-          if (__ldg(tv + j) == vi[0]) { slot = j; break; }
-        key = (int32_t)(8LL * g.n_cube + 4LL * nt[1] + slot);
-      }
+  for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = vi[k]; r.w[8 * i + k] = w[k]; }
+  r.status[i] = st;
+  int32_t key = (int32_t)n_group_keys(g.n_cube, g.n_tets);  // failed q: last bucket
+  if (!st) {
+    const long long node = nt[0];
+    if (nt[1] < 0) {
+      const int32_t ni = __ldg(g.node_index + node);
+      const int32_t* cv = g.cube_vertices + 8 * (long long)ni;
+      int slot = 0;
+      for (int j = 0; j < 8; ++j)
+        if (__ldg(cv + 7 - j) == vi[0]) { slot = j; break; }
+      key = 8 * ni + slot;
+    } else {
+      const int32_t* tv = g.tet_vertices + 4 * (long long)nt[1];
+      int slot = 0;
+      for (int j = 0; j < 4; ++j)
+        if (__ldg(tv + j) == vi[0]) { slot = j; break; }
+      key = (int32_t)(8LL * g.n_cube + 4LL * nt[1] + slot);
     }
-    r.key[i] = key;
+  }
+  r.key[i] = st ? key_fail : key_base + key;
+  return st;
+}
+
+// mode: 0 interpolate_at (moveinto), 1 ir_interpolate_at (ir_moveinto),
+// 2 no move (Q already in the trellis domain)
+__global__ void __launch_bounds__(kLocateThreads)
+locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long base, int mode,
+              Records r, ErrorWord* err) {
+  extern __shared__ double smem_d[];
+  const SmemZone z = stage_zone(g, smem_d);
+  __syncthreads();
+  const int key_fail = (int)n_group_keys(g.n_cube, g.n_tets);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int st = locate_one(g, z, Q + 3 * i, i, mode, r, 0, key_fail);
     if (st) report(err, base + i, st);
+  }
+}
+
+// Many trellises in one persistent launch.  Work comes in tiles of one
+// item's q (tiles[t] = item, first q, count); a CTA restages the zone
+// tables whenever its next tile belongs to another item.  Records are
+// batch-wide (item i's q start at q_off[i]); each item reads its Q through
+// Qptr[i] and reports errors into err[i] with item-local q indices.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS)
+locate_batch_kernel(const DevGeom* __restrict__ geoms, const long long* __restrict__ q_off,
+                    const int32_t* __restrict__ key_off, int key_fail, const int4* __restrict__ tiles, int n_tiles,
+                    const double* const* __restrict__ Qptr, int mode, Records r, ErrorWord* err) {
+  extern __shared__ double smem_d[];
+  __shared__ DevGeom s_geom;
+  int cur = -1;
+  SmemZone z{};
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const int4 tile = tiles[t];
+    if (tile.x != cur) {
+      __syncthreads();  // the previous item's tables are no longer read
+      for (int w = threadIdx.x; w < (int)(sizeof(DevGeom) / sizeof(int)); w += THREADS)
+        reinterpret_cast<int*>(&s_geom)[w] = reinterpret_cast<const int*>(geoms + tile.x)[w];
+      __syncthreads();
+      z = stage_zone(s_geom, smem_d);
+      __syncthreads();
+      cur = tile.x;
+    }
+    const DevGeom& g = s_geom;
+    const double* Q = Qptr[cur];
+    const long long qo = q_off[cur];
+    const int kb = key_off[cur];
+    for (int k = threadIdx.x; k < tile.z; k += THREADS) {
+      const long long il = (long long)tile.y + k;
+      const int st = locate_one(g, z, Q + 3 * il, qo + il, mode, r, kb, key_fail);
+      if (st) report(err + cur, il, st);
+    }
   }
 }
 
 cudaError_t preload_locate_kernel() {
   cudaFuncAttributes a;
   return cudaFuncGetAttributes(&a, locate_kernel);
+}
+
+void launch_locate_batch(const DevGeom* geoms, const long long* q_off, const int32_t* key_off, int key_fail,
+                         const int4* tiles, int n_tiles, const double* const* Qptr, int mode, const Records& r,
+                         ErrorWord* err, size_t smem, int threads, int grid, cudaStream_t s) {
+  if (n_tiles <= 0) return;
+  if (grid > n_tiles) grid = n_tiles;
+  switch (threads) {
+    case 64:
+      locate_batch_kernel<64><<<grid, 64, smem, s>>>(geoms, q_off, key_off, key_fail, tiles, n_tiles, Qptr, mode, r, err);
+      break;
+    case 256:
+      locate_batch_kernel<256><<<grid, 256, smem, s>>>(geoms, q_off, key_off, key_fail, tiles, n_tiles, Qptr, mode, r, err);
+      break;
+    default:
+      locate_batch_kernel<128><<<grid, 128, smem, s>>>(geoms, q_off, key_off, key_fail, tiles, n_tiles, Qptr, mode, r, err);
+      break;
+  }
 }
 
 size_t locate_smem_bytes(const DevGeom& g) {

@@ -260,6 +260,51 @@ brx_status brx_mlp_forward(const brx_mlp_dims* d, const float* params, const flo
 brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const float* params, float omega_scale,
                                   float res_scale, float clip);
 
+/* ---------------------------------------------------------------------
+ * Batched queries over many interpolators (the batched entry point the
+ * reference's host would add beside ir_interpolate_at; no counterpart in
+ * the reference itself).  Every stage of a batch is one launch over all
+ * items: locate, the counting sort of all items' q, the values gather and
+ * the vectors gather.  Items may differ in trellis, space group, mode and
+ * atom count and q count; they must share the device, the storage kind
+ * and complex-ness of their values and of their vectors, whether values
+ * are scalar-only, and whether vectors are present.  Handles must outlive
+ * the batch and keep their data (no brx_fill in between).  Q and outputs
+ * are device buffers with the single-query layouts.
+ *
+ *   brx_batch_create   plan for n items with n_q[i] q each (ir: 1 for
+ *                      ir_interpolate_at, 0 for interpolate_at; flags:
+ *                      BRX_FLAG_NO_MOVE, BRX_FLAG_OUT_F32)
+ *   brx_batch_set_io   the items' Q and output pointers (host arrays of
+ *                      device pointers; vectors NULL without vectors)
+ *   brx_batch_run      enqueue the batch on stream: copies and launches
+ *                      only, so it can be recorded by a stream capture
+ *   brx_batch_capture  record brx_batch_run into a CUDA graph kept by the
+ *                      batch; brx_batch_launch replays it (and sees the
+ *                      pointers of the latest brx_batch_set_io)
+ *   brx_batch_sync     wait for stream; the first failing item's status and
+ *                      message (prefixed "item i: "), its index in *failed
+ *   brx_batch_tune     time launch-shape candidates on the current I/O with
+ *                      CUDA events (locate block size, CTAs per SM, q per
+ *                      tile; each gather's shared-memory budget) and keep
+ *                      the fastest; drops a captured graph
+ *   brx_batch_config   the chosen shapes: locate threads, locate CTAs per
+ *                      SM, q per tile, values and vectors smem budget (KB),
+ *                      values and vectors CTAs per SM, number of tiles */
+typedef struct brx_batch brx_batch;
+brx_status brx_batch_create(brx_handle* const* handles, int32_t n, const int64_t* n_q, int32_t ir, uint32_t flags,
+                            brx_batch** out);
+void brx_batch_destroy(brx_batch* b);
+brx_status brx_batch_set_io(brx_batch* b, const double* const* Q, void* const* values, void* const* vectors);
+brx_status brx_batch_run(brx_batch* b, void* stream);
+brx_status brx_batch_capture(brx_batch* b, void* stream);
+brx_status brx_batch_launch(brx_batch* b, void* stream);
+brx_status brx_batch_sync(brx_batch* b, void* stream, int32_t* failed);
+brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps);
+brx_status brx_batch_config(const brx_batch* b, int32_t* cfg, int32_t n);
+int64_t brx_batch_launch_count(const brx_batch* b);
+const char* brx_batch_last_error(const brx_batch* b);
+
 /* Wait for work queued with BRX_FLAG_ASYNC and report its status. */
 brx_status brx_sync(brx_handle* h, void* stream);
 

@@ -1,0 +1,119 @@
+"""Batched queries (brx_batch_*): many grids of different space groups,
+trellises, mode counts and ragged q counts in one launch per stage must give
+each grid exactly what its own ir_interpolate_at gives (bit for bit: the
+same kernels and operation order per q), through a plain run, a captured
+graph replayed on new inputs, and after autotuning; failures name the item.
+"""
+import numpy as np
+import pytest
+
+from _cases import crystal_case
+from brille_gb300 import BZTrellisQdc
+from brille_gb300.batch import BatchQuery
+from brille_gb300.grid import BZTrellisQdd
+from brille_gb300._lib import BrxError
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+NAMES = ["diamond2", "hex16", "P-1", "R-3m", "Im-3m", "diamond8"]
+COUNTS = [1000, 3001, 0, 1, 2500, 777]
+
+
+def _grids(storage="f64", values_only=False):
+    out = []
+    for name in NAMES:
+        c = crystal_case(name)
+        if values_only:
+            g = BZTrellisQdd(c["bz"], trellis=c["tr"])
+            g.fill(c["w"][:, :, None], [1, 0, 0, 0, 3], storage=storage)
+        else:
+            g = BZTrellisQdc(c["bz"], trellis=c["tr"])
+            g.fill(c["w"], [1, 0, 0, 0, 3], c["v"], [0, 3 * c["model"].n_atoms, 0, 2, 1], storage=storage)
+        out.append(g)
+    return out
+
+
+def _Q(seed, counts=COUNTS, scale=1.0):
+    rng = np.random.default_rng(seed)
+    return [rng.uniform(-scale, scale, (n, 3)) for n in counts]
+
+
+def _check(grids, Qs, vals, vecs, out_f32):
+    for i, (g, Q) in enumerate(zip(grids, Qs)):
+        if len(Q) == 0:
+            continue
+        v, c = g.ir_interpolate_at(Q, out_f32=out_f32)
+        assert np.array_equal(vals[i].cpu().numpy(), v), i
+        if c is not None:
+            assert np.array_equal(vecs[i].cpu().numpy(), c), i
+
+
+@pytest.mark.parametrize("storage,out_f32", [("f64", False), ("f32", True)])
+def test_batch_matches_single_queries(storage, out_f32):
+    grids = _grids(storage)
+    Qs = _Q(1)
+    bq = BatchQuery(grids, COUNTS, out_f32=out_f32)
+    vals, vecs = bq.query([torch.from_numpy(q).cuda() for q in Qs])
+    _check(grids, Qs, vals, vecs, out_f32)
+
+
+def test_values_only_batch_uses_scalar_gather():
+    grids = _grids("f64", values_only=True)
+    Qs = _Q(2)
+    bq = BatchQuery(grids, COUNTS)
+    vals, vecs = bq.query([torch.from_numpy(q).cuda() for q in Qs])
+    assert all(v is None for v in vecs)
+    _check(grids, Qs, vals, vecs, False)
+
+
+def test_graph_replay_on_new_inputs_and_tuning():
+    grids = _grids("f32")
+    bq = BatchQuery(grids, COUNTS, out_f32=True)
+    s = torch.cuda.Stream()
+    Q1 = [torch.from_numpy(q).cuda() for q in _Q(3)]
+    vals, vecs = bq.outputs()
+    bq.set_io(Q1, vals, vecs)
+    bq.capture(s.cuda_stream)
+    bq.launch(s.cuda_stream)
+    bq.sync(s.cuda_stream)
+    _check(grids, [q.cpu().numpy() for q in Q1], vals, vecs, True)
+    # new Q buffers, same graph
+    Q2 = [torch.from_numpy(q).cuda() for q in _Q(4)]
+    bq.set_io(Q2, vals, vecs)
+    bq.launch(s.cuda_stream)
+    bq.sync(s.cuda_stream)
+    _check(grids, [q.cpu().numpy() for q in Q2], vals, vecs, True)
+    cfg = bq.tune(s.cuda_stream, reps=1)
+    assert cfg["locate_threads"] in (64, 128, 256) and cfg["tiles"] > 0
+    assert cfg["vectors_ctas_per_sm"] >= 1
+    for v in vals:
+        v.zero_()
+    bq.run(s.cuda_stream)
+    bq.sync(s.cuda_stream)
+    _check(grids, [q.cpu().numpy() for q in Q2], vals, vecs, True)
+
+
+def test_failure_names_the_item():
+    grids = _grids("f64")
+    counts = [50] * len(grids)
+    # points already in each trellis (q_ir of a first locate), except item 3's,
+    # moved far outside: with no move, not found
+    Qs = [g.locate(q)["q_ir"] for g, q in zip(grids, _Q(5, counts))]
+    Qs[3] = Qs[3] + 10.0
+    bq = BatchQuery(grids, counts, no_move=True)
+    with pytest.raises(BrxError) as e:
+        bq.query([torch.from_numpy(q).cuda() for q in Qs])
+    assert e.value.item == 3
+    assert "item 3" in str(e.value)
+
+
+def test_mixed_element_kinds_are_rejected():
+    c = crystal_case("diamond2")
+    a = BZTrellisQdc(c["bz"], trellis=c["tr"])
+    a.fill(c["w"], [1, 0, 0, 0, 3], c["v"], [0, 6, 0, 2, 1])
+    b = BZTrellisQdd(c["bz"], trellis=c["tr"])
+    b.fill(c["w"][:, :, None], [1, 0, 0, 0, 3])
+    with pytest.raises(BrxError):
+        BatchQuery([a, b], [10, 10])
