@@ -22,6 +22,7 @@
 #include <limits>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/brx.h"
@@ -713,10 +714,34 @@ void brx_destroy(brx_handle* h) {
   delete h;
 }
 
+}  // extern "C"
+
+template <typename In, typename Out>
+__global__ void convert_kernel(const In* __restrict__ src, Out* __restrict__ dst, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if constexpr (std::is_same<Out, __nv_bfloat16>::value) dst[i] = __float2bfloat16_rn((float)src[i]);
+    else dst[i] = (Out)src[i];
+  }
+}
+
+template <typename In, typename Out>
+static void convert(const In* src, Out* dst, size_t n, cudaStream_t s) {
+  if (!n) return;
+  size_t blocks = (n + 255) / 256;
+  if (blocks > 65536) blocks = 65536;
+  convert_kernel<In, Out><<<(unsigned)blocks, 256, 0, s>>>(src, dst, n);
+}
+
+extern "C" {
+
+// Vertex data to the device in the storage precision.  Sources are float64
+// / complex128 or float32 / complex64, in host or device memory; the
+// conversion runs on the device (host sources are staged in chunks).
 static brx_status fill_one(brx_handle* h, const brx_data* d, Interp& dst, int storage) {
   if (!d) { dst.present = false; return BRX_OK; }
   if (!d->data || d->n_branches < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "data must be non-empty");
-  if (d->dtype != BRX_F64 && d->dtype != BRX_C128) return fail(h, BRX_ERR_INVALID_ARGUMENT, "data must be float64 or complex128");
+  if (d->dtype != BRX_F64 && d->dtype != BRX_C128 && d->dtype != BRX_F32 && d->dtype != BRX_C64)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "data must be float64, complex128, float32 or complex64");
   for (int i = 0; i < 3; ++i)
     if (d->elements[i] < 0) return fail(h, BRX_ERR_INVALID_ARGUMENT, "negative element count");
   if (d->elements[1] % 3 || d->elements[2] % 9)
@@ -724,37 +749,58 @@ static brx_status fill_one(brx_handle* h, const brx_data* d, Interp& dst, int st
   const int s = d->elements[0] + d->elements[1] + d->elements[2];
   if (s < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "each branch needs at least one element");
   if (s > 32 * 24) return fail(h, BRX_ERR_INVALID_ARGUMENT, "more than 768 elements per branch are not supported");
+  const bool in64 = d->dtype == BRX_F64 || d->dtype == BRX_C128;
   dst.present = true;
-  dst.cplx = d->dtype == BRX_C128;
+  dst.cplx = d->dtype == BRX_C128 || d->dtype == BRX_C64;
   dst.B = d->n_branches;
   dst.s = s;
   for (int i = 0; i < 3; ++i) dst.el[i] = d->elements[i];
   dst.rotates_like = d->rotates_like;
   dst.length_unit = d->length_unit;
   const size_t count = (size_t)h->host_geom.n_vertices * dst.B * s * (dst.cplx ? 2 : 1);  // reals
-  const bool src_host = host_ptr(d->data);
-  std::vector<double> tmp;
-  const double* src = static_cast<const double*>(d->data);
-  if (!src_host) {
-    tmp.resize(count);
-    BRX_CUDA(h, cudaMemcpy(tmp.data(), d->data, sizeof(double) * count, cudaMemcpyDeviceToHost));
-    src = tmp.data();
-  }
+  const size_t in_size = in64 ? 8 : 4;
   dst.store = storage == BRX_STORE_F64 ? ST_F64 : (storage == BRX_STORE_F32 ? ST_F32 : ST_BF16);
-  if (storage == BRX_STORE_F64) {
-    BRX_CUDA(h, dst.data.ensure(sizeof(double) * count));
-    BRX_CUDA(h, cudaMemcpy(dst.data.p, src, sizeof(double) * count, cudaMemcpyHostToDevice));
-  } else if (storage == BRX_STORE_F32) {
-    std::vector<float> f(count);
-    for (size_t i = 0; i < count; ++i) f[i] = (float)src[i];
-    BRX_CUDA(h, dst.data.ensure(sizeof(float) * count));
-    BRX_CUDA(h, cudaMemcpy(dst.data.p, f.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+  const size_t out_size = dst.store == ST_F64 ? 8 : (dst.store == ST_F32 ? 4 : 2);
+  BRX_CUDA(h, dst.data.ensure(out_size * count));
+  cudaStream_t cs = h->sc[0].stream;
+  auto conv = [&](const void* src, size_t off, size_t n) {
+    char* out = static_cast<char*>(dst.data.p) + out_size * off;
+    if (in64) {
+      const double* in = static_cast<const double*>(src);
+      if (dst.store == ST_F64) convert(in, reinterpret_cast<double*>(out), n, cs);
+      else if (dst.store == ST_F32) convert(in, reinterpret_cast<float*>(out), n, cs);
+      else convert(in, reinterpret_cast<__nv_bfloat16*>(out), n, cs);
+    } else {
+      const float* in = static_cast<const float*>(src);
+      if (dst.store == ST_F64) convert(in, reinterpret_cast<double*>(out), n, cs);
+      else if (dst.store == ST_F32) convert(in, reinterpret_cast<float*>(out), n, cs);
+      else convert(in, reinterpret_cast<__nv_bfloat16*>(out), n, cs);
+    }
+  };
+  if (!host_ptr(d->data)) {
+    conv(d->data, 0, count);
   } else {
-    std::vector<__nv_bfloat16> f(count);
-    for (size_t i = 0; i < count; ++i) f[i] = __float2bfloat16_rn((float)src[i]);
-    BRX_CUDA(h, dst.data.ensure(sizeof(__nv_bfloat16) * count));
-    BRX_CUDA(h, cudaMemcpy(dst.data.p, f.data(), sizeof(__nv_bfloat16) * count, cudaMemcpyHostToDevice));
+    // chunks of at most 64 Mi reals through one device staging buffer
+    const size_t chunk = std::min<size_t>(count, (size_t)64 << 20);
+    DevBuf stage;
+    if (stage.ensure(in_size * chunk) != cudaSuccess) return fail(h, BRX_ERR_OUT_OF_MEMORY, "fill staging buffer");
+    for (size_t off = 0; off < count; off += chunk) {
+      const size_t n = std::min(chunk, count - off);
+      cudaError_t e = cudaMemcpyAsync(stage.p, static_cast<const char*>(d->data) + in_size * off, in_size * n,
+                                      cudaMemcpyHostToDevice, cs);
+      if (e == cudaSuccess) {
+        conv(stage.p, off, n);
+        e = cudaStreamSynchronize(cs);  // the staging buffer is reused
+      }
+      if (e != cudaSuccess) {
+        stage.release();
+        return cuda_fail(h, e, "fill");
+      }
+    }
+    stage.release();
   }
+  BRX_CUDA(h, cudaGetLastError());
+  BRX_CUDA(h, cudaStreamSynchronize(cs));
   return BRX_OK;
 }
 

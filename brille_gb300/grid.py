@@ -81,6 +81,43 @@ def _elements(arr, el):
     return B, e, rot, lu
 
 
+def _is_device(x):
+    return hasattr(x, "data_ptr") and bool(getattr(x, "is_cuda", False))
+
+
+def _as_data(x, dt):
+    """numpy arrays are converted to the grid's dtype on the host; CUDA
+    tensors stay on the device (float32/complex64 or float64/complex128) and
+    are converted by brx_fill."""
+    if _is_device(x):
+        import torch
+
+        want_cplx = np.dtype(dt).kind == "c"
+        if x.is_complex() != want_cplx:
+            x = x.to(torch.complex128 if want_cplx else torch.float64)
+        if x.dtype not in (torch.float64, torch.complex128, torch.float32, torch.complex64):
+            x = x.to(torch.float64)
+        return x.contiguous()
+    return np.ascontiguousarray(np.asarray(x), dtype=dt)
+
+
+def _make_data(arr, nv, B, e, rot, lu):
+    if not _is_device(arr):
+        return _abi.make_data(arr.reshape(nv, -1), B, e, rot, lu)
+    import torch
+
+    codes = {torch.float64: _abi.BRX_F64, torch.complex128: _abi.BRX_C128, torch.float32: _abi.BRX_F32,
+             torch.complex64: _abi.BRX_C64}
+    d = _abi.Data()
+    d.data = arr.data_ptr()
+    d.dtype = codes[arr.dtype]
+    d.n_branches = int(B)
+    d.elements[:] = [int(x) for x in e]
+    d.rotates_like = int(rot)
+    d.length_unit = int(lu)
+    return d, arr
+
+
 def _ptr(obj):
     """Address of a numpy array or of an object with data_ptr() (torch)."""
     if obj is None:
@@ -174,27 +211,28 @@ class _Grid:
                                       "with set_permutations()")
         vdt = np.complex128 if self.VALUE_COMPLEX else np.float64
         cdt = np.complex128 if self.VECTOR_COMPLEX else np.float64
-        vals = np.ascontiguousarray(np.asarray(values), dtype=vdt)
+        vals = _as_data(values, vdt)
         nv = self.trellis.vertices.shape[0]
         if vals.shape[0] != nv:
             raise RuntimeError(f"Provided {vals.shape[0]} arrays but {nv} were expected!")
         Bv, ev, rv, lv = _elements(vals, values_elements)
-        vd, vkeep = _abi.make_data(vals.reshape(nv, -1), Bv, ev, rv, lv)
+        vd, vkeep = _make_data(vals, nv, Bv, ev, rv, lv)
         cd = ckeep = None
         Bc = ev_c = None
+        vecs = None
         if vectors is not None:
-            vecs = np.ascontiguousarray(np.asarray(vectors), dtype=cdt)
+            vecs = _as_data(vectors, cdt)
             if vecs.shape[0] != nv:
                 raise RuntimeError(f"Provided {vecs.shape[0]} arrays but {nv} were expected!")
             Bc, ev_c, rc, lc = _elements(vecs, vectors_elements)
             if Bc != Bv:
                 raise RuntimeError("The values and vectors must have matching number of points and branches")
-            cd, ckeep = _abi.make_data(vecs.reshape(nv, -1), Bc, ev_c, rc, lc)
+            cd, ckeep = _make_data(vecs, nv, Bc, ev_c, rc, lc)
         h = self._handle()
         st = load().brx_fill(h, C.byref(vd), C.byref(cd) if cd is not None else None, _STORAGE[storage])
         check(st, h)
-        self._fill = dict(values=vals, vectors=None if vectors is None else np.asarray(vectors),
-                          vshape=vals.shape[1:], cshape=None if vectors is None else np.shape(vectors)[1:],
+        self._fill = dict(values=vals, vectors=vecs,
+                          vshape=tuple(vals.shape[1:]), cshape=None if vecs is None else tuple(vecs.shape[1:]),
                           vdtype=vdt, cdtype=cdt, values_weights=values_weights, vectors_weights=vectors_weights,
                           storage=storage)
         return True

@@ -133,7 +133,7 @@ typedef struct brx_geometry {
  * wrap/_interpolator.hpp:13-110). */
 typedef struct brx_data {
   const void* data;               /* n_vertices × n_branches × span elements (host or device) */
-  int32_t dtype;                  /* BRX_F64 or BRX_C128 */
+  int32_t dtype;                  /* BRX_F64, BRX_C128, BRX_F32 or BRX_C64 */
   int32_t n_branches;             /* B */
   int32_t elements[3];            /* scalars, vector elements (3 per vector), matrix elements (9 per matrix) */
   int32_t rotates_like;           /* BRX_ROT_* */
