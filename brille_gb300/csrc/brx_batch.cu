@@ -184,7 +184,18 @@ brx_status plan_gather(brx_batch* b, std::vector<brx::GatherParams>& P, int stor
       const long long y = brx::gather_ybuf(store, cplx, P[i].MB, P[i].s);
       if (y > wy) { wy = y; worst = i; }
     }
-    if (P[worst].MB <= 1) break;
+    if (P[worst].MB <= 1) {
+      // the largest buffer cannot shrink: accept what the device holds
+      if (need > b->smem_optin) break;
+      gb->qmax = brx::kGroupQ;
+      gb->e_modes = e;
+      gb->ph_atoms = na;
+      gb->ybuf = yb;
+      *smem = need;
+      *ctas = brx::gather_max_ctas(store, cplx, b->out_f32, need);
+      if (*ctas < 1) break;
+      return BRX_OK;
+    }
     P[worst].MB = (P[worst].MB + 1) / 2;
   }
   return bfail(b, BRX_ERR_INVALID_ARGUMENT, "batch gather does not fit in shared memory");
@@ -566,7 +577,7 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
           b->loc_threads = threads;
           b->loc_ctas = per_sm;
           b->tile_q = tq;
-          if ((st = plan(b))) break;
+          if (plan(b)) continue;
           stage_io(b);
           const float t = time_run(0, 1);
           if (t < best) { best = t; bt = threads; bc = per_sm; bq = tq; }
@@ -583,7 +594,7 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
     for (size_t bud : budgets) {
       if (bud > b->smem_optin) continue;
       b->budget_vals = bud;
-      if ((st = plan(b))) break;
+      if (plan(b)) continue;
       stage_io(b);
       const float t = time_run(2, 3);
       if (t < best) { best = t; bb = bud; }
@@ -596,7 +607,7 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
     for (size_t bud : budgets) {
       if (bud > b->smem_optin) continue;
       b->budget_vecs = bud;
-      if ((st = plan(b))) break;
+      if (plan(b)) continue;
       stage_io(b);
       const float t = time_run(3, 4);
       if (t < best) { best = t; bb = bud; }
