@@ -301,7 +301,11 @@ def _batch_item(k, seed, vmin, vmax):
     bz = BrillouinZone(lat)
     target = float(np.exp(rng.uniform(np.log(vmin), np.log(vmax))))
     ratio = bz.volume / ConvexHull(bz.ir_vertices).volume
-    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * 4.0 / (ratio * target))
+    frac = 4.0 / (ratio * target)
+    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac)
+    # one correction: vertex count scales about as 1/node volume
+    if not 0.67 < len(tr.vertices) / target < 1.5:
+        tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac * len(tr.vertices) / target)
     return name, lat, tr
 
 
