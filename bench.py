@@ -565,6 +565,7 @@ def main():
     ap.add_argument("--out-f64", action="store_true", help="float64/complex128 outputs")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-tune", action="store_true", help="keep the default gather shared-memory budgets")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned", "batch"],
                     help="precision: FP32 and BF16 storage against the FP64 path; learned: the learned residual "
                          "on coarse trellises against the plain fine trellis")
@@ -630,6 +631,12 @@ def main():
 
     def step(i):
         grid.query_into(Qs[i % nbuf], n, vals, vecs, out_f32=out_f32, async_=True, stream=sp)
+
+    tuned = None
+    if not args.no_tune:
+        t = time.time()
+        tuned = grid.tune(Qs[0], out_f32=out_f32, reps=1, stream=sp)
+        log(f"[setup] gather budgets (KB, values/vectors) {tuned} in {time.time() - t:.1f}s")
 
     for i in range(args.warmup):
         step(i)
@@ -713,6 +720,7 @@ def main():
                         q_per_step=n, q_range=qr, storage=args.storage,
                         outputs="f32/c64" if out_f32 else "f64/c128",
                         l2="outputs of %.1f GB per step exceed the 129 MB L2" % (n * (bq_vals + bq_vecs) / 1e9),
+                        gather_smem_kb=tuned,
                         parallelism=f"replicas x{world}, q sharded, no collective on the data path"),
             roofline=roofline, e2e=e2e, cpu_baseline=cpu, gpu_launches=int(launches),
             clocks=clk.summary())

@@ -198,8 +198,8 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   return p;
 }
 
-size_t smem_budget(brx_handle* h) {
-  size_t b = 56 * 1024;
+size_t smem_budget(brx_handle* h, int which) {
+  size_t b = h->gather_budget[which];
   if (h->smem_optin && b > h->smem_optin) b = h->smem_optin;
   return b;
 }
@@ -394,8 +394,8 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     {
       GatherParams p = gather_params(h, h->vals, s, m, ir ? vmode : ROT_NONE, false, 0);
       p.out = vdst;
-      p.MB = gather_pick_modes(p, h->vals.store, h->vals.cplx, smem_budget(h));
-      h->launches += launch_gather(p, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h), cs);
+      p.MB = gather_pick_modes(p, h->vals.store, h->vals.cplx, smem_budget(h, 0));
+      h->launches += launch_gather(p, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h, 0), cs);
       h->launches += launch_residual(h, s, m, vdst, f32, cs);
     }
     if (ev[3]) cudaEventRecord(ev[3], cs);
@@ -404,8 +404,8 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       cdst = o_host ? static_cast<char*>(s.cbuf.p) : static_cast<char*>(vecs_out) + crow * (size_t)base;
       GatherParams p = gather_params(h, h->vecs, s, m, ir ? cmode : ROT_NONE, h->vecs.cplx, 1);
       p.out = cdst;
-      p.MB = gather_pick_modes(p, h->vecs.store, h->vecs.cplx, smem_budget(h));
-      h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h), cs);
+      p.MB = gather_pick_modes(p, h->vecs.store, h->vecs.cplx, smem_budget(h, 1));
+      h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h, 1), cs);
     }
     if (ev[4]) {
       cudaEventRecord(ev[4], cs);
@@ -898,6 +898,58 @@ brx_status brx_profile(brx_handle* h, int32_t enable) {
   h->stage_q = 0;
   h->stage_groups = 0;
   h->group_used = 0;
+  return BRX_OK;
+}
+
+// Times the gathers under each candidate shared-memory budget on a sample
+// query (stage events, best of reps) and keeps the fastest per data kind.
+brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, uint32_t flags, void* stream, int32_t reps) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!h->filled) return fail(h, BRX_ERR_NOT_FILLED, "The interpolation data must be filled before interpolating.");
+  if (!Q || n < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "a non-empty sample is needed");
+  if (reps < 1) reps = 1;
+  flags &= ~BRX_FLAG_ASYNC;
+  const bool f32 = flags & BRX_FLAG_OUT_F32;
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  DevBuf vo, co;
+  const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
+  const size_t crow = h->vecs.present ? (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32) : 0;
+  BRX_CUDA(h, vo.ensure(vrow * (size_t)n));
+  if (crow) {
+    cudaError_t e = co.ensure(crow * (size_t)n);
+    if (e != cudaSuccess) { vo.release(); return cuda_fail(h, e, "tune buffers"); }
+  }
+  const size_t cands[] = {24 * 1024, 32 * 1024, 40 * 1024, 56 * 1024, 72 * 1024, 96 * 1024, 128 * 1024, 160 * 1024};
+  brx_status st = BRX_OK;
+  for (int which = 0; which < 2 && !st; ++which) {
+    const Interp& d = which ? h->vecs : h->vals;
+    if (!d.present || !uses_groups(d, which ? d.cplx : false)) continue;
+    size_t best_b = h->gather_budget[which];
+    double best = 1e300;
+    for (size_t c : cands) {
+      if (c > h->smem_optin) continue;
+      h->gather_budget[which] = c;
+      double t = 1e300;
+      for (int r = 0; r < reps && !st; ++r) {
+        brx_profile(h, 1);
+        st = run_query(h, 1, Q, n, vo.p, crow ? co.p : nullptr, flags, stream, nullptr);
+        if (!st) t = std::min(t, h->stage_ms[2 + which]);
+      }
+      if (st) break;
+      if (t < best) { best = t; best_b = c; }
+    }
+    h->gather_budget[which] = best_b;
+  }
+  brx_profile(h, 0);
+  h->profile = false;
+  vo.release();
+  co.release();
+  return st;
+}
+
+brx_status brx_tuning(const brx_handle* h, int32_t* kb, int32_t n) {
+  if (!h || !kb || n < 1) return BRX_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < n && i < 2; ++i) kb[i] = (int32_t)(h->gather_budget[i] / 1024);
   return BRX_OK;
 }
 

@@ -101,6 +101,9 @@ struct brx_handle {
   brx_mlp_dims mlp_dims{};
   float mlp_omega_scale = 1.f, mlp_res_scale = 1.f, mlp_clip = 0.f;
   int mlp_groups = 1;  // warp groups per CTA of the inference kernel
+  // shared-memory budget per CTA of the values (0) and vectors (1) gathers
+  // (modes staged per block, hence CTAs per SM); brx_tune picks them
+  size_t gather_budget[2] = {56 * 1024, 56 * 1024};
   DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
@@ -117,7 +120,7 @@ int span(const Interp& d);
 brx_status rotation_mode(const Interp& d, int* mode, std::string* msg);
 brx::GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, long long n, int rot_mode,
                                 bool phase, int which);
-size_t smem_budget(brx_handle* h);
+size_t smem_budget(brx_handle* h, int which);
 size_t out_elem_bytes(const Interp& d, bool f32);
 brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, bool q_host);
 brx_status reset_errors(brx_handle* h, cudaStream_t s);

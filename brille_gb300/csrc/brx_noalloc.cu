@@ -157,14 +157,14 @@ extern "C" brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double*
   {
     brx::GatherParams gp = gather_params(h, h->vals, s, n, vmode, false, 0);
     gp.out = values_out;
-    gp.MB = brx::gather_pick_modes(gp, h->vals.store, h->vals.cplx, smem_budget(h));
-    h->launches += brx::launch_gather(gp, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h), cs);
+    gp.MB = brx::gather_pick_modes(gp, h->vals.store, h->vals.cplx, smem_budget(h, 0));
+    h->launches += brx::launch_gather(gp, h->vals.store, h->vals.cplx, f32, h->num_sms, smem_budget(h, 0), cs);
   }
   if (h->vecs.present) {
     brx::GatherParams gp = gather_params(h, h->vecs, s, n, cmode, h->vecs.cplx, 1);
     gp.out = vectors_out;
-    gp.MB = brx::gather_pick_modes(gp, h->vecs.store, h->vecs.cplx, smem_budget(h));
-    h->launches += brx::launch_gather(gp, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h), cs);
+    gp.MB = brx::gather_pick_modes(gp, h->vecs.store, h->vecs.cplx, smem_budget(h, 1));
+    h->launches += brx::launch_gather(gp, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h, 1), cs);
   }
   BRX_CUDA(h, cudaGetLastError());
   BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(brx::ErrorWord), cudaMemcpyDeviceToHost, cs));

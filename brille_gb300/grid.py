@@ -320,6 +320,21 @@ class _Grid:
         check(load().brx_stage_times(h, ms, 4, C.byref(q), C.byref(ng)), h)
         return list(ms), int(q.value), int(ng.value)
 
+    def tune(self, Q, *, out_f32=False, reps=2, stream=None):
+        """Pick the gathers' shared-memory budgets by timing a sample query
+        (brx_tune); returns the chosen budgets in KB (values, vectors)."""
+        h = self._handle()
+        flags = _abi.BRX_FLAG_OUT_F32 if out_f32 else 0
+        n = int(Q.shape[0])
+        check(load().brx_tune(h, _ptr(Q), n, flags, stream, int(reps)), h)
+        return self.tuning()
+
+    def tuning(self):
+        kb = (C.c_int32 * 2)()
+        h = self._handle()
+        check(load().brx_tuning(h, kb, 2), h)
+        return int(kb[0]), int(kb[1])
+
     def launch_count(self):
         return int(load().brx_launch_count(self._handle()))
 

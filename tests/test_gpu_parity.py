@@ -231,3 +231,16 @@ def test_fp32_screens_match_exact_predicates():
         del os.environ["BRX_EXACT_PREDICATES"]
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_tune_keeps_results():
+    """brx_tune changes launch shapes only: outputs are bit-identical."""
+    c = crystal_case("hex16")
+    g = _grid(c)
+    g.fill(c["w"], [1, 0, 0, 0, 3], c["v"], [0, 3 * c["model"].n_atoms, 0, 2, 1], storage="f32")
+    Q = _queries(c, 20000, seed=11)
+    v0, c0 = g.ir_interpolate_at(Q, out_f32=True)
+    kb = g.tune(Q, out_f32=True, reps=1)
+    assert kb[1] in (24, 32, 40, 56, 72, 96, 128, 160)
+    v1, c1 = g.ir_interpolate_at(Q, out_f32=True)
+    assert np.array_equal(v0, v1) and np.array_equal(c0, c1)
