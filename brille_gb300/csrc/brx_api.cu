@@ -235,6 +235,8 @@ brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, b
     std::snprintf(buf, sizeof buf, "Attempting to access null node for point Q = [%.17g %.17g %.17g]", qv[0], qv[1], qv[2]);
     return fail(h, BRX_ERR_NULL_NODE, buf);
   }
+  if (has(BRX_ERR_TIMEOUT))
+    return fail(h, BRX_ERR_TIMEOUT, "a bounded device-side wait ran out (learned residual); results are incomplete");
   if (has(BRX_ERR_NOT_FOUND)) {
     std::snprintf(buf, sizeof buf, "interpolate_at failed to find %d point%s", ew.count, ew.count > 1 ? "s." : ".");
     return fail(h, BRX_ERR_NOT_FOUND, buf);
@@ -709,6 +711,8 @@ void brx_destroy(brx_handle* h) {
   h->mlp_w.release();
   h->mlp_b.release();
   h->mlp_x.release();
+  h->mlp_wt.release();
+  h->mlp_bt.release();
   if (h->err) cudaFree(h->err);
   if (h->err_host) cudaFreeHost(h->err_host);
   delete h;

@@ -105,6 +105,8 @@ struct brx_handle {
   // (modes staged per block, hence CTAs per SM); brx_tune picks them
   size_t gather_budget[2] = {56 * 1024, 56 * 1024};
   DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
+  bool mlp_tc = false;         // dense layers on tcgen05 (else mma.sync)
+  DevBuf mlp_wt, mlp_bt;       // the tcgen05 kernel's weights (core-matrix order) and padded biases
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;

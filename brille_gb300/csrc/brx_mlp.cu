@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -479,9 +480,11 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
   __syncwarp();
 }
 
-// bf16 feature rows X (n × d_in, contiguous) of one sub-chunk: each thread
-// builds one row in shared memory, then the block writes its 128 rows as
-// 16-byte stores.
+// bf16 feature rows X of one sub-chunk in tiles of 128 rows, each tile in
+// the tensor cores' canonical K-major layout without swizzle: 8-row × 16-byte
+// core matrices, K-groups adjacent (128 B apart), 8-row groups d_in·16 B
+// apart.  Each thread builds one row in shared memory, then the block writes
+// its tile as contiguous 16-byte stores.
 constexpr int kRowsPerBlock = 128;
 
 __global__ void __launch_bounds__(kRowsPerBlock) mlp_xrows_kernel(DevGeom g, FeatureArgs a, __nv_bfloat16* X) {
@@ -498,11 +501,14 @@ __global__ void __launch_bounds__(kRowsPerBlock) mlp_xrows_kernel(DevGeom g, Fea
       for (int b = 0; b < a.B; ++b) feature_mode(a, i, b, put);
     }
     __syncthreads();
-    const int rows_here = (int)(a.n - r0 < kRowsPerBlock ? a.n - r0 : kRowsPerBlock);
-    const int chunks = d_in / 8;  // 16-byte pieces per row
-    for (int t = threadIdx.x; t < rows_here * chunks; t += kRowsPerBlock) {
-      const int r = t / chunks, c = t % chunks;
-      reinterpret_cast<uint4*>(X + (size_t)(r0 + r) * d_in)[c] = reinterpret_cast<const uint4*>(rows + (size_t)r * ss)[c];
+    // the whole tile (rows past n are zeros), 16-byte pieces in core-matrix
+    // order: piece t = ((row/8)·(d_in/8) + k/8)·8 + row%8
+    const int chunks = d_in / 8;
+    uint4* dst = reinterpret_cast<uint4*>(X + (size_t)r0 * d_in);
+    for (int t = threadIdx.x; t < kRowsPerBlock * chunks; t += kRowsPerBlock) {
+      const int r8 = t & 7, gc = t >> 3;
+      const int r = (gc / chunks) * 8 + r8, c = gc % chunks;
+      dst[t] = reinterpret_cast<const uint4*>(rows + (size_t)r * ss)[c];
     }
     __syncthreads();
   }
@@ -511,7 +517,7 @@ __global__ void __launch_bounds__(kRowsPerBlock) mlp_xrows_kernel(DevGeom g, Fea
 size_t xrows_smem(int d_in) { return (size_t)kRowsPerBlock * stage_stride(d_in) * 2; }
 
 struct InferArgs {
-  const __nv_bfloat16* X;  // n × d_in feature rows
+  const __nv_bfloat16* X;  // feature rows, tiles of 128 rows in core-matrix order
   const int32_t* status;   // n
   long long n;
   int d_in, B;
@@ -599,10 +605,8 @@ mlp_infer_kernel(InferArgs a) {
   auto stage_tile = [&](long long tile) {
     for (int t = gt; t < kInferRows * chunks; t += kGroupThreads) {
       const int r = t / chunks, c = t % chunks;
-      const long long i = tile * kInferRows + r;
       __nv_bfloat16* d = stage + (size_t)r * ss + 8 * c;
-      if (i < a.n) cp_async16(smem_u32(d), a.X + (size_t)i * d_in + 8 * c);
-      else *reinterpret_cast<uint4*>(d) = make_uint4(0u, 0u, 0u, 0u);
+      cp_async16(smem_u32(d), a.X + (size_t)tile * kInferRows * d_in + (((r >> 3) * chunks + c) << 6) + ((r & 7) << 3));
     }
     cp_async_commit();
   };
@@ -633,6 +637,275 @@ mlp_infer_kernel(InferArgs a) {
     __syncwarp();
   }
   cp_async_wait_all();
+}
+
+// ---------------------------------------------------------------------------
+// inference on tcgen05: accumulators in tensor memory
+// ---------------------------------------------------------------------------
+// Per CTA two slots of 4 warps, each taking 128-q tiles on its own: the
+// tile's feature rows arrive by one bulk copy (cp.async.bulk, completion on
+// an mbarrier) already in the canonical K-major core-matrix layout; for
+// every layer one elected thread issues K/16 tcgen05.mma (M 128, N 128 or
+// 16, bf16 × bf16 → FP32 in tensor memory) and commits them to the slot's
+// mbarrier; the slot's 128 threads then read their row of the accumulator
+// (tcgen05.ld 32x32b, warp w owns lanes 32(w mod 4)…), add the bias, apply
+// GELU and write the bf16 row into the other activation buffer, again in
+// core-matrix order, for the next layer's A operand.  While one slot runs
+// its epilogue the other slot's MMAs keep the tensor core busy.  The next
+// tile's bulk copy is issued as soon as layer 2 has read buffer 0.
+// Every wait is bounded (about a second of clock cycles): on expiry the slot
+// records BRX_ERR_TIMEOUT, leaves its loop together (barrier with an AND
+// reduction), waits for its own copy in flight and the CTA frees its tensor
+// memory.
+constexpr int kTcSlots = 2;
+constexpr int kTcThreads = 128 * kTcSlots;
+constexpr int kTcCols = 128 * kTcSlots;        // tensor-memory columns per CTA
+constexpr long long kSpinCycles = 2000000000LL;
+
+struct TcSmem {
+  size_t w_off[4];
+  int n_rows[4];   // output rows of each layer (the last padded to 16)
+  size_t w_bytes, bias_off, slot_off, buf_bytes, mbar_off, tmem_off, total;
+};
+
+__host__ __device__ inline int tc_out_pad(int n_out) { return (n_out + 15) / 16 * 16; }
+
+__host__ __device__ inline TcSmem tc_smem(int d_in, int n_out) {
+  TcSmem S;
+  const int K[4] = {d_in, kWidth, kWidth, kWidth};
+  const int N[4] = {kWidth, kWidth, kWidth, tc_out_pad(n_out)};
+  size_t o = 0;
+  for (int l = 0; l < 4; ++l) {
+    S.w_off[l] = o;
+    S.n_rows[l] = N[l];
+    o += (size_t)N[l] * K[l] * 2;
+  }
+  S.w_bytes = o;
+  o = (o + 127) & ~size_t(127);
+  S.bias_off = o;
+  o += (size_t)(3 * kWidth + tc_out_pad(n_out)) * 4;
+  o = (o + 127) & ~size_t(127);
+  S.slot_off = o;
+  S.buf_bytes = (size_t)kInferRows * (d_in > kWidth ? d_in : kWidth) * 2;
+  o += S.buf_bytes * 2 * kTcSlots;
+  S.mbar_off = o;
+  o += 8 * 2 * kTcSlots;
+  S.tmem_off = o;
+  o += 16;
+  S.total = o;
+  return S;
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle; lbo = byte distance
+// of core matrices adjacent along K, sbo = along M / N
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+// instruction descriptor, kind::f16: FP32 accumulator, bf16 A and B, both K-major
+__device__ __forceinline__ uint32_t tc_idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(mbar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mbar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t phase) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(mbar), "r"(phase)
+      : "memory");
+  return done != 0;
+}
+// bounded wait for the completion of phase `phase`
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+  const long long t0 = clock64();
+  while (!mbar_try(mbar, phase))
+    if (clock64() - t0 > kSpinCycles) return false;
+  return true;
+}
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+// AND of pred over the slot's 128 threads (named barrier 1 + slot)
+__device__ __forceinline__ bool slot_all(int slot, bool pred) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.b32 p, %1, 0;\n"
+      " barrier.cta.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)pred), "r"(1 + slot), "n"(128)
+      : "memory");
+  return r != 0;
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+struct TcArgs {
+  const __nv_bfloat16* X;   // tiles of 128 feature rows, core-matrix order
+  const int32_t* status;
+  long long n;
+  int d_in, n_out, B;
+  const uint4* Wt;          // the four layers' weights, core-matrix order (layer 3 padded to 16 rows)
+  const float* bias;        // 3·128 + pad(n_out) biases (bf16-rounded values)
+  float res_scale, clip;
+  void* values_out;
+  int out_f64;
+  ErrorWord* err;
+};
+
+__global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const TcSmem S = tc_smem(a.d_in, a.n_out);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int slot = tid / 128, st = tid % 128, wq = warp & 3;
+  float* sb = reinterpret_cast<float*>(sm + S.bias_off);
+  for (int i = tid; i < (int)(S.w_bytes / 16); i += kTcThreads) reinterpret_cast<uint4*>(sm)[i] = a.Wt[i];
+  for (int i = tid; i < 3 * kWidth + tc_out_pad(a.n_out); i += kTcThreads) sb[i] = a.bias[i];
+  const uint32_t mbar_mma = smem_u32(sm + S.mbar_off) + 16 * slot;
+  const uint32_t mbar_x = mbar_mma + 8;
+  if (tid == 0) {
+    for (int s = 0; s < kTcSlots; ++s) {
+      mbar_init(smem_u32(sm + S.mbar_off) + 16 * s, 1);
+      mbar_init(smem_u32(sm + S.mbar_off) + 16 * s + 8, 1);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(sm + S.tmem_off)),
+                 "n"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_proxy_async();  // weights written by this CTA are read by the tensor core
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t*>(sm + S.tmem_off);
+  const uint32_t tmem_d = tmem_base + 128 * slot;
+  unsigned char* buf0 = sm + S.slot_off + 2 * S.buf_bytes * slot;
+  unsigned char* buf1 = buf0 + S.buf_bytes;
+  const int B = a.B;
+  const long long n_tiles = (a.n + kInferRows - 1) / kInferRows;
+  const long long step = (long long)gridDim.x * kTcSlots;
+  const uint32_t tile_bytes = (uint32_t)kInferRows * a.d_in * 2;
+  const bool issuer = st == 0;
+  uint32_t ph_mma = 0, ph_x = 0;
+  bool x_pending = false;
+  long long tile = (long long)blockIdx.x * kTcSlots + slot;
+  if (issuer && tile < n_tiles) {
+    mbar_expect_tx(mbar_x, tile_bytes);
+    bulk_load(smem_u32(buf0), a.X + (size_t)tile * kInferRows * a.d_in, tile_bytes, mbar_x);
+    x_pending = true;
+  }
+  bool ok = true;
+  const int row = wq * 32 + lane;
+  const uint32_t taddr = tmem_d + ((uint32_t)(wq * 32) << 16);
+  for (; tile < n_tiles && ok; tile += step) {
+    for (int l = 0; l < 4 && ok; ++l) {
+      const unsigned char* A = (l & 1) ? buf1 : buf0;
+      unsigned char* O = (l & 1) ? buf0 : buf1;
+      const int K = l == 0 ? a.d_in : kWidth, N = S.n_rows[l];
+      bool good = true;
+      if (issuer) {
+        if (l == 0) {
+          good = mbar_wait(mbar_x, ph_x);
+          ph_x ^= 1;
+          x_pending = !good;
+        }
+        tc_fence_after();
+        if (good) {
+          const uint32_t a0 = smem_u32(A), b0 = smem_u32(sm + S.w_off[l]);
+          const uint32_t idesc = tc_idesc(kInferRows, N);
+          for (int k = 0; k < K / 16; ++k)
+            tc_mma(tmem_d, tc_desc(a0 + 256 * k, 128, 16 * K), tc_desc(b0 + 256 * k, 128, 16 * K), idesc, k > 0);
+          tc_commit(mbar_mma);
+        }
+      }
+      good = mbar_wait(mbar_mma, ph_mma) && good;
+      ph_mma ^= 1;
+      tc_fence_after();
+      if (l == 2 && issuer && good && tile + step < n_tiles) {
+        // layer 2 has read buffer 0: the next tile's rows go there now
+        mbar_expect_tx(mbar_x, tile_bytes);
+        bulk_load(smem_u32(buf0), a.X + (size_t)(tile + step) * kInferRows * a.d_in, tile_bytes, mbar_x);
+        x_pending = true;
+      }
+      if (good) {
+        if (l < 3) {
+          const float* bl = sb + kWidth * l;
+#pragma unroll 1
+          for (int c = 0; c < kWidth / 16; ++c) {
+            float v[16];
+            tmem_ld16(taddr + 16 * c, v);
+            uint32_t pk[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              pk[j] = pack_bf16(gelu(v[2 * j] + bl[16 * c + 2 * j]), gelu(v[2 * j + 1] + bl[16 * c + 2 * j + 1]));
+            // row `row`, K-groups 2c and 2c+1 of a 128-wide K-major operand
+            unsigned char* dst = O + (size_t)(((row >> 3) * (kWidth / 8) + 2 * c) * 128 + (row & 7) * 16);
+            *reinterpret_cast<uint4*>(dst) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            *reinterpret_cast<uint4*>(dst + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+          }
+          fence_proxy_async();
+        } else {
+          float v[16];
+          tmem_ld16(taddr, v);
+          const long long i = tile * kInferRows + row;
+          if (i < a.n && !a.status[i]) {
+            const float* bl = sb + 3 * kWidth;
+            for (int b = 0; b < B && b < 16; ++b) {
+              const float res = (v[b] + bl[b]) * a.res_scale;
+              if (a.clip > 0.f && !(fabsf(res) <= a.clip)) continue;
+              if (a.out_f64) static_cast<double*>(a.values_out)[i * B + b] += (double)res;
+              else static_cast<float*>(a.values_out)[i * B + b] += res;
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      ok = slot_all(slot, good);
+    }
+  }
+  if (!ok && st == 0) {
+    atomicOr(&a.err->flags, 1 << BRX_ERR_TIMEOUT);
+    atomicAdd(&a.err->count, 1);
+  }
+  if (issuer && x_pending) mbar_wait(mbar_x, ph_x);  // no copy may land after exit
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_base), "n"(kTcCols) : "memory");
+  }
 }
 
 }  // namespace brx
@@ -783,6 +1056,31 @@ brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const fl
   BRX_CUDA(h, h->mlp_b.ensure(b.size() * sizeof(float)));
   BRX_CUDA(h, cudaMemcpy(h->mlp_w.p, W.data(), W.size() * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice));
   BRX_CUDA(h, cudaMemcpy(h->mlp_b.p, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // the tcgen05 kernel's operands: weights in core-matrix order (layer 3
+  // padded to 16 rows), biases padded alike
+  {
+    const brx::TcSmem T = brx::tc_smem(d->d_in, d->n_out);
+    const char* env = std::getenv("BRX_MLP_KERNEL");
+    h->mlp_tc = T.total <= h->smem_optin && !(env && std::strcmp(env, "mma") == 0);
+    if (h->mlp_tc) {
+      std::vector<__nv_bfloat16> Wt(T.w_bytes / 2, __float2bfloat16_rn(0.f));
+      for (int l = 0; l < 4; ++l) {
+        const int K = L.in[l];
+        for (int nrow = 0; nrow < L.out[l]; ++nrow)
+          for (int k = 0; k < K; ++k)
+            Wt[T.w_off[l] / 2 + ((size_t)(nrow >> 3) * (K / 8) + (k >> 3)) * 64 + (nrow & 7) * 8 + (k & 7)] =
+                __float2bfloat16_rn(params[L.W[l] + (long long)nrow * K + k]);
+      }
+      std::vector<float> bt(3 * brx::kWidth + brx::tc_out_pad(d->n_out), 0.f);
+      for (int t = 0; t < 3 * brx::kWidth + d->n_out; ++t) bt[t] = b[t];
+      BRX_CUDA(h, h->mlp_wt.ensure(T.w_bytes));
+      BRX_CUDA(h, h->mlp_bt.ensure(bt.size() * sizeof(float)));
+      BRX_CUDA(h, cudaMemcpy(h->mlp_wt.p, Wt.data(), T.w_bytes, cudaMemcpyHostToDevice));
+      BRX_CUDA(h, cudaMemcpy(h->mlp_bt.p, bt.data(), bt.size() * sizeof(float), cudaMemcpyHostToDevice));
+      BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)T.total));
+    }
+  }
   const int groups = brx::infer_smem(d->d_in, d->n_out, 2).total <= h->smem_optin ? 2 : 1;
   const size_t smem = brx::infer_smem(d->d_in, d->n_out, groups).total;
   BRX_CUDA(h, cudaFuncSetAttribute(brx::mlp_infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -832,8 +1130,27 @@ int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_o
     a.values_out = static_cast<char*>(values_out) + out_row * (size_t)off;
     a.out_f64 = !out_f32;
     const long long tiles = (m + brx::kInferRows - 1) / brx::kInferRows;
-    const long long grid = std::min<long long>((tiles + groups - 1) / groups, (long long)h->num_sms);
-    brx::mlp_infer_kernel<<<(unsigned)grid, brx::kGroupThreads * groups, smem, cs>>>(a);
+    if (h->mlp_tc) {
+      brx::TcArgs t{};
+      t.X = X;
+      t.status = a.status;
+      t.n = m;
+      t.d_in = d_in;
+      t.n_out = a.n_out;
+      t.B = B;
+      t.Wt = static_cast<const uint4*>(h->mlp_wt.p);
+      t.bias = static_cast<const float*>(h->mlp_bt.p);
+      t.res_scale = a.res_scale;
+      t.clip = a.clip;
+      t.values_out = a.values_out;
+      t.out_f64 = a.out_f64;
+      t.err = h->err;
+      const long long grid = std::min<long long>((tiles + brx::kTcSlots - 1) / brx::kTcSlots, (long long)h->num_sms);
+      brx::mlp_infer_tc_kernel<<<(unsigned)grid, brx::kTcThreads, brx::tc_smem(d_in, a.n_out).total, cs>>>(t);
+    } else {
+      const long long grid = std::min<long long>((tiles + groups - 1) / groups, (long long)h->num_sms);
+      brx::mlp_infer_kernel<<<(unsigned)grid, brx::kGroupThreads * groups, smem, cs>>>(a);
+    }
     launches += 2;
   }
   return launches;
