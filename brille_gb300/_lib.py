@@ -97,7 +97,7 @@ def load(build_if_missing=True):
     lib.brx_batch_launch_count.restype = C.c_int64
     lib.brx_batch_last_error.argtypes = [bp]
     lib.brx_batch_last_error.restype = C.c_char_p
-    lib.brx_tune.argtypes = [h, C.c_void_p, C.c_int64, C.c_uint32, C.c_void_p, C.c_int32]
+    lib.brx_tune.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]
     lib.brx_tune.restype = C.c_int
     lib.brx_tuning.argtypes = [h, C.POINTER(C.c_int32), C.c_int32]
     lib.brx_tuning.restype = C.c_int

@@ -907,7 +907,8 @@ brx_status brx_profile(brx_handle* h, int32_t enable) {
 
 // Times the gathers under each candidate shared-memory budget on a sample
 // query (stage events, best of reps) and keeps the fastest per data kind.
-brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, uint32_t flags, void* stream, int32_t reps) {
+brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out, uint32_t flags,
+                    void* stream, int32_t reps) {
   if (!h) return BRX_ERR_INVALID_ARGUMENT;
   if (!h->filled) return fail(h, BRX_ERR_NOT_FILLED, "The interpolation data must be filled before interpolating.");
   if (!Q || n < 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "a non-empty sample is needed");
@@ -915,13 +916,20 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, uint32_t flags, v
   flags &= ~BRX_FLAG_ASYNC;
   const bool f32 = flags & BRX_FLAG_OUT_F32;
   BRX_CUDA(h, cudaSetDevice(h->device));
+  // the caller's output buffers, or temporary ones
   DevBuf vo, co;
   const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
   const size_t crow = h->vecs.present ? (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32) : 0;
-  BRX_CUDA(h, vo.ensure(vrow * (size_t)n));
-  if (crow) {
+  void* vp = values_out;
+  void* cp = vectors_out;
+  if (!vp) {
+    BRX_CUDA(h, vo.ensure(vrow * (size_t)n));
+    vp = vo.p;
+  }
+  if (crow && !cp) {
     cudaError_t e = co.ensure(crow * (size_t)n);
     if (e != cudaSuccess) { vo.release(); return cuda_fail(h, e, "tune buffers"); }
+    cp = co.p;
   }
   const size_t cands[] = {24 * 1024, 32 * 1024, 40 * 1024, 56 * 1024, 72 * 1024, 96 * 1024, 128 * 1024, 160 * 1024};
   brx_status st = BRX_OK;
@@ -936,7 +944,7 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, uint32_t flags, v
       double t = 1e300;
       for (int r = 0; r < reps && !st; ++r) {
         brx_profile(h, 1);
-        st = run_query(h, 1, Q, n, vo.p, crow ? co.p : nullptr, flags, stream, nullptr);
+        st = run_query(h, 1, Q, n, vp, crow ? cp : nullptr, flags, stream, nullptr);
         if (!st) t = std::min(t, h->stage_ms[2 + which]);
       }
       if (st) break;

@@ -320,13 +320,14 @@ class _Grid:
         check(load().brx_stage_times(h, ms, 4, C.byref(q), C.byref(ng)), h)
         return list(ms), int(q.value), int(ng.value)
 
-    def tune(self, Q, *, out_f32=False, reps=2, stream=None):
+    def tune(self, Q, *, out_f32=False, reps=2, stream=None, values_out=None, vectors_out=None):
         """Pick the gathers' shared-memory budgets by timing a sample query
-        (brx_tune); returns the chosen budgets in KB (values, vectors)."""
+        (brx_tune), into the given output buffers or temporary ones; returns
+        the chosen budgets in KB (values, vectors)."""
         h = self._handle()
         flags = _abi.BRX_FLAG_OUT_F32 if out_f32 else 0
         n = int(Q.shape[0])
-        check(load().brx_tune(h, _ptr(Q), n, flags, stream, int(reps)), h)
+        check(load().brx_tune(h, _ptr(Q), n, _ptr(values_out), _ptr(vectors_out), flags, stream, int(reps)), h)
         return self.tuning()
 
     def tuning(self):
