@@ -1,6 +1,6 @@
 // Learned residual correction of interpolated eigenvalues.
 //
-// A small MLP (d_in → 128 → 128 → 128 → n_out, GELU) predicts, per mode, the
+// A small MLP (d_in → 128 → 128 → 128 → n_out, tanh-form GELU) predicts, per mode, the
 // difference between the exact eigenvalue and the trellis interpolation at
 // q.  Its input row is built on the GPU from the locate record of q:
 //
@@ -40,27 +40,28 @@ namespace brx {
 constexpr int kWidth = 128;
 
 __device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
-// erf by Abramowitz & Stegun 7.1.26 (|error| ≤ 1.5e-7 in exact arithmetic,
-// 6e-7 in FP32 over [-6, 6]): one reciprocal and
-// one exponential on the special-function unit instead of a full-precision
-// erf, for the 3·128 activations of every q.  Training and inference share
-// it, so the network is trained on the function it is evaluated with.
-__device__ __forceinline__ float erf_as(float x) {
-  const float ax = fabsf(x);
-  const float t = __frcp_rn(fmaf(0.3275911f, ax, 1.f));
-  float p = fmaf(1.061405429f, t, -1.453152027f);
-  p = fmaf(p, t, 1.421413741f);
-  p = fmaf(p, t, -0.284496736f);
-  p = fmaf(p, t, 0.254829592f);
-  p *= t;
-  const float y = 1.f - p * __expf(-ax * ax);
-  return copysignf(y, x);
+// GELU in its tanh form, 0.5·x·(1 + tanh(√(2/π)·(x + 0.044715·x³))).
+// Training evaluates tanh accurately; inference uses the special-function
+// unit's tanh.approx (relative error about 2⁻¹¹, below the bf16 rounding of
+// the activations), one instruction where an erf costs a dozen.
+constexpr float kGeluC = 0.7978845608028654f, kGeluA = 0.044715f;
+__device__ __forceinline__ float gelu(float x) {
+  const float u = kGeluC * fmaf(kGeluA * x * x, x, x);
+  return 0.5f * x * (1.f + tanhf(u));
 }
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erf_as(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.f + erf_as(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanhf(kGeluC * fmaf(kGeluA * x2, x, x));
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * kGeluC * fmaf(3.f * kGeluA, x2, 1.f);
+}
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;\n" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_fast(float x) {
+  const float h = 0.5f * x;
+  return fmaf(h, tanh_approx(kGeluC * fmaf(kGeluA * x * x, x, x)), h);
 }
 
 // Offsets of the parameter blocks in the flat FP32 parameter vector:
@@ -463,9 +464,9 @@ __device__ __forceinline__ void warp_layer(const __nv_bfloat16* Wl, int in, int 
     if (kHidden) {
       const float b0 = bl[c0], b1 = bl[c0 + 1];
       *reinterpret_cast<uint32_t*>(dst + (size_t)(row0 + g) * ds + c0) =
-          pack_bf16(gelu(acc[t][0] + b0), gelu(acc[t][1] + b1));
+          pack_bf16(gelu_fast(acc[t][0] + b0), gelu_fast(acc[t][1] + b1));
       *reinterpret_cast<uint32_t*>(dst + (size_t)(row0 + g + 8) * ds + c0) =
-          pack_bf16(gelu(acc[t][2] + b0), gelu(acc[t][3] + b1));
+          pack_bf16(gelu_fast(acc[t][2] + b0), gelu_fast(acc[t][3] + b1));
     } else {
       if (c0 < n_valid) {
         out[(row0 + g) * out_ld + c0] = acc[t][0] + bl[c0];
@@ -642,24 +643,25 @@ mlp_infer_kernel(InferArgs a) {
 // ---------------------------------------------------------------------------
 // inference on tcgen05: accumulators in tensor memory
 // ---------------------------------------------------------------------------
-// Per CTA two slots of 4 warps, each taking 128-q tiles on its own: the
+// Per CTA four slots of 4 warps, each taking 128-q tiles on its own: the
 // tile's feature rows arrive by one bulk copy (cp.async.bulk, completion on
 // an mbarrier) already in the canonical K-major core-matrix layout; for
 // every layer one elected thread issues K/16 tcgen05.mma (M 128, N 128 or
-// 16, bf16 × bf16 → FP32 in tensor memory) and commits them to the slot's
-// mbarrier; the slot's 128 threads then read their row of the accumulator
-// (tcgen05.ld 32x32b, warp w owns lanes 32(w mod 4)…), add the bias, apply
-// GELU and write the bf16 row into the other activation buffer, again in
-// core-matrix order, for the next layer's A operand.  While one slot runs
-// its epilogue the other slot's MMAs keep the tensor core busy.  The next
-// tile's bulk copy is issued as soon as layer 2 has read buffer 0.
+// 16, bf16 × bf16 → FP32 in tensor memory, 128 columns per slot) and
+// commits them to the slot's mbarrier; the slot's 128 threads then read
+// their row of the accumulator (tcgen05.ld 32x32b, warp w owns lanes
+// 32(w mod 4)…), add the bias, apply GELU and write the bf16 row back into
+// the slot's one activation buffer (the MMA has finished reading it), in
+// core-matrix order, as the next layer's A operand.  While one slot runs its
+// epilogue the other slots' MMAs keep the tensor core busy.  The next tile's
+// bulk copy is issued as soon as layer 3 has read the buffer.
 // Every wait is bounded (about a second of clock cycles): on expiry the slot
 // records BRX_ERR_TIMEOUT, leaves its loop together (barrier with an AND
 // reduction), waits for its own copy in flight and the CTA frees its tensor
 // memory.
-constexpr int kTcSlots = 2;
+constexpr int kTcSlots = 4;
 constexpr int kTcThreads = 128 * kTcSlots;
-constexpr int kTcCols = 128 * kTcSlots;        // tensor-memory columns per CTA
+constexpr int kTcCols = 128 * kTcSlots;        // tensor-memory columns per CTA (all 512)
 constexpr long long kSpinCycles = 2000000000LL;
 
 struct TcSmem {
@@ -687,7 +689,7 @@ __host__ __device__ inline TcSmem tc_smem(int d_in, int n_out) {
   o = (o + 127) & ~size_t(127);
   S.slot_off = o;
   S.buf_bytes = (size_t)kInferRows * (d_in > kWidth ? d_in : kWidth) * 2;
-  o += S.buf_bytes * 2 * kTcSlots;
+  o += S.buf_bytes * kTcSlots;
   S.mbar_off = o;
   o += 8 * 2 * kTcSlots;
   S.tmem_off = o;
@@ -770,6 +772,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
 }
 
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,"
+      "%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
 struct TcArgs {
   const __nv_bfloat16* X;   // tiles of 128 feature rows, core-matrix order
   const int32_t* status;
@@ -812,8 +830,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
   tc_fence_after();
   const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t*>(sm + S.tmem_off);
   const uint32_t tmem_d = tmem_base + 128 * slot;
-  unsigned char* buf0 = sm + S.slot_off + 2 * S.buf_bytes * slot;
-  unsigned char* buf1 = buf0 + S.buf_bytes;
+  unsigned char* buf = sm + S.slot_off + S.buf_bytes * slot;
   const int B = a.B;
   const long long n_tiles = (a.n + kInferRows - 1) / kInferRows;
   const long long step = (long long)gridDim.x * kTcSlots;
@@ -824,7 +841,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
   long long tile = (long long)blockIdx.x * kTcSlots + slot;
   if (issuer && tile < n_tiles) {
     mbar_expect_tx(mbar_x, tile_bytes);
-    bulk_load(smem_u32(buf0), a.X + (size_t)tile * kInferRows * a.d_in, tile_bytes, mbar_x);
+    bulk_load(smem_u32(buf), a.X + (size_t)tile * kInferRows * a.d_in, tile_bytes, mbar_x);
     x_pending = true;
   }
   bool ok = true;
@@ -832,8 +849,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
   const uint32_t taddr = tmem_d + ((uint32_t)(wq * 32) << 16);
   for (; tile < n_tiles && ok; tile += step) {
     for (int l = 0; l < 4 && ok; ++l) {
-      const unsigned char* A = (l & 1) ? buf1 : buf0;
-      unsigned char* O = (l & 1) ? buf0 : buf1;
       const int K = l == 0 ? a.d_in : kWidth, N = S.n_rows[l];
       bool good = true;
       if (issuer) {
@@ -844,7 +859,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
         }
         tc_fence_after();
         if (good) {
-          const uint32_t a0 = smem_u32(A), b0 = smem_u32(sm + S.w_off[l]);
+          const uint32_t a0 = smem_u32(buf), b0 = smem_u32(sm + S.w_off[l]);
           const uint32_t idesc = tc_idesc(kInferRows, N);
           for (int k = 0; k < K / 16; ++k)
             tc_mma(tmem_d, tc_desc(a0 + 256 * k, 128, 16 * K), tc_desc(b0 + 256 * k, 128, 16 * K), idesc, k > 0);
@@ -854,27 +869,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
       good = mbar_wait(mbar_mma, ph_mma) && good;
       ph_mma ^= 1;
       tc_fence_after();
-      if (l == 2 && issuer && good && tile + step < n_tiles) {
-        // layer 2 has read buffer 0: the next tile's rows go there now
+      if (l == 3 && issuer && good && tile + step < n_tiles) {
+        // layer 3 has read the buffer: the next tile's rows go there now
         mbar_expect_tx(mbar_x, tile_bytes);
-        bulk_load(smem_u32(buf0), a.X + (size_t)(tile + step) * kInferRows * a.d_in, tile_bytes, mbar_x);
+        bulk_load(smem_u32(buf), a.X + (size_t)(tile + step) * kInferRows * a.d_in, tile_bytes, mbar_x);
         x_pending = true;
       }
       if (good) {
         if (l < 3) {
           const float* bl = sb + kWidth * l;
 #pragma unroll 1
-          for (int c = 0; c < kWidth / 16; ++c) {
-            float v[16];
-            tmem_ld16(taddr + 16 * c, v);
-            uint32_t pk[8];
+          for (int c = 0; c < kWidth / 32; ++c) {
+            float v[32];
+            tmem_ld32(taddr + 32 * c, v);
+            uint32_t pk[16];
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-              pk[j] = pack_bf16(gelu(v[2 * j] + bl[16 * c + 2 * j]), gelu(v[2 * j + 1] + bl[16 * c + 2 * j + 1]));
-            // row `row`, K-groups 2c and 2c+1 of a 128-wide K-major operand
-            unsigned char* dst = O + (size_t)(((row >> 3) * (kWidth / 8) + 2 * c) * 128 + (row & 7) * 16);
-            *reinterpret_cast<uint4*>(dst) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-            *reinterpret_cast<uint4*>(dst + 128) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            for (int j = 0; j < 16; ++j)
+              pk[j] = pack_bf16(gelu_fast(v[2 * j] + bl[32 * c + 2 * j]),
+                                gelu_fast(v[2 * j + 1] + bl[32 * c + 2 * j + 1]));
+            // row `row`, K-groups 4c … 4c+3 of a 128-wide K-major operand
+            unsigned char* dst = buf + (size_t)(((row >> 3) * (kWidth / 8) + 4 * c) * 128 + (row & 7) * 16);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              *reinterpret_cast<uint4*>(dst + 128 * q) = make_uint4(pk[4 * q], pk[4 * q + 1], pk[4 * q + 2], pk[4 * q + 3]);
           }
           fence_proxy_async();
         } else {

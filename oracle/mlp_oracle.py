@@ -6,9 +6,9 @@ smoke check and by bench.py's CPU baseline, never by the product path.
 
 The reference has no learned part, so there is no reference code to follow.
 This file restates the network that include/brx.h defines (d_in → 128 → 128
-→ 128 → n_out, exact-erf GELU, mean squared error over the first n_modes
-outputs; the device evaluates erf by Abramowitz & Stegun 7.1.26, which in
-FP32 stays within 6e-7 of the exact erf used here).  It is pinned two ways: its analytic gradients agree with central
+→ 128 → n_out, GELU in its tanh form, mean squared error over the first
+n_modes outputs; the device's inference evaluates tanh with the
+special-function unit's approximation, about 2^-11 relative).  It is pinned two ways: its analytic gradients agree with central
 finite differences in FP64 (tests/test_mlp_oracle.py), and its feature base
 column equals the C oracle's own interpolated eigenvalues.
 
@@ -64,21 +64,18 @@ def init_params(d_in, n_out, seed=0):
     return p
 
 
-def _erf(x):
-    try:
-        from scipy.special import erf
-        return erf(x)
-    except ImportError:  # pragma: no cover
-        import math
-        return np.vectorize(math.erf)(x)
+GELU_C = np.sqrt(2.0 / np.pi)
+GELU_A = 0.044715
 
 
 def gelu(x):
-    return 0.5 * x * (1.0 + _erf(x / np.sqrt(2.0)))
+    """GELU in its tanh form."""
+    return 0.5 * x * (1.0 + np.tanh(GELU_C * (x + GELU_A * x ** 3)))
 
 
 def gelu_grad(x):
-    return 0.5 * (1.0 + _erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(GELU_C * (x + GELU_A * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * GELU_C * (1.0 + 3.0 * GELU_A * x * x)
 
 
 def forward(params, X, d_in, n_out, rounding=True):
