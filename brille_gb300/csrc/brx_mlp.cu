@@ -105,68 +105,81 @@ struct FeatureArgs {
   float inv_omega;         // 1 / omega_scale
 };
 
-__device__ __forceinline__ float vertex_value(const FeatureArgs& a, long long v, int b) {
-  return a.values_f64 ? (float)static_cast<const double*>(a.values)[v * a.B + b]
-                      : static_cast<const float*>(a.values)[v * a.B + b];
-}
 
 // Feature arithmetic is FP32 with explicit rounding (no contraction), so
 // that the oracle repeats it bit for bit; the rows are rounded to bf16 for
 // the network anyway.
-
-// Columns of q i's row that do not depend on the mode: position in the node
-// cell (0-2), slot weights (3-10), tetrahedron flag (11), position in the
-// trellis box (12 + 9B + 0..2).  The caller has checked status[i] == 0.
-template <class Put>
-__device__ void feature_head(const DevGeom& g, const FeatureArgs& a, long long i, Put put) {
-  const long long node = a.node[2 * i];
-  const long long nx = g.n_knots[0] - 1, ny = g.n_knots[1] - 1;
-  const int sub[3] = {(int)(node % nx), (int)((node / nx) % ny), (int)(node / (nx * ny))};
+//
+// The whole row of q i through put(col, value) (the caller zeroes the row
+// first and has checked status[i] == 0): position in the node cell (0-2),
+// slot weights (3-10), tetrahedron flag (11), vertex eigenvalues
+// (12 + slot·B + mode), interpolated eigenvalues Σ w·v in slot order
+// (12 + 8B + mode, also returned through base unscaled: the FP32 gather's
+// own result for FP32 storage), position in the trellis box (12 + 9B + 0..2).
+// The record's vertex ids and weights are read once, as vectors.
+template <typename VT, class Put>
+__device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs& a, long long i, Put put,
+                                            float* base) {
+  const int node = a.node[2 * i], tet = a.node[2 * i + 1];
+  const int nx = g.n_knots[0] - 1, ny = g.n_knots[1] - 1;
+  const int rest = node / nx;
+  const int sub[3] = {node - rest * nx, rest % ny, rest / ny};
   const float q0 = (float)a.q_ir[3 * i], q1 = (float)a.q_ir[3 * i + 1], q2 = (float)a.q_ir[3 * i + 2];
   float x[3];
+#pragma unroll
   for (int d = 0; d < 3; ++d)
     x[d] = __fadd_rn(__fadd_rn(__fmul_rn((float)g.outer_B[d], q0), __fmul_rn((float)g.outer_B[3 + d], q1)),
                      __fmul_rn((float)g.outer_B[6 + d], q2));
+  const int B = a.B;
+#pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const float lo = (float)g.knots[d][sub[d]], hi = (float)g.knots[d][sub[d] + 1];
+    const double* kn = g.knots[d];
+    const float lo = (float)kn[sub[d]], hi = (float)kn[sub[d] + 1];
     put(d, __fdiv_rn(__fsub_rn(x[d], lo), __fsub_rn(hi, lo)));
+    const float lo0 = (float)kn[0], hi0 = (float)kn[g.n_knots[d] - 1];
+    put(12 + 9 * B + d, __fdiv_rn(__fsub_rn(x[d], lo0), __fsub_rn(hi0, lo0)));
   }
   const int nw = min(a.nw[i], 8);
-  for (int k = 0; k < nw; ++k) put(3 + k, (float)a.w[8 * i + k]);
-  put(11, a.node[2 * i + 1] >= 0 ? 1.f : 0.f);
-  for (int d = 0; d < 3; ++d) {
-    const float lo = (float)g.knots[d][0], hi = (float)g.knots[d][g.n_knots[d] - 1];
-    put(12 + 9 * a.B + d, __fdiv_rn(__fsub_rn(x[d], lo), __fsub_rn(hi, lo)));
+  const int4 v0 = reinterpret_cast<const int4*>(a.vidx + 8 * i)[0];
+  const int4 v1 = reinterpret_cast<const int4*>(a.vidx + 8 * i)[1];
+  const int vid[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
+  float wf[8];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const double2 w2 = reinterpret_cast<const double2*>(a.w + 8 * i)[k];
+    wf[2 * k] = (float)w2.x;
+    wf[2 * k + 1] = (float)w2.y;
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    if (k < nw) put(3 + k, wf[k]);
+  put(11, tet >= 0 ? 1.f : 0.f);
+  const VT* vals = static_cast<const VT*>(a.values);
+  for (int b = 0; b < B; ++b) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k < nw) {
+        const float ev = (float)vals[(long long)vid[k] * B + b];
+        put(12 + k * B + b, __fmul_rn(ev, a.inv_omega));
+        s = __fadd_rn(s, __fmul_rn(wf[k], ev));
+      }
+    }
+    if (base) base[b] = s;
+    put(12 + 8 * B + b, __fmul_rn(s, a.inv_omega));
   }
 }
 
-// Columns of mode b: its vertex eigenvalues (12 + slot·B + b) and its
-// interpolated eigenvalue Σ w·v in slot order (12 + 8B + b), which is also
-// returned unscaled (the FP32 gather's own result for FP32 storage).
-template <class Put>
-__device__ float feature_mode(const FeatureArgs& a, long long i, int b, Put put) {
-  const int nw = min(a.nw[i], 8);
-  float s = 0.f;
-  for (int k = 0; k < nw; ++k) {
-    const float ev = vertex_value(a, a.vidx[8 * i + k], b);
-    put(12 + k * a.B + b, __fmul_rn(ev, a.inv_omega));
-    s = __fadd_rn(s, __fmul_rn((float)a.w[8 * i + k], ev));
-  }
-  put(12 + 8 * a.B + b, __fmul_rn(s, a.inv_omega));
-  return s;
-}
-
-// The whole row through put(col, value) (the caller zeroes the row first),
-// and through base the B interpolated eigenvalues in the data's own unit
-// (NaN for a q whose locate failed).
+// The row through put and the plain values through base (NaN where the
+// locate failed); the caller zeroes the row first.
 template <class Put>
 __device__ void feature_row(const DevGeom& g, const FeatureArgs& a, long long i, Put put, float* base) {
   if (a.status[i]) {
     for (int b = 0; b < a.B; ++b) base[b] = __int_as_float(0x7fc00000);
     return;
   }
-  feature_head(g, a, i, put);
-  for (int b = 0; b < a.B; ++b) base[b] = feature_mode(a, i, b, put);
+  if (a.values_f64) feature_all<double>(g, a, i, put, base);
+  else feature_all<float>(g, a, i, put, base);
 }
 
 __global__ void mlp_features_kernel(DevGeom g, FeatureArgs a, float* X, float* base) {
@@ -498,8 +511,8 @@ __global__ void __launch_bounds__(kRowsPerBlock) mlp_xrows_kernel(DevGeom g, Fea
     const long long i = r0 + threadIdx.x;
     if (i < a.n && !a.status[i]) {
       auto put = [row](int k, float v) { row[k] = __float2bfloat16_rn(v); };
-      feature_head(g, a, i, put);
-      for (int b = 0; b < a.B; ++b) feature_mode(a, i, b, put);
+      if (a.values_f64) feature_all<double>(g, a, i, put, nullptr);
+      else feature_all<float>(g, a, i, put, nullptr);
     }
     __syncthreads();
     // the whole tile (rows past n are zeros), 16-byte pieces in core-matrix
