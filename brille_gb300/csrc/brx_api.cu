@@ -194,7 +194,8 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.gamma_F0 = h->g.gamma_F0;
   p.gamma_vidx = h->g.gamma_vidx;
   p.gamma_vectors = h->g.gamma_vectors;
-  p.qmax = kGroupQ;
+  p.qmax = h->group_q;
+  p.qsplit = h->qsplit;
   return p;
 }
 
@@ -389,7 +390,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     // data (eigenvalues) is gathered per q and needs no grouping
     const bool grouped = uses_groups(h->vals, false) || (h->vecs.present && uses_groups(h->vecs, h->vecs.cplx));
     if (grouped)
-      h->launches += launch_grouping(s.r.key, m, n_group_keys(h->g.n_cube, h->g.n_tets), kGroupQ, s.sort_scratch,
+      h->launches += launch_grouping(s.r.key, m, n_group_keys(h->g.n_cube, h->g.n_tets), h->group_q, s.sort_scratch,
                                      s.order, s.groups, s.n_groups, cs);
     if (ev[2]) cudaEventRecord(ev[2], cs);
     char* vdst = o_host ? static_cast<char*>(s.vbuf.p) : static_cast<char*>(vals_out) + vrow * (size_t)base;
@@ -933,6 +934,18 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
   }
   const size_t cands[] = {24 * 1024, 32 * 1024, 40 * 1024, 56 * 1024, 72 * 1024, 96 * 1024, 128 * 1024, 160 * 1024};
   brx_status st = BRX_OK;
+  // time of the gather stage `which` (2 values, 3 vectors), best of reps
+  auto timed = [&](int which) -> double {
+    double t = 1e300;
+    for (int r = 0; r < reps && !st; ++r) {
+      brx_profile(h, 1);
+      st = run_query(h, 1, Q, n, vp, crow ? cp : nullptr, flags, stream, nullptr);
+      if (!st) t = std::min(t, h->stage_ms[which]);
+    }
+    return t;
+  };
+  // the heavier gather decides the group size and the work split
+  const int lead = (h->vecs.present && uses_groups(h->vecs, h->vecs.cplx)) ? 1 : 0;
   for (int which = 0; which < 2 && !st; ++which) {
     const Interp& d = which ? h->vecs : h->vals;
     if (!d.present || !uses_groups(d, which ? d.cplx : false)) continue;
@@ -941,16 +954,29 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
     for (size_t c : cands) {
       if (c > h->smem_optin) continue;
       h->gather_budget[which] = c;
-      double t = 1e300;
-      for (int r = 0; r < reps && !st; ++r) {
-        brx_profile(h, 1);
-        st = run_query(h, 1, Q, n, vp, crow ? cp : nullptr, flags, stream, nullptr);
-        if (!st) t = std::min(t, h->stage_ms[2 + which]);
-      }
+      const double t = timed(2 + which);
       if (st) break;
       if (t < best) { best = t; best_b = c; }
     }
     h->gather_budget[which] = best_b;
+    if (which != lead || st) continue;
+    // coordinate descent over q per work descriptor, then units per thread
+    int best_g = h->group_q;
+    for (int gq : {16, 32, 64}) {
+      h->group_q = gq;
+      const double t = timed(2 + which);
+      if (st) break;
+      if (t < best) { best = t; best_g = gq; }
+    }
+    h->group_q = best_g;
+    int best_s = h->qsplit;
+    for (int qs : {1, 2, 4}) {
+      h->qsplit = qs;
+      const double t = timed(2 + which);
+      if (st) break;
+      if (t < best) { best = t; best_s = qs; }
+    }
+    h->qsplit = best_s;
   }
   brx_profile(h, 0);
   h->profile = false;
@@ -959,9 +985,11 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
   return st;
 }
 
-brx_status brx_tuning(const brx_handle* h, int32_t* kb, int32_t n) {
-  if (!h || !kb || n < 1) return BRX_ERR_INVALID_ARGUMENT;
-  for (int i = 0; i < n && i < 2; ++i) kb[i] = (int32_t)(h->gather_budget[i] / 1024);
+brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n) {
+  if (!h || !out || n < 1) return BRX_ERR_INVALID_ARGUMENT;
+  const int32_t v[4] = {(int32_t)(h->gather_budget[0] / 1024), (int32_t)(h->gather_budget[1] / 1024), h->group_q,
+                        h->qsplit};
+  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
   return BRX_OK;
 }
 

@@ -431,7 +431,8 @@ __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* 
   const int B = p.B, s = p.s;
   const int tid = threadIdx.x, nth = blockDim.x;
   const int nitem = mb * G;
-  int qsplit = (2 * nth + nitem - 1) / nitem;
+  const int units = p.qsplit > 0 ? p.qsplit : 2;
+  int qsplit = (units * nth + nitem - 1) / nitem;
   if (qsplit > count) qsplit = count;
   if (qsplit < 1) qsplit = 1;
   const bool gamma = p.rot_mode == ROT_GAMMA;
@@ -1049,7 +1050,7 @@ void launch_scalar_batch(const GatherParams* items, const long long* qb_off, int
 
 // ---------------------------------------------------------------------------
 // grouping: counting sort of q by group key, then one work descriptor per
-// group (at most kGroupQ q each)
+// group (at most qmax q each)
 // ---------------------------------------------------------------------------
 // Lanes of a warp holding the same key add once, through their lowest lane:
 // trellises with few tetrahedra put millions of q on a handful of keys.

@@ -104,6 +104,8 @@ struct brx_handle {
   // shared-memory budget per CTA of the values (0) and vectors (1) gathers
   // (modes staged per block, hence CTAs per SM); brx_tune picks them
   size_t gather_budget[2] = {56 * 1024, 56 * 1024};
+  int group_q = brx::kGroupQ;  // q per gather work descriptor
+  int qsplit = 2;         // FP32 gather work units per thread and block
   DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
   bool mlp_tc = false;         // dense layers on tcgen05 (else mma.sync)
   DevBuf mlp_wt, mlp_bt;       // the tcgen05 kernel's weights (core-matrix order) and padded biases

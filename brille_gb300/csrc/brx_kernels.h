@@ -17,10 +17,10 @@ enum StoreKind { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2 };
 struct GroupDesc {
   int32_t key;    // group key (cube node / tetrahedron and pivot slot)
   int32_t start;  // first entry in the key-sorted order
-  int32_t count;  // number of q (≤ kGroupQ)
+  int32_t count;  // number of q (≤ the query's group size)
 };
 
-constexpr int kGroupQ = 32;
+constexpr int kGroupQ = 32;  // default q per work descriptor
 
 struct GatherParams {
   // locate records (chunk-local)
@@ -64,6 +64,7 @@ struct GatherParams {
   void* out;                 // n × B × s, double or float (complex: pairs)
   int MB;                    // modes staged per block
   int qmax;                  // q per work descriptor
+  int qsplit;                // FP32 gather: about qsplit work units per thread and block (0: 2)
   // batches: records are indexed by batch-wide q, the output by q − q_base;
   // group keys are batch-wide, the trellis's own by key − key_base
   long long q_base;

@@ -323,7 +323,7 @@ class _Grid:
     def tune(self, Q, *, out_f32=False, reps=2, stream=None, values_out=None, vectors_out=None):
         """Pick the gathers' shared-memory budgets by timing a sample query
         (brx_tune), into the given output buffers or temporary ones; returns
-        the chosen budgets in KB (values, vectors)."""
+        the chosen shapes (see tuning())."""
         h = self._handle()
         flags = _abi.BRX_FLAG_OUT_F32 if out_f32 else 0
         n = int(Q.shape[0])
@@ -331,10 +331,12 @@ class _Grid:
         return self.tuning()
 
     def tuning(self):
-        kb = (C.c_int32 * 2)()
+        """(values smem KB, vectors smem KB, q per work descriptor, work
+        units per thread)."""
+        v = (C.c_int32 * 4)()
         h = self._handle()
-        check(load().brx_tuning(h, kb, 2), h)
-        return int(kb[0]), int(kb[1])
+        check(load().brx_tuning(h, v, 4), h)
+        return tuple(int(x) for x in v)
 
     def launch_count(self):
         return int(load().brx_launch_count(self._handle()))

@@ -323,16 +323,18 @@ brx_status brx_profile(brx_handle* h, int32_t enable);
  * the number of gather work groups. */
 brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* q_count, int64_t* groups);
 
-/* Autotune the gathers of this handle: times each candidate shared-memory
- * budget per CTA (24-160 KB; it sets the modes staged per block and so the
- * CTAs per SM) on a sample query (Q: n × 3, host or device; outputs as for
- * brx_ir_interpolate_at, or NULL for temporary device buffers; flags as for
- * brx_ir_interpolate_at) with stage events, best of reps, and keeps the
- * fastest for the values and for the vectors.  brx_tuning returns the
- * chosen budgets in KB (values, vectors). */
+/* Autotune the gathers of this handle on a sample query (Q: n × 3, host or
+ * device; outputs as for brx_ir_interpolate_at, or NULL for temporary
+ * device buffers; flags as for brx_ir_interpolate_at), timing with stage
+ * events, best of reps: each gather's shared-memory budget per CTA (24-160
+ * KB; it sets the modes staged per block and so the CTAs per SM), then,
+ * for the heavier gather, the q per work descriptor (16, 32, 64) and the
+ * work units per thread (1, 2, 4).  Results never change, only launch
+ * shapes.  brx_tuning returns values budget (KB), vectors budget (KB),
+ * q per descriptor, units per thread. */
 brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out, uint32_t flags,
                     void* stream, int32_t reps);
-brx_status brx_tuning(const brx_handle* h, int32_t* kb, int32_t n);
+brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n);
 
 int32_t brx_abi_version(void);
 
