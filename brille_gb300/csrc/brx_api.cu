@@ -124,7 +124,7 @@ brx_status rotation_mode(const Interp& d, int* mode, std::string* msg) {
 brx_status ensure_scratch(brx_handle* h, long long chunk) {
   if (chunk <= h->scratch_q) return BRX_OK;
   const size_t n = (size_t)chunk;
-  const size_t parts[10] = {24 * n, 64 * n, 12 * n, 8 * n, 8 * n, 4 * n, 32 * n, 4 * n, 4 * n, 4 * n};
+  const size_t parts[11] = {24 * n, 64 * n, 32 * n, 12 * n, 8 * n, 8 * n, 4 * n, 32 * n, 4 * n, 4 * n, 4 * n};
   size_t rec = 0;
   for (size_t b : parts) rec += (b + 255) & ~size_t(255);
   for (auto& s : h->sc) {
@@ -137,6 +137,7 @@ brx_status ensure_scratch(brx_handle* h, long long chunk) {
     };
     s.r.q_ir = reinterpret_cast<double*>(take(24 * n));
     s.r.w = reinterpret_cast<double*>(take(64 * n));
+    s.r.w32 = reinterpret_cast<float*>(take(32 * n));
     s.r.tau = reinterpret_cast<int32_t*>(take(12 * n));
     s.r.rot = reinterpret_cast<int32_t*>(take(8 * n));
     s.r.node = reinterpret_cast<int32_t*>(take(8 * n));
@@ -162,6 +163,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.nw = s.r.nw;
   p.vidx = s.r.vidx;
   p.w = s.r.w;
+  p.w32 = s.r.w32;
   p.rot = s.r.rot;
   p.q_ir = s.r.q_ir;
   p.status = s.r.status;

@@ -113,6 +113,7 @@ brx::GatherParams item_params(brx_batch* b, int i, const Interp& d, int rot_mode
   p.nw = b->r.nw;
   p.vidx = b->r.vidx;
   p.w = b->r.w;
+  p.w32 = b->r.w32;
   p.rot = b->r.rot;
   p.q_ir = b->r.q_ir;
   p.status = b->r.status;
@@ -403,7 +404,7 @@ brx_status brx_batch_create(brx_handle* const* handles, int32_t n, const int64_t
   if (cudaSetDevice(b->device) != cudaSuccess) return bail(BRX_ERR_CUDA);
   // records, sort scratch and work descriptors for every q of the batch
   const size_t m = (size_t)std::max<long long>(1, b->total_q);
-  const size_t parts[10] = {24 * m, 64 * m, 12 * m, 8 * m, 8 * m, 4 * m, 32 * m, 4 * m, 4 * m, 4 * m};
+  const size_t parts[11] = {24 * m, 64 * m, 32 * m, 12 * m, 8 * m, 8 * m, 4 * m, 32 * m, 4 * m, 4 * m, 4 * m};
   size_t rec = 0;
   for (size_t x : parts) rec += align256(x);
   if (b->rec.ensure(rec) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
@@ -415,6 +416,7 @@ brx_status brx_batch_create(brx_handle* const* handles, int32_t n, const int64_t
   };
   b->r.q_ir = reinterpret_cast<double*>(take(24 * m));
   b->r.w = reinterpret_cast<double*>(take(64 * m));
+  b->r.w32 = reinterpret_cast<float*>(take(32 * m));
   b->r.tau = reinterpret_cast<int32_t*>(take(12 * m));
   b->r.rot = reinterpret_cast<int32_t*>(take(8 * m));
   b->r.node = reinterpret_cast<int32_t*>(take(8 * m));

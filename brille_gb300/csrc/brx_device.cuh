@@ -140,6 +140,7 @@ struct Records {
   int32_t* nw;      // n
   int32_t* vidx;    // n × 8
   double* w;        // n × 8
+  float* w32;       // n × 8: the weights rounded once to FP32 (for the FP32 gathers)
   int32_t* status;  // n
   int32_t* key;     // n: gather group (cube node or tetrahedron, and pivot slot)
 };

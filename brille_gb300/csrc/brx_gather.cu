@@ -589,7 +589,7 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       const int nw = p.nw[qi];
       for (int k = 0; k < nw; ++k) {
         const int v = p.vidx[8 * qi + k];
-        const Acc wk = (Acc)p.w[8 * qi + k];
+        const Acc wk = sizeof(Acc) == 4 ? (Acc)p.w32[8 * qi + k] : (Acc)p.w[8 * qi + k];
         for (int x = 0; x < nslot; ++x)
           if (gc.vid[x] == v) wsl[x] = wk;
       }
@@ -809,7 +809,7 @@ __device__ __forceinline__ void scalar_one(const GatherParams& p, long long qi, 
       const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b) : b;
       Acc dr, di;
       Ld<St, CPLX>::get(data, ((long long)v * B + row) * s + e, dr, di);
-      const Acc w = (Acc)p.w[8 * qi + x];
+      const Acc w = sizeof(Acc) == 4 ? (Acc)p.w32[8 * qi + x] : (Acc)p.w[8 * qi + x];
       vr = A::add(vr, A::mul(w, dr));
       if (CPLX) vi = A::add(vi, A::mul(w, di));
     }

@@ -27,6 +27,7 @@ struct GatherParams {
   const int32_t* nw;
   const int32_t* vidx;
   const double* w;
+  const float* w32;          // the weights in FP32 (read by the FP32 gathers)
   const int32_t* rot;
   const double* q_ir;
   const int32_t* status;     // per-q status (scalar path)

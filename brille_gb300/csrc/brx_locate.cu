@@ -536,6 +536,12 @@ __device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, c
   r.nw[i] = nw;
 #pragma unroll
   for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = vi[k]; r.w[8 * i + k] = w[k]; }
+  // FP64→FP32 conversions run on the FP64 pipe: once here, not per mode
+  if (r.w32) {
+    float4* w4 = reinterpret_cast<float4*>(r.w32 + 8 * i);
+    w4[0] = make_float4((float)w[0], (float)w[1], (float)w[2], (float)w[3]);
+    w4[1] = make_float4((float)w[4], (float)w[5], (float)w[6], (float)w[7]);
+  }
   r.status[i] = st;
   int32_t key = (int32_t)n_group_keys(g.n_cube, g.n_tets);  // failed q: last bucket
   if (!st) {

@@ -96,6 +96,7 @@ struct FeatureArgs {
   const int32_t* nw;
   const int32_t* vidx;     // n × 8
   const double* w;         // n × 8
+  const float* w32;        // n × 8 FP32 copies, or null
   const int32_t* status;
   long long n;
   const void* values;      // n_vertices × B, float or double
@@ -144,11 +145,18 @@ __device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs&
   const int4 v1 = reinterpret_cast<const int4*>(a.vidx + 8 * i)[1];
   const int vid[8] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
   float wf[8];
+  if (a.w32) {
+    const float4 w0 = reinterpret_cast<const float4*>(a.w32 + 8 * i)[0];
+    const float4 w1 = reinterpret_cast<const float4*>(a.w32 + 8 * i)[1];
+    wf[0] = w0.x; wf[1] = w0.y; wf[2] = w0.z; wf[3] = w0.w;
+    wf[4] = w1.x; wf[5] = w1.y; wf[6] = w1.z; wf[7] = w1.w;
+  } else {
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const double2 w2 = reinterpret_cast<const double2*>(a.w + 8 * i)[k];
-    wf[2 * k] = (float)w2.x;
-    wf[2 * k + 1] = (float)w2.y;
+    for (int k = 0; k < 4; ++k) {
+      const double2 w2 = reinterpret_cast<const double2*>(a.w + 8 * i)[k];
+      wf[2 * k] = (float)w2.x;
+      wf[2 * k + 1] = (float)w2.y;
+    }
   }
 #pragma unroll
   for (int k = 0; k < 8; ++k)
@@ -1140,9 +1148,10 @@ int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_o
   // sub-chunks whose feature rows stay in L2 between the two kernels
   for (long long off = 0; off < n; off += kResidualSub) {
     const long long m = std::min<long long>(kResidualSub, n - off);
-    const brx::FeatureArgs f = feature_args(h, s.r.q_ir + 3 * off, s.r.node + 2 * off, s.r.nw + off,
-                                            s.r.vidx + 8 * off, s.r.w + 8 * off, s.r.status + off, m, d_in,
-                                            h->mlp_omega_scale);
+    brx::FeatureArgs f = feature_args(h, s.r.q_ir + 3 * off, s.r.node + 2 * off, s.r.nw + off,
+                                      s.r.vidx + 8 * off, s.r.w + 8 * off, s.r.status + off, m, d_in,
+                                      h->mlp_omega_scale);
+    f.w32 = s.r.w32 + 8 * off;
     const long long blocks = std::min<long long>((m + brx::kRowsPerBlock - 1) / brx::kRowsPerBlock,
                                                  (long long)h->num_sms * 8);
     brx::mlp_xrows_kernel<<<(unsigned)blocks, brx::kRowsPerBlock, brx::xrows_smem(d_in), cs>>>(h->g, f, X);

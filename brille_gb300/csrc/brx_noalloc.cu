@@ -11,7 +11,7 @@
 //
 // How: the per-q scratch of the pipeline (locate records, gather work
 // descriptors, work-queue counters) lives in one file-scope __device__ array
-// of fixed size, enough for BRX_NOALLOC_MAX_Q q per call (about 12 MB, held by
+// of fixed size, enough for BRX_NOALLOC_MAX_Q q per call (about 14 MB, held by
 // every GPU that loads this library until the process exits).  Host code
 // cannot use the array's name as a device address, so the first call on each
 // device looks the address up with cudaGetSymbolAddress (with that device
@@ -41,7 +41,7 @@ namespace {
 
 // per-q bytes: q_ir 24, weights 64, τ 12, R/R⁻¹ 8, node 8, count 4, vertex ids 32, status 4, key 4,
 // order 4, work descriptor 12; each array is padded to 256 bytes
-constexpr size_t kPerQ = 24 + 64 + 12 + 8 + 8 + 4 + 32 + 4 + 4 + 4 + 12;
+constexpr size_t kPerQ = 24 + 64 + 32 + 12 + 8 + 8 + 4 + 32 + 4 + 4 + 4 + 12;
 constexpr size_t kScratchBytes = kPerQ * BRX_NOALLOC_MAX_Q + 16 * 256;
 
 static __device__ __align__(256) unsigned char brx_noalloc_scratch[kScratchBytes];
@@ -134,6 +134,7 @@ extern "C" brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double*
   Scratch s;
   s.r.q_ir = reinterpret_cast<double*>(take(24 * m));
   s.r.w = reinterpret_cast<double*>(take(64 * m));
+  s.r.w32 = reinterpret_cast<float*>(take(32 * m));
   s.r.tau = reinterpret_cast<int32_t*>(take(12 * m));
   s.r.rot = reinterpret_cast<int32_t*>(take(8 * m));
   s.r.node = reinterpret_cast<int32_t*>(take(8 * m));

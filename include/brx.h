@@ -195,7 +195,7 @@ brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir,
  * captured), serving loops that cannot take cudaMalloc's device-wide
  * synchronisation, and host frameworks whose own pool owns the device memory.
  * No counterpart in the reference.  All per-q scratch lives in one fixed
- * __device__ array of this library (about 12 MB on every device that loads
+ * __device__ array of this library (about 14 MB on every device that loads
  * it, kept until exit), so a call allocates nothing.  Limits: Q and outputs
  * must be device pointers; n ≤ BRX_NOALLOC_MAX_Q (larger n is rejected with
  * BRX_ERR_INVALID_ARGUMENT).  The first call on a device looks up the array
