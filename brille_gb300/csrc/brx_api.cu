@@ -964,7 +964,7 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
     if (which != lead || st) continue;
     // coordinate descent over q per work descriptor, then units per thread
     int best_g = h->group_q;
-    for (int gq : {16, 32, 64}) {
+    for (int gq : {16, 32, 64, 128}) {
       h->group_q = gq;
       const double t = timed(2 + which);
       if (st) break;

@@ -328,7 +328,7 @@ brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* 
  * device buffers; flags as for brx_ir_interpolate_at), timing with stage
  * events, best of reps: each gather's shared-memory budget per CTA (24-160
  * KB; it sets the modes staged per block and so the CTAs per SM), then,
- * for the heavier gather, the q per work descriptor (16, 32, 64) and the
+ * for the heavier gather, the q per work descriptor (16-128) and the
  * work units per thread (1, 2, 4).  Results never change, only launch
  * shapes.  brx_tuning returns values budget (KB), vectors budget (KB),
  * q per descriptor, units per thread. */

@@ -241,6 +241,6 @@ def test_tune_keeps_results():
     Q = _queries(c, 20000, seed=11)
     v0, c0 = g.ir_interpolate_at(Q, out_f32=True)
     kb = g.tune(Q, out_f32=True, reps=1)
-    assert kb[1] in (24, 32, 40, 56, 72, 96, 128, 160) and kb[2] in (16, 32, 64) and kb[3] in (1, 2, 4)
+    assert kb[1] in (24, 32, 40, 56, 72, 96, 128, 160) and kb[2] in (16, 32, 64, 128) and kb[3] in (1, 2, 4)
     v1, c1 = g.ir_interpolate_at(Q, out_f32=True)
     assert np.array_equal(v0, v1) and np.array_equal(c0, c1)
