@@ -635,7 +635,7 @@ def main():
     tuned = None
     if not args.no_tune:
         t = time.time()
-        tuned = grid.tune(Qs[0], out_f32=out_f32, reps=1, stream=sp, values_out=vals, vectors_out=vecs)
+        tuned = grid.tune(Qs[0], out_f32=out_f32, reps=2, stream=sp, values_out=vals, vectors_out=vecs)
         log(f"[setup] gather budgets (KB, values/vectors) {tuned} in {time.time() - t:.1f}s")
 
     for i in range(args.warmup):
