@@ -830,6 +830,41 @@ __global__ void scalar_gather_kernel(GatherParams p) {
   }
 }
 
+// FP32 scalar values without a permutation table, W consecutive branches
+// per thread (B a multiple of W, 4W-byte aligned rows): the record is read
+// once per W outputs, vertex rows and outputs move as float2/float4, and
+// the indexing is 32-bit (a chunk holds at most 2^24 q, B ≤ 96).  Same sum
+// order as scalar_one.
+template <int W>
+__global__ void scalar_gather_vec_kernel(GatherParams p) {
+  using V = typename std::conditional<W == 4, float4, float2>::type;
+  const int B = p.B, nch = B / W;
+  const int total = (int)p.n * nch;
+  const float* data = static_cast<const float*>(p.data);
+  float* out = static_cast<float*>(p.out);
+  for (int it = blockIdx.x * blockDim.x + threadIdx.x; it < total; it += gridDim.x * blockDim.x) {
+    const int qi = it / nch, c = it - qi * nch;
+    if (p.status[qi]) continue;
+    const int nw = p.nw[qi];
+    float acc[W];
+#pragma unroll
+    for (int k = 0; k < W; ++k) acc[k] = 0.f;
+    for (int x = 0; x < nw; ++x) {
+      const int v = p.vidx[8 * qi + x];
+      const float w = p.w32[8 * qi + x];
+      const V d = __ldg(reinterpret_cast<const V*>(data + (size_t)v * B) + c);
+      const float* dv = reinterpret_cast<const float*>(&d);
+#pragma unroll
+      for (int k = 0; k < W; ++k) acc[k] = Ar<float>::add(acc[k], Ar<float>::mul(w, dv[k]));
+    }
+    V o;
+    float* ov = reinterpret_cast<float*>(&o);
+#pragma unroll
+    for (int k = 0; k < W; ++k) ov[k] = acc[k];
+    reinterpret_cast<V*>(out + (size_t)qi * B)[c] = o;
+  }
+}
+
 // Scalar-only items of a batch: one thread per (item, q, branch); qb_off[i]
 // is the first pair of item i.
 template <typename Acc, typename St, bool CPLX, typename Out>
@@ -873,6 +908,19 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
   if (p.nvec == 0 && p.nmat == 0 && !p.phase_allowed) {
+    if constexpr (std::is_same<Acc, float>::value && std::is_same<St, float>::value && !CPLX &&
+                  std::is_same<Out, float>::value) {
+      const int W = (p.B % 4 == 0) ? 4 : (p.B % 2 == 0 ? 2 : 0);
+      const bool aligned = ((uintptr_t)p.data % (4 * W ? 4 * W : 1)) == 0 && ((uintptr_t)p.out % (4 * W ? 4 * W : 1)) == 0;
+      if (W && aligned && p.s == 1 && p.n_keys == 0 && p.w32 && p.n * (long long)p.B < (1LL << 31)) {
+        const long long total = p.n * (long long)(p.B / W);
+        long long blocks = (total + 255) / 256;
+        if (blocks > (long long)num_sms * 16) blocks = (long long)num_sms * 16;
+        if (W == 4) scalar_gather_vec_kernel<4><<<(unsigned)blocks, 256, 0, s>>>(p);
+        else scalar_gather_vec_kernel<2><<<(unsigned)blocks, 256, 0, s>>>(p);
+        return;
+      }
+    }
     long long total = p.n * (long long)p.B;
     long long blocks = (total + 255) / 256;
     if (blocks > (long long)num_sms * 16) blocks = (long long)num_sms * 16;
@@ -936,6 +984,9 @@ cudaError_t preload_locate_kernel();
 
 cudaError_t preload_query_kernels() {
   cudaError_t e;
+  cudaFuncAttributes a;
+  if ((e = cudaFuncGetAttributes(&a, scalar_gather_vec_kernel<4>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, scalar_gather_vec_kernel<2>)) != cudaSuccess) return e;
   if ((e = preload_store<double, double>()) != cudaSuccess) return e;
   if ((e = preload_store<float, float>()) != cudaSuccess) return e;
   if ((e = preload_store<float, __nv_bfloat16>()) != cudaSuccess) return e;
