@@ -154,7 +154,7 @@ __device__ __forceinline__ void cpY(St* dst, const St* src) {
 }
 
 struct GroupLayout {
-  size_t q, rot, ident, w, R, ph, M, de, e, Y, total;
+  size_t q, oq, rot, ident, w, R, ph, M, de, e, Y, total;
 };
 
 // e_modes: antiphase entries per slot; ybuf: elements of one of the two
@@ -169,6 +169,7 @@ __host__ __device__ inline GroupLayout group_layout_dims(int QM, int e_modes, in
     return at;
   };
   L.q = take(sizeof(long long) * QM);
+  L.oq = take(sizeof(long long) * QM);
   L.rot = take(sizeof(int) * 2 * QM);
   L.ident = take(sizeof(int) * 2 * QM);
   L.w = take(sizeof(Acc) * 8 * QM);
@@ -421,12 +422,70 @@ __device__ __forceinline__ void issue_rows(const GatherParams& p, const GroupInf
 // group) × a share of the group's q: the unit's rows of every slot, with
 // their antiphase, stay in registers while it loops over its q.  NS is the
 // number of vertex slots (8 for a cube node, 4 for a tetrahedron).
+// The q loop of one vector work unit (FP32): weighted sum of the unit's
+// slot rows held in registers, rotation and Γ phase per q, three complex
+// elements stored at the q's output offset.
+template <int NS, typename Acc, bool CPLX, typename Out>
+__device__ __forceinline__ void vector_unit(const Acc (&yr)[NS][3], const Acc (&yi)[NS][3], const Acc* s_w,
+                                            const Acc* s_M, const int* s_rotf, const Acc* s_ph, const int* s_de,
+                                            const long long* s_oq, int qs, int count, int qsplit, bool gamma, int na,
+                                            int k_atom, int e0, long long row_off, Out* out) {
+  constexpr int comps = CPLX ? 2 : 1;
+  for (int j = qs; j < count; j += qsplit) {
+    Acc wv[8];
+    {
+      const float4 w0 = *reinterpret_cast<const float4*>(s_w + 8 * j);
+      wv[0] = w0.x; wv[1] = w0.y; wv[2] = w0.z; wv[3] = w0.w;
+      if (NS == 8) {
+        const float4 w1 = *reinterpret_cast<const float4*>(s_w + 8 * j + 4);
+        wv[4] = w1.x; wv[5] = w1.y; wv[6] = w1.z; wv[7] = w1.w;
+      }
+    }
+    Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
+#pragma unroll
+    for (int x = 0; x < NS; ++x) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        vr[k] += wv[x] * yr[x][k];
+        if (CPLX) vi[k] += wv[x] * yi[x][k];
+      }
+    }
+    int de = e0;
+    if (s_rotf[j]) {
+      const float4 m0 = *reinterpret_cast<const float4*>(s_M + 12 * j);
+      const float4 m1 = *reinterpret_cast<const float4*>(s_M + 12 * j + 4);
+      const float m8 = s_M[12 * j + 8];
+      const Acc M[9] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w, m8};
+      Acc tr[3], ti[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        tr[a] = M[3 * a] * vr[0] + M[3 * a + 1] * vr[1] + M[3 * a + 2] * vr[2];
+        ti[a] = M[3 * a] * vi[0] + M[3 * a + 1] * vi[1] + M[3 * a + 2] * vi[2];
+      }
+      if (gamma) {
+        de = s_de[j * na + k_atom];
+        const float2 ph = *reinterpret_cast<const float2*>(s_ph + 2 * (j * na + k_atom));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          vr[a] = ph.x * tr[a] - ph.y * ti[a];
+          vi[a] = ph.x * ti[a] + ph.y * tr[a];
+        }
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
+      }
+    }
+    store_group<Out, CPLX>(out + s_oq[j] + row_off + (long long)de * comps, vr, vi, 3);
+  }
+}
+
 template <int NS, typename Acc, typename St, bool CPLX, typename Out>
 __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* s_Y, int rs, const Acc* s_e,
                                                const Acc* s_w, const Acc* s_R, const int* s_id, const Acc* s_M,
                                                const int* s_rotf, const Acc* s_ph, const int* s_de,
-                                               const long long* s_q, long long qb, int count, int pivot, int MB,
-                                               int b0, int mb, int G, int na, Out* out) {
+                                               const long long* s_q, const long long* s_oq, long long qb,
+                                               int count, int pivot, int MB, int b0, int mb, int G, int na,
+                                               Out* out) {
   constexpr int comps = CPLX ? 2 : 1;
   const int B = p.B, s = p.s;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -466,6 +525,11 @@ __device__ __forceinline__ void reg_tile_items(const GatherParams& p, const St* 
     }
     const int k_atom = gi - p.nsc;
     const size_t row_off = (size_t)bb * s * comps;
+    if (ne == 3) {
+      vector_unit<NS, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, qs, count, qsplit, gamma, na, k_atom,
+                                      e0, (long long)row_off, out);
+      continue;
+    }
     for (int j = qs; j < count; j += qsplit) {
       Acc wv[8];
       {
@@ -533,6 +597,7 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
   const int QM = gb.qmax;
   const GroupLayout L = group_layout_dims<Acc, St>(QM, gb.e_modes, gb.ph_atoms, gb.ybuf);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
+  long long* s_oq = reinterpret_cast<long long*>(sm + L.oq);
   int* s_rot = reinterpret_cast<int*>(sm + L.rot);
   int* s_id = reinterpret_cast<int*>(sm + L.ident);
   Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
@@ -585,6 +650,7 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
     for (int j = tid; j < count; j += nth) {
       const long long qi = p.order[start + j];
       s_q[j] = qi;
+      s_oq[j] = (qi - qb) * (long long)B * s * comps;
       Acc wsl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       const int nw = p.nw[qi];
       for (int k = 0; k < nw; ++k) {
@@ -708,11 +774,11 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       const int nitem = mb * G;
       if constexpr (kRegTile) {
         if (nslot == 4)
-          reg_tile_items<4, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, qb,
-                                                count, pivot, MB, b0, mb, G, na, out);
+          reg_tile_items<4, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, s_oq,
+                                                qb, count, pivot, MB, b0, mb, G, na, out);
         else
-          reg_tile_items<8, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, qb,
-                                                count, pivot, MB, b0, mb, G, na, out);
+          reg_tile_items<8, Acc, St, CPLX, Out>(p, s_Y, rs, s_e, s_w, s_R, s_id, s_M, s_rotf, s_ph, s_de, s_q, s_oq,
+                                                qb, count, pivot, MB, b0, mb, G, na, out);
       } else {
         const int items = count * nitem;
         for (int it = tid; it < items; it += nth) {

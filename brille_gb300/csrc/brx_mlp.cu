@@ -115,8 +115,9 @@ struct FeatureArgs {
 // first and has checked status[i] == 0): position in the node cell (0-2),
 // slot weights (3-10), tetrahedron flag (11), vertex eigenvalues
 // (12 + slot·B + mode), interpolated eigenvalues Σ w·v in slot order
-// (12 + 8B + mode, also returned through base unscaled: the FP32 gather's
-// own result for FP32 storage), position in the trellis box (12 + 9B + 0..2).
+// (12 + 8B + mode, also returned through base unscaled; the FP32 gather
+// forms the same sum, possibly with fused multiply-adds), position in the
+// trellis box (12 + 9B + 0..2).
 // The record's vertex ids and weights are read once, as vectors.
 template <typename VT, class Put>
 __device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs& a, long long i, Put put,
