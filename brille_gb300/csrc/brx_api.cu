@@ -198,6 +198,8 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.gamma_vectors = h->g.gamma_vectors;
   p.qmax = h->group_q;
   p.qsplit = h->qsplit;
+  p.err = h->err;
+  p.variant = h->gather_variant;
   return p;
 }
 
@@ -979,6 +981,13 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
       if (t < best) { best = t; best_s = qs; }
     }
     h->qsplit = best_s;
+    // the classic gather against the warp-independent one (FP32 data)
+    if (d.store != ST_F64 && !st) {
+      const int keep = h->gather_variant;
+      h->gather_variant = 1 - keep;
+      const double t = timed(2 + which);
+      if (!st && !(t < best)) h->gather_variant = keep;
+    }
   }
   brx_profile(h, 0);
   h->profile = false;
@@ -989,9 +998,9 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
 
 brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n) {
   if (!h || !out || n < 1) return BRX_ERR_INVALID_ARGUMENT;
-  const int32_t v[4] = {(int32_t)(h->gather_budget[0] / 1024), (int32_t)(h->gather_budget[1] / 1024), h->group_q,
-                        h->qsplit};
-  for (int i = 0; i < n && i < 4; ++i) out[i] = v[i];
+  const int32_t v[5] = {(int32_t)(h->gather_budget[0] / 1024), (int32_t)(h->gather_budget[1] / 1024), h->group_q,
+                        h->qsplit, h->gather_variant};
+  for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
   return BRX_OK;
 }
 

@@ -148,6 +148,8 @@ brx::GatherParams item_params(brx_batch* b, int i, const Interp& d, int rot_mode
   p.gamma_vectors = h->g.gamma_vectors;
   p.qmax = brx::kGroupQ;
   p.q_base = b->q_off[i];
+  p.err = b->d_err + i;
+  p.variant = 1;  // the batch kernel is the classic one
   p.key_base = b->key_off[i];
   return p;
 }

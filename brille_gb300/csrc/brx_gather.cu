@@ -18,6 +18,7 @@
 
 #include <type_traits>
 
+#include "../../include/brx.h"
 #include "brx_kernels.h"
 
 namespace brx {
@@ -855,6 +856,343 @@ __global__ void __launch_bounds__(kGatherThreads) group_gather_batch_kernel(Gath
 // Scalar-only interpolators (eigenvalues): one thread per (q, branch),
 // out = Σ_x w_x d[v_x][perm_x(b)] in the reference's order.  The rows are
 // small enough to stay in L2, so no grouping is needed.
+// ---------------------------------------------------------------------------
+// FP32 gather, warp-independent (vector and scalar elements, no matrices)
+// ---------------------------------------------------------------------------
+// Per group the CTA stages the q records once (two barriers), then every
+// warp works alone on its own blocks of MBw modes: one bulk copy
+// (cp.async.bulk, completion on the warp's mbarrier) per vertex row into one
+// of the warp's two staging buffers while the other is in use, the
+// antiphase of each (slot, mode) by two lanes, and one (mode, element group)
+// unit per lane over all q of the group, rows held in registers.  No CTA
+// barrier inside the mode loop.  Waits are bounded (about a second); on
+// expiry the query reports BRX_ERR_TIMEOUT.
+constexpr int kWarpGatherMaxWarps = 8;
+constexpr long long kGatherSpin = 2000000000LL;
+
+struct WarpLayout {
+  size_t q, oq, w, M, rotf, ph, de, e, Y, mbar, total;
+  int row_bytes;  // one staged row: the data row plus 16 bytes
+  size_t ybuf;    // one staging buffer: 8 slots × MBw rows
+};
+
+template <typename St, bool CPLX>
+__host__ __device__ inline WarpLayout warp_layout(int QM, int MBw, int s, int na, int warps) {
+  WarpLayout L;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = (o + 15) & ~size_t(15);
+    o = at + bytes;
+    return at;
+  };
+  const int nan = na > 0 ? na : 1;
+  L.q = take(8 * (size_t)QM);
+  L.oq = take(8 * (size_t)QM);
+  L.w = take(4 * 8 * (size_t)QM);
+  L.M = take(4 * 12 * (size_t)QM);
+  L.rotf = take(4 * (size_t)QM);
+  L.ph = take(4 * 2 * (size_t)nan * QM);
+  L.de = take(4 * (size_t)nan * QM);
+  L.e = take(4 * 2 * 8 * (size_t)MBw * warps);
+  L.row_bytes = s * (CPLX ? 2 : 1) * (int)sizeof(St) + 16;
+  L.ybuf = (size_t)8 * MBw * L.row_bytes;
+  L.Y = take(2 * L.ybuf * warps);
+  L.mbar = take(16 * (size_t)warps);
+  L.total = (o + 15) & ~size_t(15);
+  return L;
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void g_mbar_init(uint32_t m) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m) : "memory");
+}
+__device__ __forceinline__ void g_expect_tx(uint32_t m, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(m), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void g_bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t m) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(m)
+               : "memory");
+}
+__device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(m), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > kGatherSpin) return false;
+  }
+}
+
+template <typename St, bool CPLX, typename Out>
+__global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kernel(GatherParams p) {
+  using Acc = float;
+  constexpr int comps = CPLX ? 2 : 1;
+  extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ GatherParams s_par;
+  __shared__ GroupInfo s_g;
+  __shared__ int s_abort;
+  const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
+  for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth)
+    reinterpret_cast<int*>(&s_par)[w] = reinterpret_cast<const int*>(&p)[w];
+  const int B = p.B, s = p.s, MBw = p.MB, QM = p.qmax;
+  const bool gamma = p.rot_mode == ROT_GAMMA;
+  const int na = gamma ? p.nvec : 0;
+  const int G = p.nsc + p.nvec;
+  const WarpLayout L = warp_layout<St, CPLX>(QM, MBw, s, na, nwarps);
+  long long* s_q = reinterpret_cast<long long*>(sm + L.q);
+  long long* s_oq = reinterpret_cast<long long*>(sm + L.oq);
+  Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
+  Acc* s_M = reinterpret_cast<Acc*>(sm + L.M);
+  int* s_rotf = reinterpret_cast<int*>(sm + L.rotf);
+  Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
+  int* s_de = reinterpret_cast<int*>(sm + L.de);
+  Acc* s_e = reinterpret_cast<Acc*>(sm + L.e) + (size_t)warp * 2 * 8 * MBw;
+  unsigned char* Yw = sm + L.Y + (size_t)warp * 2 * L.ybuf;
+  const uint32_t mbar = smem_addr(sm + L.mbar) + 16 * warp;
+  if (lane == 0) {
+    g_mbar_init(mbar);
+    g_mbar_init(mbar + 8);
+  }
+  if (tid == 0) s_abort = 0;
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  __syncthreads();
+  GatherBatch gb{};
+  gb.groups = p.groups;
+  gb.n_groups = p.n_groups;
+  gb.counter = p.counter;
+  const int n_groups = *p.n_groups;
+  const int nblk = (B + MBw - 1) / MBw;
+  const uint32_t row_g = (uint32_t)(s * comps * sizeof(St));  // bytes of one data row
+  const St* data = reinterpret_cast<const St*>(p.data);
+  Out* out = reinterpret_cast<Out*>(p.out);
+  uint32_t phase[2] = {0u, 0u};
+  bool pending[2] = {false, false};
+  bool ok = true;
+
+  // rows of block blk into buffer buf: one bulk copy per (used slot, mode)
+  auto issue = [&](const GroupInfo& gi, int blk, int buf) {
+    const int b0 = blk * MBw, mb = min(MBw, B - b0), ns = gi.nslot - gi.pivot;
+    const int rows = ns * mb;
+    const uint32_t m = mbar + 8 * buf;
+    if (lane == 0) g_expect_tx(m, (uint32_t)rows * row_g);
+    __syncwarp();
+    unsigned char* Yb = Yw + (size_t)buf * L.ybuf;
+    for (int r = lane; r < rows; r += 32) {
+      const int x = gi.pivot + r / mb, mm = r % mb, b = b0 + mm;
+      const int pid = gi.pid[x];
+      const int row = pid >= 0 ? __ldg(s_par.perms + (long long)pid * B + b) : b;
+      const St* src = data + ((long long)gi.vid[x] * B + row) * s * comps;
+      g_bulk(smem_addr(Yb + (size_t)(x * MBw + mm) * L.row_bytes), src, row_g, m);
+    }
+    pending[buf] = true;
+  };
+
+  for (;;) {
+    if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g, lane);
+    __syncthreads();
+    if (s_g.count < 0 || s_abort) break;
+    const GroupInfo& gc = s_g;
+    const int count = gc.count, start = gc.start, nslot = gc.nslot, pivot = gc.pivot;
+    int buf = 0;
+    if (warp < nblk) issue(gc, warp, 0);
+    // per-q records: weights by slot, the 3×3 applied to vectors, output offsets
+    for (int j = tid; j < count; j += nth) {
+      const long long qi = p.order[start + j];
+      s_q[j] = qi;
+      s_oq[j] = (qi - p.q_base) * (long long)B * s * comps;
+      Acc wsl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      const int nw = p.nw[qi];
+      for (int k = 0; k < nw; ++k) {
+        const int v = p.vidx[8 * qi + k];
+        const Acc wk = p.w32[8 * qi + k];
+        for (int x = 0; x < nslot; ++x)
+          if (gc.vid[x] == v) wsl[x] = wk;
+      }
+      for (int x = 0; x < 8; ++x) s_w[8 * j + x] = wsl[x];
+      int rotf = 0;
+      if (p.rot_mode != ROT_NONE) {
+        const int r0 = p.rot[2 * qi], r1 = p.rot[2 * qi + 1];
+        Acc R[9], Ri[9];
+        for (int e = 0; e < 9; ++e) {
+          if (gamma && p.gamma_cart) {
+            R[e] = (Acc)p.rot_cart[9 * r0 + e];
+            Ri[e] = (Acc)p.rot_cart[9 * r1 + e];
+          } else {
+            R[e] = (Acc)p.ops[9 * r0 + e];
+            Ri[e] = (Acc)p.ops[9 * r1 + e];
+          }
+        }
+        const int32_t* W = p.ops + 9 * r0;
+        const bool ident = W[0] == 1 && W[1] == 0 && W[2] == 0 && W[3] == 0 && W[4] == 1 && W[5] == 0 &&
+                           W[6] == 0 && W[7] == 0 && W[8] == 1;
+        Acc scale = 1;
+        if (p.rot_mode == ROT_AXIAL)
+          scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
+                  R[2] * (R[3] * R[7] - R[4] * R[6]);
+        for (int a = 0; a < 3; ++a)
+          for (int c = 0; c < 3; ++c) {
+            Acc mv;
+            if (p.rot_mode == ROT_RECIP) mv = R[3 * c + a];
+            else if (gamma || p.rot_mode == ROT_AXIAL) mv = scale * Ri[3 * a + c];
+            else mv = R[3 * a + c];
+            s_M[12 * j + 3 * a + c] = mv;
+          }
+        rotf = (gamma || !ident) ? 1 : 0;
+        if (gamma) {
+          for (int k = 0; k < na; ++k) {
+            s_de[j * na + k] = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + r1);
+            const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + r1);
+            double dq = 0.0;
+            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi], d[0]));
+            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 1], d[1]));
+            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 2], d[2]));
+            const double frac = dq - rint(dq);  // e^{2πi n} = 1 exactly
+            float sn, cs;
+            sincospif(2.0f * (float)frac, &sn, &cs);
+            s_ph[2 * (j * na + k)] = cs;
+            s_ph[2 * (j * na + k) + 1] = sn;
+          }
+        }
+      }
+      s_rotf[j] = rotf;
+    }
+    __syncthreads();
+    for (int blk = warp; blk < nblk && ok; blk += nwarps) {
+      if (blk + nwarps < nblk) issue(gc, blk + nwarps, buf ^ 1);
+      bool got = g_wait(mbar + 8 * buf, phase[buf]);
+      got = __all_sync(0xffffffffu, got);
+      if (!got) {
+        ok = false;
+        break;
+      }
+      phase[buf] ^= 1u;
+      pending[buf] = false;
+      const unsigned char* Yb = Yw + (size_t)buf * L.ybuf;
+      const int b0 = blk * MBw, mb = min(MBw, B - b0);
+      // antiphase of every (slot, mode), two lanes each
+      const int npairs = (nslot - pivot) * mb;
+      for (int r = 0; r < 2 * npairs; r += 32) {
+        const int t = r + lane, pr = t >> 1, half = t & 1;
+        Acc rd = 0, id = 0;
+        int x = pivot, mm = 0;
+        if (pr < npairs) {
+          x = pivot + pr / mb;
+          mm = pr % mb;
+          if (CPLX && p.phase_allowed && x != pivot) {
+            const St* a = reinterpret_cast<const St*>(Yb + (size_t)(pivot * MBw + mm) * L.row_bytes);
+            const St* c = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+            for (int e = half; e < s; e += 2) {
+              Acc ar, ai, br, bi;
+              ldY<Acc, St, CPLX>(a + 2 * e, ar, ai);
+              ldY<Acc, St, CPLX>(c + 2 * e, br, bi);
+              rd += ar * br + ai * bi;
+              id += ar * bi - ai * br;
+            }
+          }
+        }
+        rd += __shfl_xor_sync(0xffffffffu, rd, 1);
+        id += __shfl_xor_sync(0xffffffffu, id, 1);
+        if (pr < npairs && half == 0) {
+          Acc er = 1, ei = 0;
+          if (CPLX && p.phase_allowed && x != pivot) {
+            const Acc mag = sqrtf(rd * rd + id * id);
+            if (mag > (Acc)0) {
+              er = rd / mag;
+              ei = -(id / mag);
+            }
+          }
+          s_e[2 * (x * MBw + mm)] = er;
+          s_e[2 * (x * MBw + mm) + 1] = ei;
+        }
+      }
+      __syncwarp();
+      // one (mode, element group) unit per lane, over every q of the group
+      for (int u = lane; u < mb * G; u += 32) {
+        const int mm = u / G, gi = u % G, bb = b0 + mm;
+        const int e0 = gi < p.nsc ? gi : p.nsc + 3 * (gi - p.nsc);
+        const int ne = gi < p.nsc ? 1 : 3;
+        const long long row_off = (long long)bb * s * comps;
+        if (nslot == 8) {
+          Acc yr[8][3], yi[8][3];
+#pragma unroll
+          for (int x = 0; x < 8; ++x) {
+            const bool usex = x >= pivot;
+            const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
+            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              Acc dr = 0, di = 0;
+              if (usex && k < ne) ldY<Acc, St, CPLX>(y + (e0 + k) * comps, dr, di);
+              yr[x][k] = er * dr - ei * di;
+              yi[x][k] = er * di + ei * dr;
+            }
+          }
+          if (ne == 3) {
+            vector_unit<8, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, 0, count, 1, gamma, na,
+                                           gi - p.nsc, e0, row_off, out);
+          } else {
+            for (int j = 0; j < count; ++j) {
+              Acc vr = 0, vi = 0;
+#pragma unroll
+              for (int x = 0; x < 8; ++x) {
+                vr += s_w[8 * j + x] * yr[x][0];
+                vi += s_w[8 * j + x] * yi[x][0];
+              }
+              store_group<Out, CPLX>(out + s_oq[j] + row_off + (long long)e0 * comps, &vr, &vi, 1);
+            }
+          }
+        } else {
+          Acc yr[4][3], yi[4][3];
+#pragma unroll
+          for (int x = 0; x < 4; ++x) {
+            const bool usex = x >= pivot;
+            const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
+            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              Acc dr = 0, di = 0;
+              if (usex && k < ne) ldY<Acc, St, CPLX>(y + (e0 + k) * comps, dr, di);
+              yr[x][k] = er * dr - ei * di;
+              yi[x][k] = er * di + ei * dr;
+            }
+          }
+          if (ne == 3) {
+            vector_unit<4, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, 0, count, 1, gamma, na,
+                                           gi - p.nsc, e0, row_off, out);
+          } else {
+            for (int j = 0; j < count; ++j) {
+              Acc vr = 0, vi = 0;
+#pragma unroll
+              for (int x = 0; x < 4; ++x) {
+                vr += s_w[8 * j + x] * yr[x][0];
+                vi += s_w[8 * j + x] * yi[x][0];
+              }
+              store_group<Out, CPLX>(out + s_oq[j] + row_off + (long long)e0 * comps, &vr, &vi, 1);
+            }
+          }
+        }
+      }
+      __syncwarp();  // the buffer may be refilled
+      buf ^= 1;
+    }
+    if (!ok && lane == 0) {
+      atomicExch(&s_abort, 1);
+      atomicOr(&p.err->flags, 1 << BRX_ERR_TIMEOUT);
+      atomicAdd(&p.err->count, 1);
+    }
+    __syncthreads();  // records and staging buffers are no longer read
+    if (s_abort) break;
+  }
+  // no copy may land after exit
+  for (int b = 0; b < 2; ++b)
+    if (pending[b]) g_wait(mbar + 8 * b, phase[b]);
+}
+
 // Interpolated values of branch b for q at record index qi (batch-wide),
 // written at output row qo.
 template <typename Acc, typename St, bool CPLX, typename Out>
@@ -971,6 +1309,40 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
   return (p.B + nblk - 1) / nblk;
 }
 
+// The warp-independent FP32 gather when the data fit it: vectors and scalars
+// only, rows a multiple of 16 bytes at 16-byte aligned addresses, shared
+// memory for 8 (or 4) warps.  Returns false when the classic kernel must run.
+template <typename St, bool CPLX, typename Out>
+static bool launch_warp(const GatherParams& p, int num_sms, cudaStream_t s) {
+  const int comps = CPLX ? 2 : 1;
+  const size_t row_g = (size_t)p.s * comps * sizeof(St);
+  if (p.variant == 1 || p.nmat != 0 || row_g % 16 != 0 || (uintptr_t)p.data % 16 != 0) return false;
+  const int G = p.nsc + p.nvec;
+  if (G < 1) return false;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
+  for (int warps : {kWarpGatherMaxWarps, kWarpGatherMaxWarps / 2}) {
+    int MBw = (32 + G - 1) / G;
+    if (MBw > p.B) MBw = p.B;
+    while (MBw > 1 && warp_layout<St, CPLX>(p.qmax, MBw, p.s, na, warps).total > (size_t)optin) --MBw;
+    const size_t smem = warp_layout<St, CPLX>(p.qmax, MBw, p.s, na, warps).total;
+    if (smem > (size_t)optin) continue;
+    cudaFuncSetAttribute(warp_gather_kernel<St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_gather_kernel<St, CPLX, Out>, warps * 32, smem);
+    if (per_sm < 1) continue;
+    GatherParams q = p;
+    q.MB = MBw;
+    long long grid = (long long)num_sms * per_sm;
+    if (grid > p.n) grid = p.n > 0 ? p.n : 1;
+    warp_gather_kernel<St, CPLX, Out><<<(unsigned)grid, warps * 32, smem, s>>>(q);
+    return true;
+  }
+  return false;
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
   if (p.nvec == 0 && p.nmat == 0 && !p.phase_allowed) {
@@ -993,6 +1365,8 @@ static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
     scalar_gather_kernel<Acc, St, CPLX, Out><<<(unsigned)blocks, 256, 0, s>>>(p);
     return;
   }
+  if constexpr (sizeof(Acc) == 4)
+    if (launch_warp<St, CPLX, Out>(p, num_sms, s)) return;
   const size_t smem = layout_bytes<Acc, St, CPLX>(p, p.MB);
   static bool configured = false;
   if (!configured) {
@@ -1014,6 +1388,8 @@ static cudaError_t preload_t() {
   cudaFuncAttributes a;
   cudaError_t e = cudaFuncGetAttributes(&a, group_gather_kernel<Acc, St, CPLX, Out>);
   if (e != cudaSuccess) return e;
+  if constexpr (sizeof(Acc) == 4)
+    if ((e = cudaFuncGetAttributes(&a, warp_gather_kernel<St, CPLX, Out>)) != cudaSuccess) return e;
   return cudaFuncGetAttributes(&a, scalar_gather_kernel<Acc, St, CPLX, Out>);
 }
 

@@ -106,6 +106,7 @@ struct brx_handle {
   size_t gather_budget[2] = {56 * 1024, 56 * 1024};
   int group_q = brx::kGroupQ;  // q per gather work descriptor
   int qsplit = 2;         // FP32 gather work units per thread and block
+  int gather_variant = 0; // FP32 gather: 0 warp-independent where it applies, 1 classic
   DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
   bool mlp_tc = false;         // dense layers on tcgen05 (else mma.sync)
   DevBuf mlp_wt, mlp_bt;       // the tcgen05 kernel's weights (core-matrix order) and padded biases

@@ -66,6 +66,8 @@ struct GatherParams {
   int MB;                    // modes staged per block
   int qmax;                  // q per work descriptor
   int qsplit;                // FP32 gather: about qsplit work units per thread and block (0: 2)
+  ErrorWord* err;            // bounded waits that run out report here
+  int variant;               // FP32 gather: 0 warp-independent kernel where it applies, 1 classic
   // batches: records are indexed by batch-wide q, the output by q − q_base;
   // group keys are batch-wide, the trellis's own by key − key_base
   long long q_base;

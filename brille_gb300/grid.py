@@ -332,10 +332,11 @@ class _Grid:
 
     def tuning(self):
         """(values smem KB, vectors smem KB, q per work descriptor, work
-        units per thread)."""
-        v = (C.c_int32 * 4)()
+        units per thread, FP32 gather kernel: 0 warp-independent, 1
+        CTA-synchronous)."""
+        v = (C.c_int32 * 5)()
         h = self._handle()
-        check(load().brx_tuning(h, v, 4), h)
+        check(load().brx_tuning(h, v, 5), h)
         return tuple(int(x) for x in v)
 
     def launch_count(self):

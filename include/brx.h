@@ -329,9 +329,12 @@ brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* 
  * events, best of reps: each gather's shared-memory budget per CTA (24-160
  * KB; it sets the modes staged per block and so the CTAs per SM), then,
  * for the heavier gather, the q per work descriptor (16-128) and the
- * work units per thread (1, 2, 4).  Results never change, only launch
- * shapes.  brx_tuning returns values budget (KB), vectors budget (KB),
- * q per descriptor, units per thread. */
+ * work units per thread (1, 2, 4), and for FP32 data whether the
+ * warp-independent gather (bulk-copied rows, per-warp mbarriers) or the
+ * CTA-synchronous one is faster.  Results of FP64 data never change, those
+ * of FP32 data only by rounding order.  brx_tuning returns values budget
+ * (KB), vectors budget (KB), q per descriptor, units per thread, gather
+ * kernel (0 warp-independent, 1 CTA-synchronous). */
 brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out, uint32_t flags,
                     void* stream, int32_t reps);
 brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n);

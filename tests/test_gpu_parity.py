@@ -234,7 +234,8 @@ def test_fp32_screens_match_exact_predicates():
 
 
 def test_tune_keeps_results():
-    """brx_tune changes launch shapes only: outputs are bit-identical."""
+    """brx_tune changes launch shapes only: outputs are bit-identical unless
+    it switches the FP32 gather kernel, which changes rounding order only."""
     c = crystal_case("hex16")
     g = _grid(c)
     g.fill(c["w"], [1, 0, 0, 0, 3], c["v"], [0, 3 * c["model"].n_atoms, 0, 2, 1], storage="f32")
@@ -243,4 +244,8 @@ def test_tune_keeps_results():
     kb = g.tune(Q, out_f32=True, reps=1)
     assert kb[1] in (24, 32, 40, 56, 72, 96, 128, 160) and kb[2] in (16, 32, 64, 128) and kb[3] in (1, 2, 4)
     v1, c1 = g.ir_interpolate_at(Q, out_f32=True)
-    assert np.array_equal(v0, v1) and np.array_equal(c0, c1)
+    assert np.array_equal(v0, v1)
+    if kb[4] == 0:
+        assert np.array_equal(c0, c1)
+    else:
+        assert np.allclose(c0, c1, rtol=0, atol=1e-5)
