@@ -1,8 +1,8 @@
 """Batched queries (brx_batch_*): many grids of different space groups,
 trellises, mode counts and ragged q counts in one launch per stage must give
-each grid exactly what its own ir_interpolate_at gives (bit for bit: the
-same kernels and operation order per q), through a plain run, a captured
-graph replayed on new inputs, and after autotuning; failures name the item.
+each grid what its own ir_interpolate_at gives (FP64 bit for bit; FP32 to
+rounding order), through a plain run, a captured graph replayed on new
+inputs, and after autotuning; failures name the item.
 """
 import numpy as np
 import pytest
@@ -41,13 +41,16 @@ def _Q(seed, counts=COUNTS, scale=1.0):
 
 
 def _check(grids, Qs, vals, vecs, out_f32):
+    """FP64: bit-identical.  FP32: the single query may take the
+    warp-independent gather, which sums in another order (1e-5)."""
+    same = (lambda a, b: np.allclose(a, b, rtol=1e-5, atol=1e-6)) if out_f32 else np.array_equal
     for i, (g, Q) in enumerate(zip(grids, Qs)):
         if len(Q) == 0:
             continue
         v, c = g.ir_interpolate_at(Q, out_f32=out_f32)
-        assert np.array_equal(vals[i].cpu().numpy(), v), i
+        assert same(vals[i].cpu().numpy(), v), i
         if c is not None:
-            assert np.array_equal(vecs[i].cpu().numpy(), c), i
+            assert same(vecs[i].cpu().numpy(), c), i
 
 
 @pytest.mark.parametrize("storage,out_f32", [("f64", False), ("f32", True)])
