@@ -7,7 +7,7 @@ inputs, and after autotuning; failures name the item.
 import numpy as np
 import pytest
 
-from _cases import crystal_case
+from _cases import conditioned_modes, crystal_case
 from brille_gb300 import BZTrellisQdc
 from brille_gb300.batch import BatchQuery
 from brille_gb300.grid import BZTrellisQdd
@@ -21,10 +21,19 @@ NAMES = ["diamond2", "hex16", "P-1", "R-3m", "Im-3m", "diamond8"]
 COUNTS = [1000, 3001, 0, 1, 2500, 777]
 
 
+CASES = {}
+
+
+def _case(name):
+    if name not in CASES:
+        CASES[name] = crystal_case(name)
+    return CASES[name]
+
+
 def _grids(storage="f64", values_only=False):
     out = []
     for name in NAMES:
-        c = crystal_case(name)
+        c = _case(name)
         if values_only:
             g = BZTrellisQdd(c["bz"], trellis=c["tr"])
             g.fill(c["w"][:, :, None], [1, 0, 0, 0, 3], storage=storage)
@@ -42,15 +51,29 @@ def _Q(seed, counts=COUNTS, scale=1.0):
 
 def _check(grids, Qs, vals, vecs, out_f32):
     """FP64: bit-identical.  FP32: the single query may take the
-    warp-independent gather, which sums in another order (1e-5)."""
-    same = (lambda a, b: np.allclose(a, b, rtol=1e-5, atol=1e-6)) if out_f32 else np.array_equal
+    warp-independent gather, which sums in another order: eigenvalues to
+    1e-5, eigenvectors to 1e-4 in overlap on the (q, mode) pairs whose
+    antiphase is well conditioned (elsewhere the phase is rounding noise)."""
     for i, (g, Q) in enumerate(zip(grids, Qs)):
         if len(Q) == 0:
             continue
         v, c = g.ir_interpolate_at(Q, out_f32=out_f32)
-        assert same(vals[i].cpu().numpy(), v), i
-        if c is not None:
-            assert same(vecs[i].cpu().numpy(), c), i
+        bv = vals[i].cpu().numpy()
+        if not out_f32:
+            assert np.array_equal(bv, v), i
+            if c is not None:
+                assert np.array_equal(vecs[i].cpu().numpy(), c), i
+            continue
+        assert np.allclose(bv, v, rtol=1e-5, atol=1e-5 * np.abs(v).max()), i
+        if c is None:
+            continue
+        bc = vecs[i].cpu().numpy().reshape(len(Q), c.shape[1], -1)
+        cc = c.reshape(len(Q), c.shape[1], -1)
+        ov = np.abs(np.einsum("nbe,nbe->nb", np.conj(bc), cc))
+        nrm = np.linalg.norm(bc, axis=-1) * np.linalg.norm(cc, axis=-1)
+        ok = (nrm > 1e-12) & conditioned_modes(_case(NAMES[i]), Q)
+        assert ok.mean() > 0.2, i
+        assert (1 - ov[ok] / nrm[ok]).max() < 1e-4, i
 
 
 @pytest.mark.parametrize("storage,out_f32", [("f64", False), ("f32", True)])
