@@ -934,7 +934,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ GatherParams s_par;
-  __shared__ GroupInfo s_g;
+  __shared__ GroupInfo s_g[2];
   __shared__ int s_abort;
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
   for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth)
@@ -992,15 +992,19 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
     pending[buf] = true;
   };
 
+  int cur = 0, buf = 0;
+  if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g[0], lane);
+  __syncthreads();
+  if (s_g[0].count >= 0 && warp < nblk) issue(s_g[0], warp, 0);
   for (;;) {
-    if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g, lane);
-    __syncthreads();
-    if (s_g.count < 0 || s_abort) break;
-    const GroupInfo& gc = s_g;
+    const GroupInfo& gc = s_g[cur];
+    if (gc.count < 0 || s_abort) break;
+    // the next descriptor is taken now; its first rows load before the
+    // group barrier at the end
+    if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g[cur ^ 1], lane);
     const int count = gc.count, start = gc.start, nslot = gc.nslot, pivot = gc.pivot;
-    int buf = 0;
-    if (warp < nblk) issue(gc, warp, 0);
-    // per-q records: weights by slot, the 3×3 applied to vectors, output offsets
+    // per-q records over all threads: weights by slot, the 3×3 applied to
+    // vectors, output offsets ...
     for (int j = tid; j < count; j += nth) {
       const long long qi = p.order[start + j];
       s_q[j] = qi;
@@ -1043,23 +1047,27 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
             s_M[12 * j + 3 * a + c] = mv;
           }
         rotf = (gamma || !ident) ? 1 : 0;
-        if (gamma) {
-          for (int k = 0; k < na; ++k) {
-            s_de[j * na + k] = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + r1);
-            const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + r1);
-            double dq = 0.0;
-            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi], d[0]));
-            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 1], d[1]));
-            dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 2], d[2]));
-            const double frac = dq - rint(dq);  // e^{2πi n} = 1 exactly
-            float sn, cs;
-            sincospif(2.0f * (float)frac, &sn, &cs);
-            s_ph[2 * (j * na + k)] = cs;
-            s_ph[2 * (j * na + k) + 1] = sn;
-          }
-        }
       }
       s_rotf[j] = rotf;
+    }
+    // ... and the Γ permutation and phase of every (q, atom)
+    if (gamma) {
+      for (int t = tid; t < count * na; t += nth) {
+        const int j = t / na, k = t - j * na;
+        const long long qi = p.order[start + j];
+        const int r1 = p.rot[2 * qi + 1];
+        s_de[t] = p.nsc + 3 * __ldg(p.gamma_F0 + k * p.n_ops + r1);
+        const double* d = p.gamma_vectors + 3 * __ldg(p.gamma_vidx + k * p.n_ops + r1);
+        double dq = 0.0;
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi], d[0]));
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 1], d[1]));
+        dq = __dadd_rn(dq, __dmul_rn(p.q_ir[3 * qi + 2], d[2]));
+        const double frac = dq - rint(dq);  // e^{2πi n} = 1 exactly
+        float sn, cs;
+        sincospif(2.0f * (float)frac, &sn, &cs);
+        s_ph[2 * t] = cs;
+        s_ph[2 * t + 1] = sn;
+      }
     }
     __syncthreads();
     for (int blk = warp; blk < nblk && ok; blk += nwarps) {
@@ -1180,13 +1188,16 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
       __syncwarp();  // the buffer may be refilled
       buf ^= 1;
     }
+    // this warp's first block of the next group (both buffers are free)
+    const GroupInfo& gn = s_g[cur ^ 1];
+    if (ok && gn.count >= 0 && warp < nblk) issue(gn, warp, buf);
     if (!ok && lane == 0) {
       atomicExch(&s_abort, 1);
       atomicOr(&p.err->flags, 1 << BRX_ERR_TIMEOUT);
       atomicAdd(&p.err->count, 1);
     }
-    __syncthreads();  // records and staging buffers are no longer read
-    if (s_abort) break;
+    __syncthreads();  // records are no longer read
+    cur ^= 1;
   }
   // no copy may land after exit
   for (int b = 0; b < 2; ++b)
