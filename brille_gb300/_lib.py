@@ -93,6 +93,8 @@ def load(build_if_missing=True):
     lib.brx_batch_tune.restype = C.c_int
     lib.brx_batch_config.argtypes = [bp, C.POINTER(C.c_int32), C.c_int32]
     lib.brx_batch_config.restype = C.c_int
+    lib.brx_batch_set_config.argtypes = [bp, C.POINTER(C.c_int32), C.c_int32]
+    lib.brx_batch_set_config.restype = C.c_int
     lib.brx_batch_launch_count.argtypes = [bp]
     lib.brx_batch_launch_count.restype = C.c_int64
     lib.brx_batch_last_error.argtypes = [bp]
@@ -101,6 +103,8 @@ def load(build_if_missing=True):
     lib.brx_tune.restype = C.c_int
     lib.brx_tuning.argtypes = [h, C.POINTER(C.c_int32), C.c_int32]
     lib.brx_tuning.restype = C.c_int
+    lib.brx_set_tuning.argtypes = [h, C.POINTER(C.c_int32), C.c_int32]
+    lib.brx_set_tuning.restype = C.c_int
     lib.brx_abi_version.argtypes = []
     lib.brx_abi_version.restype = C.c_int32
     _lib = lib

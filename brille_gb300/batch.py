@@ -20,7 +20,8 @@ from . import _abi
 from ._lib import BrxError, load
 
 _CONFIG_KEYS = ("locate_threads", "locate_ctas_per_sm", "q_per_tile", "values_smem_kb", "vectors_smem_kb",
-                "values_ctas_per_sm", "vectors_ctas_per_sm", "tiles")
+                "values_ctas_per_sm", "vectors_ctas_per_sm", "tiles", "values_gather_warps", "vectors_gather_warps",
+                "warp_min_groups", "small_q_per_group")
 
 
 def _torch():
@@ -113,6 +114,13 @@ class BatchQuery:
 
     def tune(self, stream=None, reps=2):
         self._check(load().brx_batch_tune(self._b, stream, int(reps)))
+        return self.config()
+
+    def set_config(self, cfg):
+        """Apply launch shapes as config() returns them (a dict; derived
+        entries are ignored) and re-plan; drops a captured graph."""
+        v = (C.c_int32 * len(_CONFIG_KEYS))(*(int(cfg.get(k, 0)) for k in _CONFIG_KEYS))
+        self._check(load().brx_batch_set_config(self._b, v, len(_CONFIG_KEYS)))
         return self.config()
 
     def config(self):

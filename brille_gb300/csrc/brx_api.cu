@@ -326,7 +326,12 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     if (h->vecs.present) out_q += (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
   }
   long long chunk = 1LL << 24;
-  if (o_host && out_q) chunk = std::max<long long>(1024, std::min<long long>(chunk, (512LL << 20) / (long long)out_q));
+  // host outputs: chunks of about BRX_HOST_CHUNK_MB (default 512) MB of
+  // outputs, alternating between two streams and staging buffers
+  const char* chunk_env = std::getenv("BRX_HOST_CHUNK_MB");
+  const long long chunk_mb = chunk_env ? std::atoll(chunk_env) : 0;
+  const long long host_chunk = (chunk_mb > 0 && chunk_mb <= 16384 ? chunk_mb : 512) << 20;
+  if (o_host && out_q) chunk = std::max<long long>(1024, std::min<long long>(chunk, host_chunk / (long long)out_q));
   if (chunk > n) chunk = n;
   brx_status st = ensure_scratch(h, chunk);
   if (st) return st;
@@ -770,7 +775,8 @@ static brx_status fill_one(brx_handle* h, const brx_data* d, Interp& dst, int st
   const size_t in_size = in64 ? 8 : 4;
   dst.store = storage == BRX_STORE_F64 ? ST_F64 : (storage == BRX_STORE_F32 ? ST_F32 : ST_BF16);
   const size_t out_size = dst.store == ST_F64 ? 8 : (dst.store == ST_F32 ? 4 : 2);
-  BRX_CUDA(h, dst.data.ensure(out_size * count));
+  // 16 bytes of slack: the FP32 gather copies rows in whole 16-byte units
+  BRX_CUDA(h, dst.data.ensure(out_size * count + 16));
   cudaStream_t cs = h->sc[0].stream;
   auto conv = [&](const void* src, size_t off, size_t n) {
     char* out = static_cast<char*>(dst.data.p) + out_size * off;
@@ -953,16 +959,26 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
   for (int which = 0; which < 2 && !st; ++which) {
     const Interp& d = which ? h->vecs : h->vals;
     if (!d.present || !uses_groups(d, which ? d.cplx : false)) continue;
+    // budgets per kernel: the warp-independent gather (FP32 data) and the
+    // CTA-synchronous one; the kernel choice is shared by both gathers and
+    // made on the heavier one
     size_t best_b = h->gather_budget[which];
+    int best_v = h->gather_variant;
     double best = 1e300;
-    for (size_t c : cands) {
-      if (c > h->smem_optin) continue;
-      h->gather_budget[which] = c;
-      const double t = timed(2 + which);
-      if (st) break;
-      if (t < best) { best = t; best_b = c; }
+    const bool fp32 = d.store != ST_F64;
+    for (int v : {0, 1}) {
+      if ((!fp32 || which != lead) && v != h->gather_variant) continue;
+      for (size_t c : cands) {
+        if (c > h->smem_optin || st) continue;
+        h->gather_variant = v;
+        h->gather_budget[which] = c;
+        const double t = timed(2 + which);
+        if (st) break;
+        if (t < best) { best = t; best_b = c; best_v = v; }
+      }
     }
     h->gather_budget[which] = best_b;
+    h->gather_variant = best_v;
     if (which != lead || st) continue;
     // coordinate descent over q per work descriptor, then units per thread
     int best_g = h->group_q;
@@ -981,13 +997,6 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
       if (t < best) { best = t; best_s = qs; }
     }
     h->qsplit = best_s;
-    // the classic gather against the warp-independent one (FP32 data)
-    if (d.store != ST_F64 && !st) {
-      const int keep = h->gather_variant;
-      h->gather_variant = 1 - keep;
-      const double t = timed(2 + which);
-      if (!st && !(t < best)) h->gather_variant = keep;
-    }
   }
   brx_profile(h, 0);
   h->profile = false;
@@ -1001,6 +1010,22 @@ brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n) {
   const int32_t v[5] = {(int32_t)(h->gather_budget[0] / 1024), (int32_t)(h->gather_budget[1] / 1024), h->group_q,
                         h->qsplit, h->gather_variant};
   for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
+  return BRX_OK;
+}
+
+brx_status brx_set_tuning(brx_handle* h, const int32_t* v, int32_t n) {
+  if (!h || !v || n < 5) return BRX_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 2; ++i)
+    if (v[i] < 8 || (size_t)v[i] * 1024 > h->smem_optin)
+      return fail(h, BRX_ERR_INVALID_ARGUMENT, "gather budget out of range");
+  if (v[2] < 8 || v[2] > 128) return fail(h, BRX_ERR_INVALID_ARGUMENT, "q per descriptor must be in [8, 128]");
+  if (v[3] != 1 && v[3] != 2 && v[3] != 4) return fail(h, BRX_ERR_INVALID_ARGUMENT, "units per thread: 1, 2 or 4");
+  if (v[4] != 0 && v[4] != 1) return fail(h, BRX_ERR_INVALID_ARGUMENT, "gather kernel: 0 or 1");
+  h->gather_budget[0] = (size_t)v[0] * 1024;
+  h->gather_budget[1] = (size_t)v[1] * 1024;
+  h->group_q = v[2];
+  h->qsplit = v[3];
+  h->gather_variant = v[4];
   return BRX_OK;
 }
 

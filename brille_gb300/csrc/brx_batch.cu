@@ -49,14 +49,28 @@ struct brx_batch {
   // tuned launch shapes
   int loc_threads = 128, loc_ctas = 4, tile_q = 2048;
   size_t budget_vals = 56 * 1024, budget_vecs = 56 * 1024;
-  int ctas_vals = 0, ctas_vecs = 0;
+  // gather kernels: with warp on (FP32 data), items of at least warp_min_g
+  // element groups per mode take the warp-independent gather (kGroupQ q per
+  // descriptor) and the others the CTA-synchronous one with qmax_small q
+  // per descriptor (a second descriptor list); with warp off every item
+  // takes the CTA-synchronous gather
+  bool warp = true;
+  int warp_min_g = 8, qmax_small = 64;
+  std::vector<int32_t> item_class;  // 1: CTA-synchronous gather with qmax_small
+  int n_class[2] = {0, 0};
+  bool scalar_vec = false;  // FP32 scalar values by chunks of 4 branches
   // planned from the above
   std::vector<int4> tiles;
   size_t loc_smem = 0;
-  brx::GatherBatch gb_vals{}, gb_vecs{};
-  size_t smem_vals = 0, smem_vecs = 0;
+  // one launch per item class (part) and gather
+  struct GatherPlan {
+    brx::GatherBatch gb[2];
+    size_t smem[2] = {0, 0};
+    int ctas[2] = {0, 0};
+    bool on[2] = {false, false};
+  } gp_vals, gp_vecs;
   std::vector<brx::GatherParams> pv, pc;
-  std::vector<long long> qb_off;
+  std::vector<long long> qb_off;  // first (q, branch) pair, or chunk of 4 branches, of each item
   // device memory
   DevBuf tables;   // geoms | q_off | key_off | tiles | qb_off
   DevBuf io;       // Qptr | vals params | vecs params | error words
@@ -73,6 +87,8 @@ struct brx_batch {
   const int32_t* d_key_off = nullptr;
   const int4* d_tiles = nullptr;
   const long long* d_qb_off = nullptr;
+  const int32_t* d_class = nullptr;
+  long long group_cap = 0;  // descriptors the list holds
   const double* const* d_Q = nullptr;
   brx::GatherParams* d_pv = nullptr;
   brx::GatherParams* d_pc = nullptr;
@@ -86,6 +102,7 @@ struct brx_batch {
   std::vector<void*> vout, cout;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  long long graph_launches = 0;  // kernels in the captured graph
   long long launches = 0;
   std::string message = "no error";
 };
@@ -149,14 +166,14 @@ brx::GatherParams item_params(brx_batch* b, int i, const Interp& d, int rot_mode
   p.qmax = brx::kGroupQ;
   p.q_base = b->q_off[i];
   p.err = b->d_err + i;
-  p.variant = 1;  // the batch kernel is the classic one
+  p.variant = 0;  // the batch chooses its gather kernel for all items at once
   p.key_base = b->key_off[i];
   return p;
 }
 
 // Modes per block for every item under a shared-memory budget, and the
 // batch launch dimensions (the largest item's) that fit the device.
-brx_status plan_gather(brx_batch* b, std::vector<brx::GatherParams>& P, int store, bool cplx, size_t budget,
+brx_status plan_gather(brx_batch* b, std::vector<brx::GatherParams>& P, int store, bool cplx, size_t budget, int qmax,
                        brx::GatherBatch* gb, size_t* smem, int* ctas) {
   for (auto& p : P) p.MB = brx::gather_pick_modes(p, store, cplx, budget);
   for (int round = 0; round < 64; ++round) {
@@ -167,11 +184,11 @@ brx_status plan_gather(brx_batch* b, std::vector<brx::GatherParams>& P, int stor
       na = std::max(na, p.rot_mode == brx::ROT_GAMMA ? p.nvec : 0);
       yb = std::max(yb, brx::gather_ybuf(store, cplx, p.MB, p.s));
     }
-    const size_t need = brx::gather_batch_smem(store, cplx, brx::kGroupQ, e, na, yb);
+    const size_t need = brx::gather_batch_smem(store, cplx, qmax, e, na, yb);
     bool reducible = false;
     for (const auto& p : P) reducible = reducible || p.MB > 1;
     if (need <= budget || (!reducible && need <= b->smem_optin)) {
-      gb->qmax = brx::kGroupQ;
+      gb->qmax = qmax;
       gb->e_modes = e;
       gb->ph_atoms = na;
       gb->ybuf = yb;
@@ -190,7 +207,7 @@ brx_status plan_gather(brx_batch* b, std::vector<brx::GatherParams>& P, int stor
     if (P[worst].MB <= 1) {
       // the largest buffer cannot shrink: accept what the device holds
       if (need > b->smem_optin) break;
-      gb->qmax = brx::kGroupQ;
+      gb->qmax = qmax;
       gb->e_modes = e;
       gb->ph_atoms = na;
       gb->ybuf = yb;
@@ -219,31 +236,77 @@ brx_status plan(brx_batch* b) {
   b->pv.clear();
   b->pc.clear();
   b->qb_off.assign(b->n + 1, 0);
+  b->scalar_vec = !b->vals_grouped && b->vals_store == brx::ST_F32 && !b->vals_cplx && b->out_f32;
   for (int i = 0; i < b->n; ++i) {
     brx_handle* h = b->h[i];
     b->pv.push_back(item_params(b, i, h->vals, b->vals_rot[i], false, 0));
     if (b->has_vecs) b->pc.push_back(item_params(b, i, h->vecs, b->vecs_rot[i], h->vecs.cplx, 1));
-    b->qb_off[i + 1] = b->qb_off[i] + b->nq[i] * (long long)h->vals.B;
+    const long long chunks = b->nq[i] * (long long)((h->vals.B + 3) / 4);
+    if (h->n_keys != 0 || chunks >= (1LL << 31)) b->scalar_vec = false;
   }
-  b->gb_vals = brx::GatherBatch{};
-  b->gb_vecs = brx::GatherBatch{};
+  for (int i = 0; i < b->n; ++i) {
+    const int B = b->h[i]->vals.B;
+    b->qb_off[i + 1] = b->qb_off[i] + b->nq[i] * (long long)(b->scalar_vec ? (B + 3) / 4 : B);
+  }
+  // item classes: the element groups per mode of the grouped data decide
+  const std::vector<brx::GatherParams>& lead = b->has_vecs ? b->pc : b->pv;
+  const int lead_store = b->has_vecs ? b->vecs_store : b->vals_store;
+  const bool split = b->warp && lead_store != brx::ST_F64;
+  b->item_class.assign(b->n, 0);
+  b->n_class[0] = b->n_class[1] = 0;
+  for (int i = 0; i < b->n; ++i) {
+    const int G = lead[i].nsc + lead[i].nvec;
+    if (split && G < b->warp_min_g) b->item_class[i] = 1;
+    ++b->n_class[b->item_class[i]];
+  }
+  // the gathers, one launch per non-empty class: class 0 the warp-independent
+  // kernel if on and its items fit it, else (and class 1) the classic kernel
+  // under the shared-memory budget
+  auto plan_one = [&](std::vector<brx::GatherParams>& P, int store, bool cplx, size_t budget,
+                      brx_batch::GatherPlan* gp) -> brx_status {
+    *gp = brx_batch::GatherPlan{};
+    for (int c = 0; c < 2; ++c) {
+      std::vector<brx::GatherParams> Pc;
+      for (int i = 0; i < b->n; ++i)
+        if (b->item_class[i] == c) Pc.push_back(P[i]);
+      if (Pc.empty()) continue;
+      const int qmax = c == 1 ? b->qmax_small : brx::kGroupQ;
+      for (auto& p : Pc) p.qmax = qmax;
+      gp->on[c] = true;
+      if (c == 0 && b->warp &&
+          brx::gather_warp_plan(store, cplx, b->out_f32, Pc.data(), (int)Pc.size(), qmax, budget, &gp->gb[c],
+                                &gp->smem[c], &gp->ctas[c]))
+        continue;
+      gp->gb[c] = brx::GatherBatch{};
+      brx_status st = plan_gather(b, Pc, store, cplx, budget, qmax, &gp->gb[c], &gp->smem[c], &gp->ctas[c]);
+      if (st) return st;
+      // the modes per block chosen for the class's items
+      for (int i = 0, k = 0; i < b->n; ++i)
+        if (b->item_class[i] == c) P[i].MB = Pc[k++].MB;
+    }
+    return BRX_OK;
+  };
   if (b->vals_grouped) {
-    brx_status st = plan_gather(b, b->pv, b->vals_store, b->vals_cplx, b->budget_vals, &b->gb_vals, &b->smem_vals,
-                                &b->ctas_vals);
+    brx_status st = plan_one(b->pv, b->vals_store, b->vals_cplx, b->budget_vals, &b->gp_vals);
     if (st) return st;
   }
   if (b->has_vecs) {
-    brx_status st = plan_gather(b, b->pc, b->vecs_store, b->vecs_cplx, b->budget_vecs, &b->gb_vecs, &b->smem_vecs,
-                                &b->ctas_vecs);
+    brx_status st = plan_one(b->pc, b->vecs_store, b->vecs_cplx, b->budget_vecs, &b->gp_vecs);
     if (st) return st;
   }
-  // device tables: geoms | q_off | key_off | tiles | qb_off
+  for (int i = 0; i < b->n; ++i) {
+    const int qmax = b->item_class[i] == 1 ? b->qmax_small : brx::kGroupQ;
+    b->pv[i].qmax = qmax;
+    if (b->has_vecs) b->pc[i].qmax = qmax;
+  }
+  // device tables: geoms | q_off | key_off | tiles | qb_off | item classes
   const size_t o_geom = 0;
   const size_t o_qoff = align256(o_geom + sizeof(brx::DevGeom) * b->n);
   const size_t o_koff = align256(o_qoff + sizeof(long long) * (b->n + 1));
   const size_t o_tile = align256(o_koff + sizeof(int32_t) * b->n);
   const size_t o_qb = align256(o_tile + sizeof(int4) * std::max<size_t>(1, b->tiles.size()));
-  const size_t total = align256(o_qb + sizeof(long long) * (b->n + 1));
+  const size_t o_cls = align256(o_qb + sizeof(long long) * (b->n + 1));
+  const size_t total = align256(o_cls + sizeof(int32_t) * b->n);
   BB_CUDA(b, b->tables.ensure(total));
   std::vector<unsigned char> host(total, 0);
   for (int i = 0; i < b->n; ++i) std::memcpy(host.data() + o_geom + sizeof(brx::DevGeom) * i, &b->h[i]->g, sizeof(brx::DevGeom));
@@ -251,6 +314,7 @@ brx_status plan(brx_batch* b) {
   std::memcpy(host.data() + o_koff, b->key_off.data(), sizeof(int32_t) * b->n);
   if (!b->tiles.empty()) std::memcpy(host.data() + o_tile, b->tiles.data(), sizeof(int4) * b->tiles.size());
   std::memcpy(host.data() + o_qb, b->qb_off.data(), sizeof(long long) * (b->n + 1));
+  std::memcpy(host.data() + o_cls, b->item_class.data(), sizeof(int32_t) * b->n);
   BB_CUDA(b, cudaMemcpy(b->tables.p, host.data(), total, cudaMemcpyHostToDevice));
   unsigned char* base = static_cast<unsigned char*>(b->tables.p);
   b->d_geoms = reinterpret_cast<const brx::DevGeom*>(base + o_geom);
@@ -258,16 +322,23 @@ brx_status plan(brx_batch* b) {
   b->d_key_off = reinterpret_cast<const int32_t*>(base + o_koff);
   b->d_tiles = reinterpret_cast<const int4*>(base + o_tile);
   b->d_qb_off = reinterpret_cast<const long long*>(base + o_qb);
-  auto fill_gb = [&](brx::GatherBatch& gb, brx::GatherParams* items, int which) {
-    gb.items = items;
-    gb.key_off = b->d_key_off;
-    gb.n_items = b->n;
-    gb.groups = b->groups;
-    gb.n_groups = b->n_groups;
-    gb.counter = b->counters + which;
+  b->d_class = reinterpret_cast<const int32_t*>(base + o_cls);
+  // class 0 descriptors upwards from the start of the list, class 1
+  // downwards from its end
+  auto fill_gb = [&](brx_batch::GatherPlan& gp, brx::GatherParams* items, int which) {
+    for (int c = 0; c < 2; ++c) {
+      brx::GatherBatch& gb = gp.gb[c];
+      gb.items = items;
+      gb.key_off = b->d_key_off;
+      gb.n_items = b->n;
+      gb.groups = c == 0 ? b->groups : b->groups + b->group_cap;
+      gb.reverse = c;
+      gb.n_groups = b->n_groups + c;
+      gb.counter = b->counters + 2 * which + c;
+    }
   };
-  fill_gb(b->gb_vals, b->d_pv, 0);
-  fill_gb(b->gb_vecs, b->d_pc, 1);
+  fill_gb(b->gp_vals, b->d_pv, 0);
+  fill_gb(b->gp_vecs, b->d_pc, 1);
   return BRX_OK;
 }
 
@@ -304,24 +375,38 @@ long long enqueue(brx_batch* b, cudaStream_t s, cudaEvent_t* stage_ev) {
                            b->num_sms * b->loc_ctas, s);
   ++k;
   mark(1);
-  if (b->vals_grouped || b->vecs_grouped)
+  if (b->vals_grouped || b->vecs_grouped) {
+    brx::GroupSplit split;
+    if (b->n_class[1] > 0) {
+      split.key_off = b->d_key_off;
+      split.item_class = b->d_class;
+      split.n_items = b->n;
+      split.qmax = b->qmax_small;
+      split.groups_end = b->groups + b->group_cap;
+      split.n_groups = b->n_groups + 1;
+    }
     k += brx::launch_grouping(b->r.key, b->total_q, b->total_keys, brx::kGroupQ, b->sort_scratch, b->order,
-                              b->groups, b->n_groups, s);
+                              b->groups, b->n_groups, s, split);
+  }
   mark(2);
+  auto gathers = [&](const brx_batch::GatherPlan& gp, int store, bool cplx) {
+    for (int c = 0; c < 2; ++c)
+      if (gp.on[c]) {
+        brx::launch_gather_batch(gp.gb[c], store, cplx, b->out_f32, b->num_sms, gp.smem[c], gp.ctas[c], s);
+        ++k;
+      }
+  };
   if (b->vals_grouped) {
-    brx::launch_gather_batch(b->gb_vals, b->vals_store, b->vals_cplx, b->out_f32, b->num_sms, b->smem_vals,
-                             b->ctas_vals, s);
+    gathers(b->gp_vals, b->vals_store, b->vals_cplx);
+  } else if (b->scalar_vec) {
+    brx::launch_scalar_batch_vec(b->d_pv, b->d_qb_off, b->n, b->qb_off[b->n], b->num_sms, s);
   } else {
     brx::launch_scalar_batch(b->d_pv, b->d_qb_off, b->n, b->qb_off[b->n], b->vals_store, b->vals_cplx, b->out_f32,
                              b->num_sms, s);
   }
-  ++k;
+  if (!b->vals_grouped) ++k;
   mark(3);
-  if (b->has_vecs) {
-    brx::launch_gather_batch(b->gb_vecs, b->vecs_store, b->vecs_cplx, b->out_f32, b->num_sms, b->smem_vecs,
-                             b->ctas_vecs, s);
-    ++k;
-  }
+  if (b->has_vecs) gathers(b->gp_vecs, b->vecs_store, b->vecs_cplx);
   mark(4);
   cudaMemcpyAsync(b->err_host, b->d_err, sizeof(brx::ErrorWord) * b->n, cudaMemcpyDeviceToHost, s);
   return k;
@@ -432,6 +517,7 @@ brx_status brx_batch_create(brx_handle* const* handles, int32_t n, const int64_t
   b->sort_scratch = static_cast<int32_t*>(b->sortbuf.p);
   if (b->groupbuf.ensure(sizeof(brx::GroupDesc) * m + 256) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
   b->groups = static_cast<brx::GroupDesc*>(b->groupbuf.p);
+  b->group_cap = (long long)m;  // both descriptor lists together hold at most one per q
   b->n_groups = reinterpret_cast<int32_t*>(static_cast<char*>(b->groupbuf.p) + sizeof(brx::GroupDesc) * m + 64);
   b->counters = b->n_groups + 16;
   brx_status st = alloc_io(b);
@@ -508,7 +594,7 @@ brx_status brx_batch_capture(brx_batch* b, void* stream) {
   if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
   cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    enqueue(b, cap, nullptr);
+    b->graph_launches = enqueue(b, cap, nullptr);
     e = cudaStreamEndCapture(cap, &b->graph);
   }
   if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
@@ -525,7 +611,7 @@ brx_status brx_batch_launch(brx_batch* b, void* stream) {
   if (!b->exec) return brx_batch_run(b, stream);
   BB_CUDA(b, cudaSetDevice(b->device));
   BB_CUDA(b, cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)));
-  b->launches += 3 + (b->vals_grouped || b->vecs_grouped ? 7 : 0) + (b->has_vecs ? 1 : 0);
+  b->launches += b->graph_launches;
   return BRX_OK;
 }
 
@@ -590,9 +676,53 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
     b->loc_ctas = bc;
     b->tile_q = bq;
   }
-  // gathers: shared-memory budget per CTA (modes per block, CTAs per SM)
+  // gathers (the grouped one: vectors, else values), coordinate descent:
+  // budget per kernel choice (warp off; warp on for every item), then the
+  // class split, then the q per descriptor of the small class
   const size_t budgets[] = {24 * 1024, 40 * 1024, 56 * 1024, 80 * 1024, 112 * 1024};
-  if (!st && b->vals_grouped) {
+  const bool vecs = b->has_vecs;
+  if (!st && (vecs || b->vals_grouped)) {
+    size_t* budget = vecs ? &b->budget_vecs : &b->budget_vals;
+    const int from = vecs ? 3 : 2, to = vecs ? 4 : 3;
+    const int lead_store = vecs ? b->vecs_store : b->vals_store;
+    bool bw = b->warp;
+    size_t bb = *budget;
+    int bg = b->warp_min_g, bq = b->qmax_small;
+    float best = 1e30f;
+    auto trial = [&]() -> float {
+      if (plan(b)) return 1e30f;
+      stage_io(b);
+      return time_run(from, to);
+    };
+    for (int w = 0; w < (lead_store != brx::ST_F64 ? 2 : 1); ++w)
+      for (size_t bud : budgets) {
+        if (bud > b->smem_optin) continue;
+        b->warp = w == 1;
+        b->warp_min_g = 0;
+        *budget = bud;
+        const float t = trial();
+        if (t < best) { best = t; bb = bud; bw = b->warp; bg = 0; }
+      }
+    b->warp = bw;
+    *budget = bb;
+    b->warp_min_g = bg;
+    if (bw) {
+      for (int g : {4, 8, 16}) {
+        b->warp_min_g = g;
+        const float t = trial();
+        if (t < best) { best = t; bg = g; }
+      }
+      b->warp_min_g = bg;
+      if (bg > 0)
+        for (int q : {32, 64, 128}) {
+          b->qmax_small = q;
+          const float t = trial();
+          if (t < best) { best = t; bq = q; }
+        }
+      b->qmax_small = bq;
+    }
+  }
+  if (!st && vecs && b->vals_grouped) {
     size_t bb = b->budget_vals;
     float best = 1e30f;
     for (size_t bud : budgets) {
@@ -605,19 +735,6 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
     }
     b->budget_vals = bb;
   }
-  if (!st && b->has_vecs) {
-    size_t bb = b->budget_vecs;
-    float best = 1e30f;
-    for (size_t bud : budgets) {
-      if (bud > b->smem_optin) continue;
-      b->budget_vecs = bud;
-      if (plan(b)) continue;
-      stage_io(b);
-      const float t = time_run(3, 4);
-      if (t < best) { best = t; bb = bud; }
-    }
-    b->budget_vecs = bb;
-  }
   for (auto& e : ev) cudaEventDestroy(e);
   if (st) return st;
   st = plan(b);
@@ -628,9 +745,42 @@ brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps) {
 
 brx_status brx_batch_config(const brx_batch* b, int32_t* cfg, int32_t n) {
   if (!b || !cfg || n < 1) return BRX_ERR_INVALID_ARGUMENT;
-  const int32_t v[8] = {b->loc_threads, b->loc_ctas, b->tile_q, (int32_t)(b->budget_vals / 1024),
-                        (int32_t)(b->budget_vecs / 1024), b->ctas_vals, b->ctas_vecs, (int32_t)b->tiles.size()};
-  for (int i = 0; i < n && i < 8; ++i) cfg[i] = v[i];
+  auto ctas = [](const brx_batch::GatherPlan& gp) { return gp.on[0] ? gp.ctas[0] : gp.ctas[1]; };
+  auto warps = [](const brx_batch::GatherPlan& gp) { return gp.on[0] ? gp.gb[0].warps : 0; };
+  const int32_t v[12] = {b->loc_threads, b->loc_ctas, b->tile_q, (int32_t)(b->budget_vals / 1024),
+                         (int32_t)(b->budget_vecs / 1024), ctas(b->gp_vals), ctas(b->gp_vecs),
+                         (int32_t)b->tiles.size(), warps(b->gp_vals), warps(b->gp_vecs),
+                         b->warp ? b->warp_min_g : -1, b->n_class[1] > 0 ? b->qmax_small : 0};
+  for (int i = 0; i < n && i < 12; ++i) cfg[i] = v[i];
+  return BRX_OK;
+}
+
+brx_status brx_batch_set_config(brx_batch* b, const int32_t* cfg, int32_t n) {
+  if (!b || !cfg || n < 5) return BRX_ERR_INVALID_ARGUMENT;
+  if (cfg[0] != 64 && cfg[0] != 128 && cfg[0] != 256)
+    return bfail(b, BRX_ERR_INVALID_ARGUMENT, "locate threads: 64, 128 or 256");
+  if (cfg[1] < 1 || cfg[0] * cfg[1] > 2048) return bfail(b, BRX_ERR_INVALID_ARGUMENT, "locate CTAs per SM out of range");
+  if (cfg[2] < 64 || cfg[2] > (1 << 20)) return bfail(b, BRX_ERR_INVALID_ARGUMENT, "q per tile must be in [64, 2^20]");
+  for (int i = 3; i < 5; ++i)
+    if (cfg[i] < 8 || (size_t)cfg[i] * 1024 > b->smem_optin)
+      return bfail(b, BRX_ERR_INVALID_ARGUMENT, "gather budget out of range");
+  b->loc_threads = cfg[0];
+  b->loc_ctas = cfg[1];
+  b->tile_q = cfg[2];
+  b->budget_vals = (size_t)cfg[3] * 1024;
+  b->budget_vecs = (size_t)cfg[4] * 1024;
+  if (n > 10) {
+    if (cfg[10] > 64) return bfail(b, BRX_ERR_INVALID_ARGUMENT, "warp gather minimum element groups out of range");
+    b->warp = cfg[10] >= 0;
+    if (b->warp) b->warp_min_g = cfg[10];
+  }
+  if (n > 11 && cfg[11] != 0) {
+    if (cfg[11] < 8 || cfg[11] > 128) return bfail(b, BRX_ERR_INVALID_ARGUMENT, "q per descriptor must be in [8, 128]");
+    b->qmax_small = cfg[11];
+  }
+  brx_status st = plan(b);
+  if (st) return st;
+  if (b->io_set) stage_io(b);
   return BRX_OK;
 }
 

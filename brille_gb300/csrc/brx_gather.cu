@@ -16,6 +16,7 @@
 // (src/interpolator_gamma.tpp:49-139).
 #include <cuda_bf16.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "../../include/brx.h"
@@ -354,7 +355,7 @@ __device__ __forceinline__ void fetch_group(const GatherBatch& gb, int n_groups,
     if (lane == 0) gi->count = -1;
     return;
   }
-  const GroupDesc d = gb.groups[g];
+  const GroupDesc d = gb.reverse ? gb.groups[-1 - g] : gb.groups[g];
   int key = d.key;
   if (gb.items) {
     int item = 0;
@@ -871,13 +872,13 @@ constexpr int kWarpGatherMaxWarps = 8;
 constexpr long long kGatherSpin = 2000000000LL;
 
 struct WarpLayout {
-  size_t q, oq, w, M, rotf, ph, de, e, Y, mbar, total;
-  int row_bytes;  // one staged row: the data row plus 16 bytes
-  size_t ybuf;    // one staging buffer: 8 slots × MBw rows
+  size_t q, oq, w, M, rotf, ph, de, e, off, Y, mbar, total;
+  size_t ybuf;  // bytes of one staging buffer
 };
 
-template <typename St, bool CPLX>
-__host__ __device__ inline WarpLayout warp_layout(int QM, int MBw, int s, int na, int warps) {
+// QM q per group; e_modes antiphase entries per slot and warp; na Γ phases
+// per q; ybuf bytes per staging buffer (two per warp)
+__host__ __device__ inline WarpLayout warp_layout(int QM, int e_modes, int na, long long ybuf, int warps) {
   WarpLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -893,21 +894,53 @@ __host__ __device__ inline WarpLayout warp_layout(int QM, int MBw, int s, int na
   L.rotf = take(4 * (size_t)QM);
   L.ph = take(4 * 2 * (size_t)nan * QM);
   L.de = take(4 * (size_t)nan * QM);
-  L.e = take(4 * 2 * 8 * (size_t)MBw * warps);
-  L.row_bytes = s * (CPLX ? 2 : 1) * (int)sizeof(St) + 16;
-  L.ybuf = (size_t)8 * MBw * L.row_bytes;
+  L.e = take(4 * 2 * 8 * (size_t)e_modes * warps);
+  L.off = take(2 * 8 * (size_t)e_modes * warps);
+  L.ybuf = ((size_t)ybuf + 15) & ~size_t(15);
   L.Y = take(2 * L.ybuf * warps);
   L.mbar = take(16 * (size_t)warps);
   L.total = (o + 15) & ~size_t(15);
   return L;
 }
 
+// Shape of one interpolator in the warp gather: modes per warp block MBw
+// (at most 32 units of (mode, element group) per warp where G ≤ 32, within
+// the launch's e_modes and ybuf), staged row stride: the data row rounded up to 16 bytes
+// (a row copied from a 16-byte aligned address below its start fits) plus
+// 16 bytes that shift successive rows across the shared-memory banks.
+struct WarpItem {
+  int B, s, G, na, MBw, nblk, row_bytes;
+  bool gamma;
+};
+
+template <typename St, bool CPLX>
+__host__ __device__ inline WarpItem warp_item(const GatherParams& P, int e_modes, long long ybuf) {
+  WarpItem w;
+  w.B = P.B;
+  w.s = P.s;
+  w.G = P.nsc + P.nvec;
+  w.gamma = P.rot_mode == ROT_GAMMA;
+  w.na = w.gamma ? P.nvec : 0;
+  w.row_bytes = ((P.s * (CPLX ? 2 : 1) * (int)sizeof(St) + 15) & ~15) + 16;
+  int m = w.G > 0 ? 32 / w.G : 32;
+  if (m < 1) m = 1;
+  if (m > w.B) m = w.B;
+  if (m > e_modes) m = e_modes;
+  while (m > 1 && 8LL * m * w.row_bytes > ybuf) --m;
+  w.MBw = m;
+  w.nblk = (w.B + m - 1) / m;
+  return w;
+}
+
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ void g_mbar_init(uint32_t m) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(m) : "memory");
 }
-__device__ __forceinline__ void g_expect_tx(uint32_t m, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(m), "r"(bytes) : "memory");
+__device__ __forceinline__ void g_expect(uint32_t m, uint32_t bytes) {
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(m), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void g_arrive(uint32_t m) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(m) : "memory");
 }
 __device__ __forceinline__ void g_bulk(uint32_t dst, const void* src, uint32_t bytes, uint32_t m) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
@@ -928,22 +961,26 @@ __device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase) {
   }
 }
 
+// single: the one interpolator's parameters (gb.items null); otherwise a
+// batch whose groups carry their item's parameters.  gb.qmax, e_modes,
+// ph_atoms and ybuf give the shared-memory layout in either case.
 template <typename St, bool CPLX, typename Out>
-__global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kernel(GatherParams p) {
+__global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kernel(GatherParams p, GatherBatch gb) {
   using Acc = float;
   constexpr int comps = CPLX ? 2 : 1;
   extern __shared__ __align__(16) unsigned char sm[];
-  __shared__ GatherParams s_par;
+  __shared__ GatherParams s_par[2];
   __shared__ GroupInfo s_g[2];
   __shared__ int s_abort;
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
-  for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth)
-    reinterpret_cast<int*>(&s_par)[w] = reinterpret_cast<const int*>(&p)[w];
-  const int B = p.B, s = p.s, MBw = p.MB, QM = p.qmax;
-  const bool gamma = p.rot_mode == ROT_GAMMA;
-  const int na = gamma ? p.nvec : 0;
-  const int G = p.nsc + p.nvec;
-  const WarpLayout L = warp_layout<St, CPLX>(QM, MBw, s, na, nwarps);
+  const bool batch = gb.items != nullptr;
+  if (!batch)
+    for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth) {
+      reinterpret_cast<int*>(&s_par[0])[w] = reinterpret_cast<const int*>(&p)[w];
+      reinterpret_cast<int*>(&s_par[1])[w] = reinterpret_cast<const int*>(&p)[w];
+    }
+  const int QM = gb.qmax;
+  const WarpLayout L = warp_layout(QM, gb.e_modes, gb.ph_atoms, gb.ybuf, nwarps);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
   long long* s_oq = reinterpret_cast<long long*>(sm + L.oq);
   Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
@@ -951,7 +988,8 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
   int* s_rotf = reinterpret_cast<int*>(sm + L.rotf);
   Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
   int* s_de = reinterpret_cast<int*>(sm + L.de);
-  Acc* s_e = reinterpret_cast<Acc*>(sm + L.e) + (size_t)warp * 2 * 8 * MBw;
+  Acc* s_e = reinterpret_cast<Acc*>(sm + L.e) + (size_t)warp * 2 * 8 * gb.e_modes;
+  unsigned char* s_off = sm + L.off + (size_t)warp * 2 * 8 * gb.e_modes;  // row start in its staged copy
   unsigned char* Yw = sm + L.Y + (size_t)warp * 2 * L.ybuf;
   const uint32_t mbar = smem_addr(sm + L.mbar) + 16 * warp;
   if (lane == 0) {
@@ -961,47 +999,59 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
   if (tid == 0) s_abort = 0;
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   __syncthreads();
-  GatherBatch gb{};
-  gb.groups = p.groups;
-  gb.n_groups = p.n_groups;
-  gb.counter = p.counter;
-  const int n_groups = *p.n_groups;
-  const int nblk = (B + MBw - 1) / MBw;
-  const uint32_t row_g = (uint32_t)(s * comps * sizeof(St));  // bytes of one data row
-  const St* data = reinterpret_cast<const St*>(p.data);
-  Out* out = reinterpret_cast<Out*>(p.out);
+  const int n_groups = *gb.n_groups;
   uint32_t phase[2] = {0u, 0u};
   bool pending[2] = {false, false};
   bool ok = true;
 
-  // rows of block blk into buffer buf: one bulk copy per (used slot, mode)
-  auto issue = [&](const GroupInfo& gi, int blk, int buf) {
-    const int b0 = blk * MBw, mb = min(MBw, B - b0), ns = gi.nslot - gi.pivot;
+  // rows of block blk of a group into buffer buf: one bulk copy per (used
+  // slot, mode), the item's own row size and modes per block.  A copy
+  // starts at the 16-byte boundary at or below its row and covers whole
+  // 16-byte units (the data buffers carry 16 bytes of slack at their end);
+  // each lane adds its copies' bytes to the barrier's expected count before
+  // issuing them, and lane 0 arrives once all lanes have.
+  auto issue = [&](const GatherParams& P, const WarpItem& it, const GroupInfo& gi, int blk, int buf) {
+    const int b0 = blk * it.MBw, mb = min(it.MBw, it.B - b0), ns = gi.nslot - gi.pivot;
     const int rows = ns * mb;
+    const uint32_t row_g = (uint32_t)(it.s * comps * (int)sizeof(St));
     const uint32_t m = mbar + 8 * buf;
-    if (lane == 0) g_expect_tx(m, (uint32_t)rows * row_g);
-    __syncwarp();
     unsigned char* Yb = Yw + (size_t)buf * L.ybuf;
+    const unsigned char* data = static_cast<const unsigned char*>(P.data);
     for (int r = lane; r < rows; r += 32) {
       const int x = gi.pivot + r / mb, mm = r % mb, b = b0 + mm;
       const int pid = gi.pid[x];
-      const int row = pid >= 0 ? __ldg(s_par.perms + (long long)pid * B + b) : b;
-      const St* src = data + ((long long)gi.vid[x] * B + row) * s * comps;
-      g_bulk(smem_addr(Yb + (size_t)(x * MBw + mm) * L.row_bytes), src, row_g, m);
+      const int row = pid >= 0 ? __ldg(P.perms + (long long)pid * it.B + b) : b;
+      const unsigned char* src = data + ((long long)gi.vid[x] * it.B + row) * (long long)row_g;
+      const uint32_t off = (uint32_t)((uintptr_t)src & 15);
+      const uint32_t cb = (off + row_g + 15) & ~15u;
+      s_off[buf * 8 * gb.e_modes + x * it.MBw + mm] = (unsigned char)off;
+      g_expect(m, cb);
+      g_bulk(smem_addr(Yb + (size_t)(x * it.MBw + mm) * it.row_bytes), src - off, cb, m);
     }
+    __syncwarp();
+    if (lane == 0) g_arrive(m);
     pending[buf] = true;
   };
 
   int cur = 0, buf = 0;
-  if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g[0], lane);
+  if (warp == 0) fetch_group(gb, n_groups, &s_par[0], &s_g[0], lane);
   __syncthreads();
-  if (s_g[0].count >= 0 && warp < nblk) issue(s_g[0], warp, 0);
+  if (s_g[0].count >= 0) {
+    const WarpItem it0 = warp_item<St, CPLX>(s_par[0], gb.e_modes, L.ybuf);
+    const int wq0 = it0.nblk >= nwarps ? 1 : nwarps / it0.nblk;
+    if (warp < it0.nblk * wq0) issue(s_par[0], it0, s_g[0], warp % it0.nblk, 0);
+  }
   for (;;) {
     const GroupInfo& gc = s_g[cur];
     if (gc.count < 0 || s_abort) break;
+    const GatherParams& p = s_par[cur];
+    const WarpItem itm = warp_item<St, CPLX>(p, gb.e_modes, L.ybuf);
+    const int B = itm.B, s = itm.s, MBw = itm.MBw, G = itm.G, na = itm.na, nblk = itm.nblk;
+    const bool gamma = itm.gamma;
+    Out* out = reinterpret_cast<Out*>(p.out);
     // the next descriptor is taken now; its first rows load before the
     // group barrier at the end
-    if (warp == 0) fetch_group(gb, n_groups, &s_par, &s_g[cur ^ 1], lane);
+    if (warp == 0) fetch_group(gb, n_groups, &s_par[cur ^ 1], &s_g[cur ^ 1], lane);
     const int count = gc.count, start = gc.start, nslot = gc.nslot, pivot = gc.pivot;
     // per-q records over all threads: weights by slot, the 3×3 applied to
     // vectors, output offsets ...
@@ -1070,8 +1120,14 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
       }
     }
     __syncthreads();
-    for (int blk = warp; blk < nblk && ok; blk += nwarps) {
-      if (blk + nwarps < nblk) issue(gc, blk + nwarps, buf ^ 1);
+    // fewer blocks than warps: wq warps share each block, taking every
+    // wq-th q from their slice (a warp beyond nblk·wq idles this group)
+    const int wq = nblk >= nwarps ? 1 : nwarps / nblk;
+    const int wslice = wq > 1 ? warp / nblk : 0;
+    const int bfirst = wq > 1 ? (warp < nblk * wq ? warp % nblk : nblk) : warp;
+    const int bstep = wq > 1 ? nblk : nwarps;
+    for (int blk = bfirst; blk < nblk && ok; blk += bstep) {
+      if (blk + bstep < nblk) issue(p, itm, gc, blk + bstep, buf ^ 1);
       bool got = g_wait(mbar + 8 * buf, phase[buf]);
       got = __all_sync(0xffffffffu, got);
       if (!got) {
@@ -1081,6 +1137,8 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
       phase[buf] ^= 1u;
       pending[buf] = false;
       const unsigned char* Yb = Yw + (size_t)buf * L.ybuf;
+      const unsigned char* so = s_off + buf * 8 * gb.e_modes;
+      const int row_bytes = itm.row_bytes;
       const int b0 = blk * MBw, mb = min(MBw, B - b0);
       // antiphase of every (slot, mode), two lanes each
       const int npairs = (nslot - pivot) * mb;
@@ -1092,8 +1150,9 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
           x = pivot + pr / mb;
           mm = pr % mb;
           if (CPLX && p.phase_allowed && x != pivot) {
-            const St* a = reinterpret_cast<const St*>(Yb + (size_t)(pivot * MBw + mm) * L.row_bytes);
-            const St* c = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+            const St* a = reinterpret_cast<const St*>(Yb + (size_t)(pivot * MBw + mm) * row_bytes +
+                                                      so[pivot * MBw + mm]);
+            const St* c = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
             for (int e = half; e < s; e += 2) {
               Acc ar, ai, br, bi;
               ldY<Acc, St, CPLX>(a + 2 * e, ar, ai);
@@ -1119,8 +1178,13 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
         }
       }
       __syncwarp();
-      // one (mode, element group) unit per lane, over every q of the group
-      for (int u = lane; u < mb * G; u += 32) {
+      // one (mode, element group) unit per lane over its q: with U < 32
+      // units, lane slices of U lanes take every qs-th q of the warp's share
+      const int U = mb * G;
+      const int qs = U >= 32 ? 1 : 32 / U;
+      const int lslice = U >= 32 ? 0 : lane / U;
+      const int jstep = wq * qs, j0 = wslice * qs + lslice;
+      for (int u = U >= 32 ? lane : lane % U; u < U && lslice < qs; u += 32) {
         const int mm = u / G, gi = u % G, bb = b0 + mm;
         const int e0 = gi < p.nsc ? gi : p.nsc + 3 * (gi - p.nsc);
         const int ne = gi < p.nsc ? 1 : 3;
@@ -1131,7 +1195,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
           for (int x = 0; x < 8; ++x) {
             const bool usex = x >= pivot;
             const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
-            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               Acc dr = 0, di = 0;
@@ -1141,10 +1205,10 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
             }
           }
           if (ne == 3) {
-            vector_unit<8, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, 0, count, 1, gamma, na,
+            vector_unit<8, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, j0, count, jstep, gamma, na,
                                            gi - p.nsc, e0, row_off, out);
           } else {
-            for (int j = 0; j < count; ++j) {
+            for (int j = j0; j < count; j += jstep) {
               Acc vr = 0, vi = 0;
 #pragma unroll
               for (int x = 0; x < 8; ++x) {
@@ -1160,7 +1224,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
           for (int x = 0; x < 4; ++x) {
             const bool usex = x >= pivot;
             const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
-            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * L.row_bytes);
+            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               Acc dr = 0, di = 0;
@@ -1170,10 +1234,10 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
             }
           }
           if (ne == 3) {
-            vector_unit<4, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, 0, count, 1, gamma, na,
+            vector_unit<4, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, j0, count, jstep, gamma, na,
                                            gi - p.nsc, e0, row_off, out);
           } else {
-            for (int j = 0; j < count; ++j) {
+            for (int j = j0; j < count; j += jstep) {
               Acc vr = 0, vi = 0;
 #pragma unroll
               for (int x = 0; x < 4; ++x) {
@@ -1190,7 +1254,11 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
     }
     // this warp's first block of the next group (both buffers are free)
     const GroupInfo& gn = s_g[cur ^ 1];
-    if (ok && gn.count >= 0 && warp < nblk) issue(gn, warp, buf);
+    if (ok && gn.count >= 0) {
+      const WarpItem itn = warp_item<St, CPLX>(s_par[cur ^ 1], gb.e_modes, L.ybuf);
+      const int wqn = itn.nblk >= nwarps ? 1 : nwarps / itn.nblk;
+      if (warp < itn.nblk * wqn) issue(s_par[cur ^ 1], itn, gn, warp % itn.nblk, buf);
+    }
     if (!ok && lane == 0) {
       atomicExch(&s_abort, 1);
       atomicOr(&p.err->flags, 1 << BRX_ERR_TIMEOUT);
@@ -1300,6 +1368,59 @@ __global__ void scalar_gather_batch_kernel(const GatherParams* items, const long
   }
 }
 
+// FP32 scalar values of a batch without permutation tables: one thread per
+// (item, q, chunk of 4 branches), qc_off[i] the first chunk of item i; the
+// record is read once per chunk, rows and outputs move as float4 where the
+// item's B is a multiple of 4 and its data and output are 16-byte aligned,
+// else element by element.  Same sum order as scalar_one.
+__global__ void scalar_gather_batch_vec_kernel(const GatherParams* items, const long long* qc_off, int n_items,
+                                               long long total) {
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    int lo = 0, hi = n_items - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(qc_off + mid) <= it) lo = mid;
+      else hi = mid - 1;
+    }
+    const GatherParams& p = items[lo];
+    const int B = p.B, nch = (B + 3) >> 2;
+    const int local = (int)(it - __ldg(qc_off + lo));
+    const int qo = local / nch, c = local - qo * nch;
+    const long long qi = p.q_base + qo;
+    if (p.status[qi]) continue;
+    const int nw = p.nw[qi];
+    const float* data = static_cast<const float*>(p.data);
+    float* out = static_cast<float*>(p.out) + (size_t)qo * B + 4 * c;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if ((B & 3) == 0 && (((uintptr_t)data | (uintptr_t)out) & 15) == 0) {
+      for (int x = 0; x < nw; ++x) {
+        const int v = p.vidx[8 * qi + x];
+        const float w = p.w32[8 * qi + x];
+        const float4 d = __ldg(reinterpret_cast<const float4*>(data + (size_t)v * B) + c);
+        acc[0] = Ar<float>::add(acc[0], Ar<float>::mul(w, d.x));
+        acc[1] = Ar<float>::add(acc[1], Ar<float>::mul(w, d.y));
+        acc[2] = Ar<float>::add(acc[2], Ar<float>::mul(w, d.z));
+        acc[3] = Ar<float>::add(acc[3], Ar<float>::mul(w, d.w));
+      }
+      *reinterpret_cast<float4*>(out) = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    } else {
+      const int nb = min(4, B - 4 * c);
+      for (int x = 0; x < nw; ++x) {
+        const int v = p.vidx[8 * qi + x];
+        const float w = p.w32[8 * qi + x];
+        const float* row = data + (size_t)v * B + 4 * c;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (k < nb) acc[k] = Ar<float>::add(acc[k], Ar<float>::mul(w, __ldg(row + k)));
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (k < nb) out[k] = acc[k];
+    }
+  }
+}
+
 template <typename Acc, typename St, bool CPLX>
 static size_t layout_bytes(const GatherParams& p, int MB) {
   const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
@@ -1320,42 +1441,79 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
   return (p.B + nblk - 1) / nblk;
 }
 
-// The warp-independent FP32 gather when the data fit it: vectors and scalars
-// only, rows a multiple of 16 bytes at 16-byte aligned addresses, shared
-// memory for 8 (or 4) warps.  Returns false when the classic kernel must run.
+// Launch shape of the warp-independent FP32 gather over n interpolators:
+// vectors and scalars only, data at 16-byte aligned addresses with 16 bytes
+// of slack at the end.  Shared memory is sized from the largest item: the
+// first of (8 warps, then 4) × (modes per block from the most down to 1)
+// within the budget per CTA, else the first the device holds.  Fills gb's
+// layout fields and warps; false when the classic kernel must run.  Raises
+// the kernel's shared-memory limit (not capturable: call before a stream
+// capture).
 template <typename St, bool CPLX, typename Out>
-static bool launch_warp(const GatherParams& p, int num_sms, cudaStream_t s) {
+static bool warp_plan(const GatherParams* P, int n, int qmax, size_t budget, GatherBatch* gb, size_t* smem_out,
+                      int* per_sm_out) {
   const int comps = CPLX ? 2 : 1;
-  const size_t row_g = (size_t)p.s * comps * sizeof(St);
-  if (p.variant == 1 || p.nmat != 0 || row_g % 16 != 0 || (uintptr_t)p.data % 16 != 0) return false;
-  const int G = p.nsc + p.nvec;
-  if (G < 1) return false;
+  int mmax = 1, na = 0;
+  for (int i = 0; i < n; ++i) {
+    const GatherParams& p = P[i];
+    const int G = p.nsc + p.nvec;
+    if (p.nmat != 0 || (uintptr_t)p.data % 16 != 0 || G < 1 || p.B < 1) return false;
+    mmax = std::max(mmax, std::min(std::max(1, 32 / G), p.B));
+    na = std::max(na, p.rot_mode == ROT_GAMMA ? p.nvec : 0);
+  }
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int na = p.rot_mode == ROT_GAMMA ? p.nvec : 0;
-  for (int warps : {kWarpGatherMaxWarps, kWarpGatherMaxWarps / 2}) {
-    int MBw = (32 + G - 1) / G;
-    if (MBw > p.B) MBw = p.B;
-    while (MBw > 1 && warp_layout<St, CPLX>(p.qmax, MBw, p.s, na, warps).total > (size_t)optin) --MBw;
-    const size_t smem = warp_layout<St, CPLX>(p.qmax, MBw, p.s, na, warps).total;
-    if (smem > (size_t)optin) continue;
-    cudaFuncSetAttribute(warp_gather_kernel<St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_gather_kernel<St, CPLX, Out>, warps * 32, smem);
-    if (per_sm < 1) continue;
-    GatherParams q = p;
-    q.MB = MBw;
-    long long grid = (long long)num_sms * per_sm;
-    if (grid > p.n) grid = p.n > 0 ? p.n : 1;
-    warp_gather_kernel<St, CPLX, Out><<<(unsigned)grid, warps * 32, smem, s>>>(q);
-    return true;
+  for (int pass = 0; pass < 2; ++pass) {
+    const size_t limit = pass == 0 ? std::min(budget, (size_t)optin) : (size_t)optin;
+    for (int warps : {kWarpGatherMaxWarps, kWarpGatherMaxWarps / 2}) {
+      for (int cap = mmax; cap >= 1; --cap) {
+        long long yb = 16;
+        for (int i = 0; i < n; ++i) {
+          const GatherParams& p = P[i];
+          const int G = p.nsc + p.nvec;
+          const int m = std::min(std::min(std::max(1, 32 / G), p.B), cap);
+          yb = std::max(yb, 8LL * m * ((((long long)p.s * comps * (long long)sizeof(St) + 15) & ~15LL) + 16));
+        }
+        const size_t smem = warp_layout(qmax, cap, na, yb, warps).total;
+        if (smem > limit) continue;
+        cudaFuncSetAttribute(warp_gather_kernel<St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_gather_kernel<St, CPLX, Out>, warps * 32, smem);
+        if (per_sm < 1) break;
+        gb->qmax = qmax;
+        gb->e_modes = cap;
+        gb->ph_atoms = na;
+        gb->ybuf = yb;
+        gb->warps = warps;
+        *smem_out = smem;
+        *per_sm_out = per_sm;
+        return true;
+      }
+    }
   }
   return false;
 }
 
+template <typename St, bool CPLX, typename Out>
+static bool launch_warp(const GatherParams& p, int num_sms, size_t budget, cudaStream_t s) {
+  if (p.variant == 1) return false;
+  GatherBatch gb{};
+  size_t smem = 0;
+  int per_sm = 0;
+  if (!warp_plan<St, CPLX, Out>(&p, 1, p.qmax, budget, &gb, &smem, &per_sm)) return false;
+  gb.groups = p.groups;
+  gb.n_groups = p.n_groups;
+  gb.counter = p.counter;
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > p.n) grid = p.n > 0 ? p.n : 1;
+  warp_gather_kernel<St, CPLX, Out><<<(unsigned)grid, gb.warps * 32, smem, s>>>(p, gb);
+  return true;
+}
+
 template <typename Acc, typename St, bool CPLX, typename Out>
-static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
+static void launch_t(const GatherParams& p, int num_sms, size_t budget, cudaStream_t s) {
   if (p.nvec == 0 && p.nmat == 0 && !p.phase_allowed) {
     if constexpr (std::is_same<Acc, float>::value && std::is_same<St, float>::value && !CPLX &&
                   std::is_same<Out, float>::value) {
@@ -1377,7 +1535,7 @@ static void launch_t(const GatherParams& p, int num_sms, cudaStream_t s) {
     return;
   }
   if constexpr (sizeof(Acc) == 4)
-    if (launch_warp<St, CPLX, Out>(p, num_sms, s)) return;
+    if (launch_warp<St, CPLX, Out>(p, num_sms, budget, s)) return;
   const size_t smem = layout_bytes<Acc, St, CPLX>(p, p.MB);
   static bool configured = false;
   if (!configured) {
@@ -1420,7 +1578,7 @@ __global__ void scan_apply_kernel(const int32_t* in, long long m, const int32_t*
                                   int32_t* out2);
 __global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cursor, int32_t* order);
 __global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
-                                   GroupDesc* groups, int32_t* n_groups);
+                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split);
 
 cudaError_t preload_grouping_kernels() {
   cudaFuncAttributes a;
@@ -1440,6 +1598,7 @@ cudaError_t preload_query_kernels() {
   cudaFuncAttributes a;
   if ((e = cudaFuncGetAttributes(&a, scalar_gather_vec_kernel<4>)) != cudaSuccess) return e;
   if ((e = cudaFuncGetAttributes(&a, scalar_gather_vec_kernel<2>)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, scalar_gather_batch_vec_kernel)) != cudaSuccess) return e;
   if ((e = preload_store<double, double>()) != cudaSuccess) return e;
   if ((e = preload_store<float, float>()) != cudaSuccess) return e;
   if ((e = preload_store<float, __nv_bfloat16>()) != cudaSuccess) return e;
@@ -1447,18 +1606,18 @@ cudaError_t preload_query_kernels() {
   return preload_locate_kernel();
 }
 
-int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms, size_t,
+int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms, size_t budget,
                   cudaStream_t s) {
   if (p.n <= 0) return 0;
   cudaMemsetAsync(p.counter, 0, sizeof(int32_t), s);
 #define BRX_DISPATCH(ACC, ST)                                                     \
   do {                                                                            \
     if (cplx) {                                                                   \
-      if (out_f32) launch_t<ACC, ST, true, float>(p, num_sms, s);                 \
-      else launch_t<ACC, ST, true, double>(p, num_sms, s);                        \
+      if (out_f32) launch_t<ACC, ST, true, float>(p, num_sms, budget, s);                 \
+      else launch_t<ACC, ST, true, double>(p, num_sms, budget, s);                        \
     } else {                                                                      \
-      if (out_f32) launch_t<ACC, ST, false, float>(p, num_sms, s);                \
-      else launch_t<ACC, ST, false, double>(p, num_sms, s);                       \
+      if (out_f32) launch_t<ACC, ST, false, float>(p, num_sms, budget, s);                \
+      else launch_t<ACC, ST, false, double>(p, num_sms, budget, s);                       \
     }                                                                             \
   } while (0)
   switch (store_kind) {
@@ -1503,6 +1662,21 @@ static int batch_ctas(size_t smem) {
   return per_sm;
 }
 
+bool gather_warp_plan(int store_kind, bool cplx, bool out_f32, const GatherParams* items, int n, int qmax,
+                      size_t budget, GatherBatch* gb, size_t* smem, int* ctas_per_sm) {
+  if (store_kind == ST_F64) return false;
+  bool r = false;
+  BRX_STORE_TYPES(store_kind, {
+    if constexpr (sizeof(Acc) == 4) {
+      if (cplx) r = out_f32 ? warp_plan<St, true, float>(items, n, qmax, budget, gb, smem, ctas_per_sm)
+                            : warp_plan<St, true, double>(items, n, qmax, budget, gb, smem, ctas_per_sm);
+      else r = out_f32 ? warp_plan<St, false, float>(items, n, qmax, budget, gb, smem, ctas_per_sm)
+                       : warp_plan<St, false, double>(items, n, qmax, budget, gb, smem, ctas_per_sm);
+    }
+  });
+  return r;
+}
+
 int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem) {
   int r = 0;
   BRX_STORE_TYPES(store_kind, {
@@ -1518,6 +1692,12 @@ int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem) {
 template <typename Acc, typename St, bool CPLX, typename Out>
 static void batch_launch_t(const GatherBatch& gb, int num_sms, size_t smem, int ctas, cudaStream_t s) {
   if (ctas < 1) ctas = 1;
+  if constexpr (sizeof(Acc) == 4) {
+    if (gb.warps > 0) {
+      warp_gather_kernel<St, CPLX, Out><<<(unsigned)(num_sms * ctas), gb.warps * 32, smem, s>>>(GatherParams{}, gb);
+      return;
+    }
+  }
   group_gather_batch_kernel<Acc, St, CPLX, Out><<<(unsigned)(num_sms * ctas), kGatherThreads, smem, s>>>(gb);
 }
 
@@ -1533,6 +1713,14 @@ void launch_gather_batch(const GatherBatch& gb, int store_kind, bool cplx, bool 
       else batch_launch_t<Acc, St, false, double>(gb, num_sms, smem, ctas_per_sm, s);
     }
   });
+}
+
+void launch_scalar_batch_vec(const GatherParams* items, const long long* qc_off, int n_items, long long total,
+                             int num_sms, cudaStream_t s) {
+  if (total <= 0) return;
+  long long blocks = (total + 255) / 256;
+  if (blocks > (long long)num_sms * 16) blocks = (long long)num_sms * 16;
+  scalar_gather_batch_vec_kernel<<<(unsigned)blocks, 256, 0, s>>>(items, qc_off, n_items, total);
 }
 
 void launch_scalar_batch(const GatherParams* items, const long long* qb_off, int n_items, long long total,
@@ -1643,19 +1831,34 @@ __global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cur
   }
 }
 
+// One work descriptor per qmax q of every key.  With split.item_class set,
+// keys of class-1 items take split.qmax q per descriptor and go to the
+// second list, written downwards from split.groups_end.
 __global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
-                                   GroupDesc* groups, int32_t* n_groups) {
+                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split) {
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n_keys; k += (long long)gridDim.x * blockDim.x) {
     const int c = counts[k];
     if (c <= 0) continue;
-    const int nd = (c + qmax - 1) / qmax;
-    int slot = atomicAdd(n_groups, nd);
+    bool second = false;
+    if (split.item_class) {
+      int lo = 0, hi = split.n_items - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(split.key_off + mid) <= k) lo = mid;
+        else hi = mid - 1;
+      }
+      second = __ldg(split.item_class + lo) == 1;
+    }
+    const int qm = second ? split.qmax : qmax;
+    const int nd = (c + qm - 1) / qm;
+    const int slot = atomicAdd(second ? split.n_groups : n_groups, nd);
     for (int d = 0; d < nd; ++d) {
       GroupDesc g;
       g.key = (int32_t)k;
-      g.start = offsets[k] + d * qmax;
-      g.count = min(qmax, c - d * qmax);
-      groups[slot + d] = g;
+      g.start = offsets[k] + d * qm;
+      g.count = min(qm, c - d * qm);
+      if (second) split.groups_end[-1 - (slot + d)] = g;
+      else groups[slot + d] = g;
     }
   }
 }
@@ -1667,7 +1870,7 @@ size_t group_scratch_ints(long long n_keys) {
 }
 
 int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax, int32_t* scratch, int32_t* order,
-                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s) {
+                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s, const GroupSplit& split) {
   if (n <= 0) return 0;
   const long long m = n_keys + 1;  // last bucket: failed q
   const long long nb = (m + kScanThreads * kScanPer - 1) / (kScanThreads * kScanPer);
@@ -1677,6 +1880,7 @@ int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax,
   int32_t* bsums = scratch + 3 * m;
   cudaMemsetAsync(counts, 0, sizeof(int32_t) * m, s);
   cudaMemsetAsync(n_groups, 0, sizeof(int32_t), s);
+  if (split.item_class) cudaMemsetAsync(split.n_groups, 0, sizeof(int32_t), s);
   long long blocks = (n + 255) / 256;
   if (blocks > 8192) blocks = 8192;
   key_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(key, n, counts);
@@ -1687,7 +1891,7 @@ int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax,
   long long kb = (n_keys + 255) / 256;
   if (kb > 8192) kb = 8192;
   if (kb < 1) kb = 1;
-  make_groups_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, offsets, n_keys, qmax, groups, n_groups);
+  make_groups_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, offsets, n_keys, qmax, groups, n_groups, split);
   return 7;
 }
 

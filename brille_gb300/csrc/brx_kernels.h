@@ -89,6 +89,21 @@ struct GatherBatch {
   int e_modes;
   int ph_atoms;
   long long ybuf;
+  int warps;  // 0: the classic CTA-synchronous kernel; else the warp-independent one with this many warps
+  int reverse;  // descriptor g at groups[-1 - g] (a list written downwards from its end)
+};
+
+// Second descriptor list of a batch's grouping: keys of class-1 items
+// (item_class[i] == 1; key_off ascending over the items) take qmax q per
+// descriptor and are written downwards from groups_end.  item_class null:
+// one list.
+struct GroupSplit {
+  const int32_t* key_off = nullptr;
+  const int32_t* item_class = nullptr;
+  int n_items = 0;
+  int qmax = 0;
+  GroupDesc* groups_end = nullptr;
+  int32_t* n_groups = nullptr;
 };
 
 size_t locate_smem_bytes(const DevGeom& g);
@@ -104,7 +119,7 @@ void launch_locate_batch(const DevGeom* geoms, const long long* q_off, const int
 // Counting sort of q by group key and the work descriptors of the groups.
 // Returns the number of kernel launches.
 int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax, int32_t* scratch, int32_t* order,
-                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s);
+                    GroupDesc* groups, int32_t* n_groups, cudaStream_t s, const GroupSplit& split = GroupSplit{});
 size_t group_scratch_ints(long long n_keys);
 
 // Gather + rotate for one interpolator.  Returns the number of launches.
@@ -119,11 +134,21 @@ void launch_gather_batch(const GatherBatch& gb, int store_kind, bool cplx, bool 
                          int ctas_per_sm, cudaStream_t s);
 void launch_scalar_batch(const GatherParams* items, const long long* qb_off, int n_items, long long total,
                          int store_kind, bool cplx, bool out_f32, int num_sms, cudaStream_t s);
+// FP32 scalar values with FP32 outputs and no permutation tables: one
+// thread per (q, 4 branches); qc_off[i] = Σ_{k<i} n_k·⌈B_k/4⌉.
+void launch_scalar_batch_vec(const GatherParams* items, const long long* qc_off, int n_items, long long total,
+                             int num_sms, cudaStream_t s);
 // shared memory of a batch launch from its largest item dimensions
 size_t gather_batch_smem(int store_kind, bool cplx, int qmax, int e_modes, int ph_atoms, long long ybuf);
 // staging elements of one block of MB modes of an item with s elements per mode
 long long gather_ybuf(int store_kind, bool cplx, int MB, int s);
 int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem);
+// The warp-independent FP32 gather for a batch (host copies of the items)
+// within a shared-memory budget per CTA: fills gb's layout and warps, the
+// launch's shared memory and CTAs per SM; false when an item does not fit
+// it (FP64 data, matrices, unaligned data).
+bool gather_warp_plan(int store_kind, bool cplx, bool out_f32, const GatherParams* items, int n, int qmax,
+                      size_t budget, GatherBatch* gb, size_t* smem, int* ctas_per_sm);
 
 // Load every query kernel of this library on the current device (module
 // loading is otherwise deferred to the first launch).

@@ -339,6 +339,12 @@ class _Grid:
         check(load().brx_tuning(h, v, 5), h)
         return tuple(int(x) for x in v)
 
+    def set_tuning(self, values):
+        """Apply a tuning() tuple (e.g. saved from an earlier tune())."""
+        v = (C.c_int32 * 5)(*(int(x) for x in values))
+        h = self._handle()
+        check(load().brx_set_tuning(h, v, 5), h)
+
     def launch_count(self):
         return int(load().brx_launch_count(self._handle()))
 

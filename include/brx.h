@@ -286,11 +286,17 @@ brx_status brx_set_residual_model(brx_handle* h, const brx_mlp_dims* d, const fl
  *                      message (prefixed "item i: "), its index in *failed
  *   brx_batch_tune     time launch-shape candidates on the current I/O with
  *                      CUDA events (locate block size, CTAs per SM, q per
- *                      tile; each gather's shared-memory budget) and keep
- *                      the fastest; drops a captured graph
+ *                      tile; each gather's kernel and shared-memory budget)
+ *                      and keep the fastest; drops a captured graph
  *   brx_batch_config   the chosen shapes: locate threads, locate CTAs per
  *                      SM, q per tile, values and vectors smem budget (KB),
- *                      values and vectors CTAs per SM, number of tiles */
+ *                      values and vectors CTAs per SM, number of tiles,
+ *                      values and vectors gather warps per CTA of the
+ *                      warp-independent FP32 gather (0: none), the least
+ *                      element groups per mode (scalars + vectors) an item
+ *                      needs to take that gather (-1: every item takes the
+ *                      CTA-synchronous one), q per work descriptor of the
+ *                      items below it (0: no such item) */
 typedef struct brx_batch brx_batch;
 brx_status brx_batch_create(brx_handle* const* handles, int32_t n, const int64_t* n_q, int32_t ir, uint32_t flags,
                             brx_batch** out);
@@ -302,6 +308,11 @@ brx_status brx_batch_launch(brx_batch* b, void* stream);
 brx_status brx_batch_sync(brx_batch* b, void* stream, int32_t* failed);
 brx_status brx_batch_tune(brx_batch* b, void* stream, int32_t reps);
 brx_status brx_batch_config(const brx_batch* b, int32_t* cfg, int32_t n);
+/* Set the shapes brx_batch_config reports (n ≥ 5: entries 0-4; entries 5-9
+ * are derived and ignored; 10 and 11, when given, set the item split
+ * between the two gathers and the small items' q per descriptor) and
+ * re-plan; drops a captured graph. */
+brx_status brx_batch_set_config(brx_batch* b, const int32_t* cfg, int32_t n);
 int64_t brx_batch_launch_count(const brx_batch* b);
 const char* brx_batch_last_error(const brx_batch* b);
 
@@ -338,6 +349,9 @@ brx_status brx_stage_times(const brx_handle* h, double* ms, int32_t n, int64_t* 
 brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out, uint32_t flags,
                     void* stream, int32_t reps);
 brx_status brx_tuning(const brx_handle* h, int32_t* out, int32_t n);
+/* Apply tuning values in brx_tuning's order (n ≥ 5), e.g. saved from an
+ * earlier brx_tune; BRX_ERR_INVALID_ARGUMENT when one is out of range. */
+brx_status brx_set_tuning(brx_handle* h, const int32_t* values, int32_t n);
 
 int32_t brx_abi_version(void);
 

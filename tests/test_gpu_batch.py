@@ -83,17 +83,29 @@ def test_batch_matches_single_queries(storage, out_f32):
     grids = _grids(storage)
     Qs = _Q(1)
     bq = BatchQuery(grids, COUNTS, out_f32=out_f32)
+    # FP32 data: the warp-independent gather takes every item (rows of 6 to
+    # 26 atoms, aligned to 16 bytes or not); FP64: the classic gather
+    assert (bq.config()["vectors_gather_warps"] > 0) == (storage == "f32")
     vals, vecs = bq.query([torch.from_numpy(q).cuda() for q in Qs])
     _check(grids, Qs, vals, vecs, out_f32)
 
 
-def test_values_only_batch_uses_scalar_gather():
-    grids = _grids("f64", values_only=True)
+@pytest.mark.parametrize("storage,out_f32", [("f64", False), ("f32", True)])
+def test_values_only_batch_uses_scalar_gather(storage, out_f32):
+    """Scalar-only grids need no grouping; FP32 data with FP32 outputs take
+    the kernel that reads 4 branches per thread (B = 6, 9, 48, 63, 78, 24:
+    float4 rows and element-wise rows)."""
+    grids = _grids(storage, values_only=True)
     Qs = _Q(2)
-    bq = BatchQuery(grids, COUNTS)
+    bq = BatchQuery(grids, COUNTS, out_f32=out_f32)
     vals, vecs = bq.query([torch.from_numpy(q).cuda() for q in Qs])
     assert all(v is None for v in vecs)
-    _check(grids, Qs, vals, vecs, False)
+    _check(grids, Qs, vals, vecs, out_f32)
+    if out_f32:
+        # same operation order as the single queries' scalar gather
+        for i, (g, Q) in enumerate(zip(grids, Qs)):
+            if len(Q):
+                assert np.array_equal(vals[i].cpu().numpy(), g.ir_interpolate_at(Q, out_f32=True)[0]), i
 
 
 def test_graph_replay_on_new_inputs_and_tuning():
@@ -115,12 +127,34 @@ def test_graph_replay_on_new_inputs_and_tuning():
     _check(grids, [q.cpu().numpy() for q in Q2], vals, vecs, True)
     cfg = bq.tune(s.cuda_stream, reps=1)
     assert cfg["locate_threads"] in (64, 128, 256) and cfg["tiles"] > 0
-    assert cfg["vectors_ctas_per_sm"] >= 1
+    assert cfg["vectors_ctas_per_sm"] >= 1 and cfg["vectors_gather_warps"] in (0, 4, 8)
     for v in vals:
         v.zero_()
     bq.run(s.cuda_stream)
     bq.sync(s.cuda_stream)
     _check(grids, [q.cpu().numpy() for q in Q2], vals, vecs, True)
+
+
+@pytest.mark.parametrize("min_groups,small_q", [(-1, 0), (0, 0), (8, 128), (64, 32)])
+def test_item_split_between_gathers(min_groups, small_q):
+    """Every split of the items between the warp-independent gather and the
+    CTA-synchronous one (with its own q per descriptor, a second descriptor
+    list) answers as the single queries do."""
+    grids = _grids("f32")
+    Qs = _Q(6)
+    bq = BatchQuery(grids, COUNTS, out_f32=True)
+    cfg = bq.config()
+    cfg["warp_min_groups"] = min_groups
+    cfg["small_q_per_group"] = small_q
+    got = bq.set_config(cfg)
+    assert got["warp_min_groups"] == min_groups
+    if min_groups > 8:
+        assert got["small_q_per_group"] == small_q and got["vectors_gather_warps"] == 0
+    vals, vecs = bq.outputs()
+    bq.set_io([torch.from_numpy(q).cuda() for q in Qs], vals, vecs)
+    bq.run()
+    bq.sync()
+    _check(grids, Qs, vals, vecs, True)
 
 
 def test_failure_names_the_item():
