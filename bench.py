@@ -45,6 +45,14 @@ WORKLOADS = {
 }
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch (ncu,
+# one pass, --clock-control none), keyed by (workload, stage)
+PROFILED_TRAFFIC = {
+    ("hex16", "gather_vectors"): dict(bytes=32_745_354_496 + 185_691_531_520,
+                                      source="ncu, one full-size warp_gather_kernel launch"),
+}
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -566,6 +574,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-tune", action="store_true", help="keep the default gather shared-memory budgets")
+    ap.add_argument("--tuning", default=None,
+                    help="apply gather tuning values (5 integers, as config.tuning lists them) instead of tuning")
     ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned", "batch"],
                     help="precision: FP32 and BF16 storage against the FP64 path; learned: the learned residual "
                          "on coarse trellises against the plain fine trellis")
@@ -633,7 +643,10 @@ def main():
         grid.query_into(Qs[i % nbuf], n, vals, vecs, out_f32=out_f32, async_=True, stream=sp)
 
     tuned = None
-    if not args.no_tune:
+    if args.tuning:
+        grid.set_tuning([int(x) for x in args.tuning.split(",")])
+        tuned = grid.tuning()
+    elif not args.no_tune:
         t = time.time()
         tuned = grid.tune(Qs[0], out_f32=out_f32, reps=2, stream=sp, values_out=vals, vectors_out=vecs)
         log(f"[setup] gather budgets (KB, values/vectors) {tuned} in {time.time() - t:.1f}s")
@@ -674,9 +687,16 @@ def main():
     achieved = per_q_bytes * stage_q / (stage_ms[dom] / 1e3) / 1e9 if stage_ms[dom] > 0 else 0.0
     peaks = measured_peaks()
     peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
+    # DRAM bytes (read + write) of one launch of the dominant kernel on this
+    # workload, from an ncu capture of the full-size launch
+    prof = PROFILED_TRAFFIC.get((args.workload, stage_names[dom])) if n == WORKLOADS[args.workload][3] else None
+    traffic = None
+    if prof:
+        traffic = dict(bytes_per_launch=prof["bytes"], algorithmic_bytes_per_launch=per_q_bytes * n,
+                       ratio=round(prof["bytes"] / (per_q_bytes * n), 3), source=prof["source"])
     roofline = dict(bound="hbm", kernel=stage_names[dom], achieved=round(achieved, 1), peak=peak,
                     peak_source="measured" if peaks else "fallback", unit="GB/s",
-                    frac=round(achieved / peak, 4), traffic=None,
+                    frac=round(achieved / peak, 4), traffic=traffic,
                     algorithmic_bytes_per_q=per_q_bytes,
                     q_per_group=round(stage_q / max(stage_groups, 1), 2),
                     stage_ms_per_step={k: round(v / args.steps, 3) for k, v in zip(stage_names, stage_ms)})
@@ -689,10 +709,15 @@ def main():
         Qh.copy_(Qs[0][:ne].cpu())
         vh = torch.empty((ne, B), dtype=fdt, pin_memory=True)
         ch = torch.empty((ne, B, na, 3), dtype=cdt, pin_memory=True)
-        grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
-        t0 = time.perf_counter()
-        for _ in range(args.e2e_steps):
+        # freshly pinned pages reach full link speed only after a few passes
+        for _ in range(max(3, args.warmup)):
             grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
+        t0 = time.perf_counter()
+        step_s = []
+        for _ in range(args.e2e_steps):
+            ts = time.perf_counter()
+            grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
+            step_s.append(time.perf_counter() - ts)
         te = time.perf_counter() - t0
         if dist:
             t = torch.tensor([te], device=dev)
@@ -700,8 +725,17 @@ def main():
             te = float(t.item())
         h2d = ne * 24
         d2h = ne * (bq_vals + bq_vecs)
+        # the host link alone: the same output bytes copied device -> pinned host
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        with torch.cuda.stream(stream):
+            ch.copy_(vecs[:ne], non_blocking=True)
+            vh.copy_(vals[:ne], non_blocking=True)
+        stream.synchronize()
+        tl = time.perf_counter() - tl
         e2e = dict(value=world * ne * args.e2e_steps / te, unit="q-points/s", h2d_bytes_per_step=h2d,
-                   d2h_bytes_per_step=d2h)
+                   d2h_bytes_per_step=d2h, step_ms=[round(x * 1e3, 1) for x in step_s],
+                   d2h_copy_gbs=round(d2h / tl / 1e9, 1), d2h_copy_bound=round(world * ne / tl, 1))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -720,7 +754,9 @@ def main():
                         q_per_step=n, q_range=qr, storage=args.storage,
                         outputs="f32/c64" if out_f32 else "f64/c128",
                         l2="outputs of %.1f GB per step exceed the 129 MB L2" % (n * (bq_vals + bq_vecs) / 1e9),
-                        gather_smem_kb=tuned,
+                        tuning=None if tuned is None else dict(
+                            zip(("values_smem_kb", "vectors_smem_kb", "q_per_group", "units_per_thread",
+                                 "gather_kernel"), tuned)),
                         parallelism=f"replicas x{world}, q sharded, no collective on the data path"),
             roofline=roofline, e2e=e2e, cpu_baseline=cpu, gpu_launches=int(launches),
             clocks=clk.summary())

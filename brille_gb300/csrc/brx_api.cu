@@ -76,6 +76,16 @@ bool host_ptr(const void* p) {
   return a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged;
 }
 
+// Device address of page-locked host memory, else null.
+void* mapped_ptr(void* p) {
+  cudaPointerAttributes a{};
+  if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int span(const Interp& d) { return d.el[0] + d.el[1] + d.el[2]; }
 
 // whether the gather of d takes the group-ordered kernel (launch_t in
@@ -316,7 +326,21 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   if (n == 0) return BRX_OK;
 
   const bool q_host = host_ptr(Q);
-  const bool o_host = locate_only ? host_ptr(lout->status) : host_ptr(vals_out);
+  bool o_host = locate_only ? host_ptr(lout->status) : host_ptr(vals_out);
+  // page-locked host outputs: the kernels may write them directly over the
+  // host link (BRX_ZERO_COPY=1) instead of through staged chunks and copies
+  if (o_host && !locate_only) {
+    const char* zc_env = std::getenv("BRX_ZERO_COPY");
+    if (zc_env && zc_env[0] == '1') {
+      void* vz = mapped_ptr(vals_out);
+      void* cz = h->vecs.present ? mapped_ptr(vecs_out) : nullptr;
+      if (vz && (cz || !h->vecs.present)) {
+        vals_out = vz;
+        vecs_out = cz;
+        o_host = false;
+      }
+    }
+  }
   const bool any_host = q_host || o_host;
   const bool async = (flags & BRX_FLAG_ASYNC) && !any_host;
 
@@ -959,44 +983,62 @@ brx_status brx_tune(brx_handle* h, const double* Q, int64_t n, void* values_out,
   for (int which = 0; which < 2 && !st; ++which) {
     const Interp& d = which ? h->vecs : h->vals;
     if (!d.present || !uses_groups(d, which ? d.cplx : false)) continue;
-    // budgets per kernel: the warp-independent gather (FP32 data) and the
-    // CTA-synchronous one; the kernel choice is shared by both gathers and
-    // made on the heavier one
     size_t best_b = h->gather_budget[which];
-    int best_v = h->gather_variant;
     double best = 1e300;
-    const bool fp32 = d.store != ST_F64;
-    for (int v : {0, 1}) {
-      if ((!fp32 || which != lead) && v != h->gather_variant) continue;
+    if (which != lead) {
       for (size_t c : cands) {
         if (c > h->smem_optin || st) continue;
-        h->gather_variant = v;
         h->gather_budget[which] = c;
         const double t = timed(2 + which);
         if (st) break;
-        if (t < best) { best = t; best_b = c; best_v = v; }
+        if (t < best) { best = t; best_b = c; }
+      }
+      h->gather_budget[which] = best_b;
+      continue;
+    }
+    // the heavier gather: kernel (FP32 data: warp-independent or
+    // CTA-synchronous) × q per descriptor × shared-memory budget, timing
+    // each distinct launch shape once
+    int rot = ROT_NONE;
+    {
+      std::string msg;
+      if (rotation_mode(d, &rot, &msg)) rot = ROT_NONE;
+    }
+    const bool fp32 = d.store != ST_F64;
+    int best_v = h->gather_variant, best_g = h->group_q;
+    std::vector<long long> seen;
+    for (int v : {0, 1}) {
+      if (!fp32 && v == 0) continue;
+      for (int gq : {16, 32, 64, 128}) {
+        for (size_t c : cands) {
+          if (c > h->smem_optin || st) continue;
+          h->gather_variant = v;
+          h->group_q = gq;
+          h->gather_budget[which] = c;
+          GatherParams p = gather_params(h, d, h->sc[0], n, rot, which ? d.cplx : false, which);
+          const long long key = gather_shape_key(p, d.store, d.cplx, f32, c);
+          if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+          seen.push_back(key);
+          const double t = timed(2 + which);
+          if (st) break;
+          if (t < best) { best = t; best_b = c; best_v = v; best_g = gq; }
+        }
       }
     }
     h->gather_budget[which] = best_b;
     h->gather_variant = best_v;
-    if (which != lead || st) continue;
-    // coordinate descent over q per work descriptor, then units per thread
-    int best_g = h->group_q;
-    for (int gq : {16, 32, 64, 128}) {
-      h->group_q = gq;
-      const double t = timed(2 + which);
-      if (st) break;
-      if (t < best) { best = t; best_g = gq; }
-    }
     h->group_q = best_g;
-    int best_s = h->qsplit;
-    for (int qs : {1, 2, 4}) {
-      h->qsplit = qs;
-      const double t = timed(2 + which);
-      if (st) break;
-      if (t < best) { best = t; best_s = qs; }
+    // work units per thread: the CTA-synchronous kernel only
+    if (best_v == 1 && !st) {
+      int best_s = h->qsplit;
+      for (int qs : {1, 2, 4}) {
+        h->qsplit = qs;
+        const double t = timed(2 + which);
+        if (st) break;
+        if (t < best) { best = t; best_s = qs; }
+      }
+      h->qsplit = best_s;
     }
-    h->qsplit = best_s;
   }
   brx_profile(h, 0);
   h->profile = false;

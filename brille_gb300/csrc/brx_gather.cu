@@ -889,8 +889,8 @@ __host__ __device__ inline WarpLayout warp_layout(int QM, int e_modes, int na, l
   const int nan = na > 0 ? na : 1;
   L.q = take(8 * (size_t)QM);
   L.oq = take(8 * (size_t)QM);
-  L.w = take(4 * 8 * (size_t)QM);
-  L.M = take(4 * 12 * (size_t)QM);
+  L.w = take(8 * 8 * (size_t)QM);    // 8 weights per q, each as a (w, w) pair
+  L.M = take(8 * 10 * (size_t)QM);   // 3×3 per q as (m, m) pairs, padded to 10
   L.rotf = take(4 * (size_t)QM);
   L.ph = take(4 * 2 * (size_t)nan * QM);
   L.de = take(4 * (size_t)nan * QM);
@@ -961,6 +961,108 @@ __device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase) {
   }
 }
 
+// One lane's (mode, element group) unit of the warp gather over its q.
+// Values travel as (re, im) pairs on the packed FP32 pipe: the NS corner
+// rows with their antiphase once, then per q the weighted corner sum
+// (one __ffma2_rn per corner and element), the 3×3 rotation on pairs, the
+// Γ phase, and the store.  Weights and matrix entries sit in shared memory
+// as (w, w) pairs.  ne: 1 for a scalar element, 3 for a vector.
+template <int NS, typename St, bool CPLX, typename Out>
+__device__ __forceinline__ void warp_unit(const unsigned char* Yb, const unsigned char* so, int row_bytes, int MBw,
+                                          int mm, const float* s_e, int pivot, int e0, int ne, const float2* s_w2,
+                                          const float2* s_M2, const int* s_rotf, const float* s_ph, const int* s_de,
+                                          const long long* s_oq, int j0, int count, int jstep, bool gamma, int na,
+                                          int k_atom, long long row_off, Out* out) {
+  constexpr int comps = CPLX ? 2 : 1;
+  float2 y[NS][3];
+#pragma unroll
+  for (int x = 0; x < NS; ++x) {
+    const bool usex = x >= pivot;
+    const float er = usex ? s_e[2 * (x * MBw + mm)] : 0.f, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : 0.f;
+    const St* yp = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float dr = 0.f, di = 0.f;
+      if (usex && k < ne) ldY<float, St, CPLX>(yp + (e0 + k) * comps, dr, di);
+      y[x][k] = make_float2(er * dr - ei * di, er * di + ei * dr);
+    }
+  }
+  const float2 zero = make_float2(0.f, 0.f);
+  for (int j = j0; j < count; j += jstep) {
+    float2 wp[NS];
+#pragma unroll
+    for (int h = 0; h < NS / 2; ++h) {
+      const float4 t = reinterpret_cast<const float4*>(s_w2 + 8 * j)[h];
+      wp[2 * h] = make_float2(t.x, t.y);
+      wp[2 * h + 1] = make_float2(t.z, t.w);
+    }
+    Out* dst = out + s_oq[j] + row_off;
+    if (ne == 1) {
+      float2 v = zero;
+#pragma unroll
+      for (int x = 0; x < NS; ++x) v = __ffma2_rn(wp[x], y[x][0], v);
+      dst += (long long)e0 * comps;
+      if (CPLX) {
+        dst[0] = (Out)v.x;
+        dst[1] = (Out)v.y;
+      } else {
+        dst[0] = (Out)v.x;
+      }
+      continue;
+    }
+    float2 v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      v[k] = zero;
+#pragma unroll
+      for (int x = 0; x < NS; ++x) v[k] = __ffma2_rn(wp[x], y[x][k], v[k]);
+    }
+    int de = e0;
+    if (s_rotf[j]) {
+      float2 M[9];
+      const float4* m4 = reinterpret_cast<const float4*>(s_M2 + 10 * j);
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float4 t = m4[h];
+        M[2 * h] = make_float2(t.x, t.y);
+        M[2 * h + 1] = make_float2(t.z, t.w);
+      }
+      M[8] = s_M2[10 * j + 8];
+      float2 t[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        t[a] = __fmul2_rn(M[3 * a], v[0]);
+        t[a] = __ffma2_rn(M[3 * a + 1], v[1], t[a]);
+        t[a] = __ffma2_rn(M[3 * a + 2], v[2], t[a]);
+      }
+      if (gamma) {
+        de = s_de[j * na + k_atom];
+        const float2 ph = *reinterpret_cast<const float2*>(s_ph + 2 * (j * na + k_atom));
+#pragma unroll
+        for (int a = 0; a < 3; ++a) v[a] = make_float2(ph.x * t[a].x - ph.y * t[a].y, ph.x * t[a].y + ph.y * t[a].x);
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) v[a] = t[a];
+      }
+    }
+    dst += (long long)de * comps;
+    if (CPLX) {
+      using V2 = typename std::conditional<std::is_same<Out, float>::value, float2, double2>::type;
+      V2* d2 = reinterpret_cast<V2*>(dst);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        V2 o;
+        o.x = (Out)v[k].x;
+        o.y = (Out)v[k].y;
+        d2[k] = o;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dst[k] = (Out)v[k].x;
+    }
+  }
+}
+
 // single: the one interpolator's parameters (gb.items null); otherwise a
 // batch whose groups carry their item's parameters.  gb.qmax, e_modes,
 // ph_atoms and ybuf give the shared-memory layout in either case.
@@ -983,8 +1085,8 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
   const WarpLayout L = warp_layout(QM, gb.e_modes, gb.ph_atoms, gb.ybuf, nwarps);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
   long long* s_oq = reinterpret_cast<long long*>(sm + L.oq);
-  Acc* s_w = reinterpret_cast<Acc*>(sm + L.w);
-  Acc* s_M = reinterpret_cast<Acc*>(sm + L.M);
+  float2* s_w2 = reinterpret_cast<float2*>(sm + L.w);
+  float2* s_M2 = reinterpret_cast<float2*>(sm + L.M);
   int* s_rotf = reinterpret_cast<int*>(sm + L.rotf);
   Acc* s_ph = reinterpret_cast<Acc*>(sm + L.ph);
   int* s_de = reinterpret_cast<int*>(sm + L.de);
@@ -1067,7 +1169,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
         for (int x = 0; x < nslot; ++x)
           if (gc.vid[x] == v) wsl[x] = wk;
       }
-      for (int x = 0; x < 8; ++x) s_w[8 * j + x] = wsl[x];
+      for (int x = 0; x < 8; ++x) s_w2[8 * j + x] = make_float2(wsl[x], wsl[x]);
       int rotf = 0;
       if (p.rot_mode != ROT_NONE) {
         const int r0 = p.rot[2 * qi], r1 = p.rot[2 * qi + 1];
@@ -1094,7 +1196,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
             if (p.rot_mode == ROT_RECIP) mv = R[3 * c + a];
             else if (gamma || p.rot_mode == ROT_AXIAL) mv = scale * Ri[3 * a + c];
             else mv = R[3 * a + c];
-            s_M[12 * j + 3 * a + c] = mv;
+            s_M2[10 * j + 3 * a + c] = make_float2(mv, mv);
           }
         rotf = (gamma || !ident) ? 1 : 0;
       }
@@ -1189,65 +1291,12 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
         const int e0 = gi < p.nsc ? gi : p.nsc + 3 * (gi - p.nsc);
         const int ne = gi < p.nsc ? 1 : 3;
         const long long row_off = (long long)bb * s * comps;
-        if (nslot == 8) {
-          Acc yr[8][3], yi[8][3];
-#pragma unroll
-          for (int x = 0; x < 8; ++x) {
-            const bool usex = x >= pivot;
-            const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
-            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              Acc dr = 0, di = 0;
-              if (usex && k < ne) ldY<Acc, St, CPLX>(y + (e0 + k) * comps, dr, di);
-              yr[x][k] = er * dr - ei * di;
-              yi[x][k] = er * di + ei * dr;
-            }
-          }
-          if (ne == 3) {
-            vector_unit<8, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, j0, count, jstep, gamma, na,
-                                           gi - p.nsc, e0, row_off, out);
-          } else {
-            for (int j = j0; j < count; j += jstep) {
-              Acc vr = 0, vi = 0;
-#pragma unroll
-              for (int x = 0; x < 8; ++x) {
-                vr += s_w[8 * j + x] * yr[x][0];
-                vi += s_w[8 * j + x] * yi[x][0];
-              }
-              store_group<Out, CPLX>(out + s_oq[j] + row_off + (long long)e0 * comps, &vr, &vi, 1);
-            }
-          }
-        } else {
-          Acc yr[4][3], yi[4][3];
-#pragma unroll
-          for (int x = 0; x < 4; ++x) {
-            const bool usex = x >= pivot;
-            const Acc er = usex ? s_e[2 * (x * MBw + mm)] : (Acc)0, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : (Acc)0;
-            const St* y = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              Acc dr = 0, di = 0;
-              if (usex && k < ne) ldY<Acc, St, CPLX>(y + (e0 + k) * comps, dr, di);
-              yr[x][k] = er * dr - ei * di;
-              yi[x][k] = er * di + ei * dr;
-            }
-          }
-          if (ne == 3) {
-            vector_unit<4, Acc, CPLX, Out>(yr, yi, s_w, s_M, s_rotf, s_ph, s_de, s_oq, j0, count, jstep, gamma, na,
-                                           gi - p.nsc, e0, row_off, out);
-          } else {
-            for (int j = j0; j < count; j += jstep) {
-              Acc vr = 0, vi = 0;
-#pragma unroll
-              for (int x = 0; x < 4; ++x) {
-                vr += s_w[8 * j + x] * yr[x][0];
-                vi += s_w[8 * j + x] * yi[x][0];
-              }
-              store_group<Out, CPLX>(out + s_oq[j] + row_off + (long long)e0 * comps, &vr, &vi, 1);
-            }
-          }
-        }
+        if (nslot == 8)
+          warp_unit<8, St, CPLX, Out>(Yb, so, row_bytes, MBw, mm, s_e, pivot, e0, ne, s_w2, s_M2, s_rotf, s_ph, s_de,
+                                      s_oq, j0, count, jstep, gamma, na, gi - p.nsc, row_off, out);
+        else
+          warp_unit<4, St, CPLX, Out>(Yb, so, row_bytes, MBw, mm, s_e, pivot, e0, ne, s_w2, s_M2, s_rotf, s_ph, s_de,
+                                      s_oq, j0, count, jstep, gamma, na, gi - p.nsc, row_off, out);
       }
       __syncwarp();  // the buffer may be refilled
       buf ^= 1;
@@ -1675,6 +1724,18 @@ bool gather_warp_plan(int store_kind, bool cplx, bool out_f32, const GatherParam
     }
   });
   return r;
+}
+
+long long gather_shape_key(const GatherParams& p, int store_kind, bool cplx, bool out_f32, size_t budget) {
+  if (p.variant != 1) {
+    GatherBatch gb{};
+    size_t smem = 0;
+    int ctas = 0;
+    if (gather_warp_plan(store_kind, cplx, out_f32, &p, 1, p.qmax, budget, &gb, &smem, &ctas))
+      return (1LL << 48) | ((long long)p.qmax << 32) | ((long long)gb.warps << 24) | ((long long)gb.e_modes << 12) |
+             (long long)ctas;
+  }
+  return (2LL << 48) | ((long long)p.qmax << 32) | (long long)gather_pick_modes(p, store_kind, cplx, budget);
 }
 
 int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem) {

@@ -154,5 +154,9 @@ bool gather_warp_plan(int store_kind, bool cplx, bool out_f32, const GatherParam
 // loading is otherwise deferred to the first launch).
 cudaError_t preload_query_kernels();
 int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t smem_budget);
+// Launch shape launch_gather takes for p under a budget (kernel, q per
+// descriptor, warps and modes per block or modes per block, CTAs per SM)
+// as one key: equal keys run alike.
+long long gather_shape_key(const GatherParams& p, int store_kind, bool cplx, bool out_f32, size_t budget);
 
 }  // namespace brx

@@ -251,3 +251,19 @@ def test_tune_keeps_results():
         assert np.array_equal(c0, c1)
     else:
         assert np.allclose(c0, c1, rtol=0, atol=1e-5)
+
+
+def test_warp_gather_shape_independent():
+    """The FP32 warp-independent gather's outputs do not depend on its launch
+    shape (shared-memory budget, hence warps and modes per block; q per
+    descriptor) nor on host-staged chunking: bit-identical."""
+    c = crystal_case("hex16")
+    g = _grid(c)
+    g.fill(c["w"], [1, 0, 0, 0, 3], c["v"], [0, 3 * c["model"].n_atoms, 0, 2, 1], storage="f32")
+    Q = _queries(c, 6000, seed=13)
+    g.set_tuning((56, 56, 32, 2, 0))
+    v0, c0 = g.ir_interpolate_at(Q, out_f32=True)
+    for kb, gq in ((24, 16), (96, 128), (160, 16), (40, 64)):
+        g.set_tuning((56, kb, gq, 2, 0))
+        v1, c1 = g.ir_interpolate_at(Q, out_f32=True)
+        assert np.array_equal(v0, v1) and np.array_equal(c0, c1), (kb, gq)
