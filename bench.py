@@ -48,7 +48,7 @@ WORKLOADS = {
 # dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch (ncu,
 # one pass, --clock-control none), keyed by (workload, stage)
 PROFILED_TRAFFIC = {
-    ("hex16", "gather_vectors"): dict(bytes=32_745_354_496 + 185_691_531_520,
+    ("hex16", "gather_vectors"): dict(bytes=12_696_951_552 + 184_570_256_896,
                                       source="ncu, one full-size warp_gather_kernel launch"),
 }
 

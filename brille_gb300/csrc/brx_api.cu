@@ -184,6 +184,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.n = n;
   p.n_cube = h->g.n_cube;
   p.cube_vertices = h->g.cube_vertices;
+  p.rank_cube = h->rank_cube;
   p.tet_vertices = h->g.tet_vertices;
   p.data = d.data.p;
   p.B = d.B;
@@ -569,6 +570,32 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
   UP(G.node_type, G.n_nodes, g.node_type);
   UP(G.node_index, G.n_nodes, g.node_index);
   UP(G.cube_vertices, 8LL * G.n_cube, g.cube_vertices);
+  // Morton order of the cube nodes' (i, j, k) for the group keys
+  {
+    const long long nx = G.n_knots[0] - 1, ny = G.n_knots[1] - 1;
+    std::vector<std::pair<unsigned long long, int32_t>> code;
+    code.reserve((size_t)G.n_cube);
+    for (long long node = 0; node < G.n_nodes; ++node) {
+      if (G.node_type[node] != BRX_NODE_CUBE) continue;
+      const unsigned long long c[3] = {(unsigned long long)(node % nx), (unsigned long long)((node / nx) % ny),
+                                       (unsigned long long)(node / (nx * ny))};
+      unsigned long long m = 0;
+      for (int bit = 0; bit < 21; ++bit)
+        for (int d = 0; d < 3; ++d) m |= ((c[d] >> bit) & 1ULL) << (3 * bit + d);
+      code.emplace_back(m, G.node_index[node]);
+    }
+    if ((long long)code.size() != G.n_cube) return bail(BRX_ERR_INVALID_ARGUMENT);
+    std::sort(code.begin(), code.end());
+    std::vector<int32_t> rank((size_t)G.n_cube), inv((size_t)G.n_cube);
+    for (size_t r = 0; r < code.size(); ++r) {
+      const int32_t ni = code[r].second;
+      if (ni < 0 || ni >= G.n_cube) return bail(BRX_ERR_INVALID_ARGUMENT);
+      rank[(size_t)ni] = (int32_t)r;
+      inv[r] = ni;
+    }
+    UP(rank.data(), rank.size(), g.cube_rank);
+    UP(inv.data(), inv.size(), h->rank_cube);
+  }
   UP(G.poly_tet_offset, G.n_poly + 1, g.poly_tet_offset);
   UP(G.tet_vertices, 4LL * G.n_tets, g.tet_vertices);
   UP(G.tet_sphere, 4LL * G.n_tets, g.tet_sphere);

@@ -141,6 +141,7 @@ brx::GatherParams item_params(brx_batch* b, int i, const Interp& d, int rot_mode
   p.n = b->nq[i];
   p.n_cube = h->g.n_cube;
   p.cube_vertices = h->g.cube_vertices;
+  p.rank_cube = h->rank_cube;
   p.tet_vertices = h->g.tet_vertices;
   p.data = d.data.p;
   p.B = d.B;

@@ -108,6 +108,9 @@ struct DevGeom {
   int32_t n_cube;
   long long n_tets;
   const int32_t* cube_vertices;
+  // cube nodes in Morton order of their (i, j, k): group keys follow it, so
+  // the gathers visit nodes that share vertices close together in time
+  const int32_t* cube_rank;   // cube index → rank
   const int32_t* poly_tet_offset;
   const int32_t* tet_vertices;
   const double* tet_sphere;

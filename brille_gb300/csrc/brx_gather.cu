@@ -380,7 +380,7 @@ __device__ __forceinline__ void fetch_group(const GatherBatch& gb, int n_groups,
   if (key < 8 * p.n_cube) {
     pivot = key & 7;
     nslot = 8;
-    if (lane < 8) vid = __ldg(p.cube_vertices + 8 * (long long)(key >> 3) + 7 - lane);
+    if (lane < 8) vid = __ldg(p.cube_vertices + 8 * (long long)__ldg(p.rank_cube + (key >> 3)) + 7 - lane);
   } else {
     const long long t = (key - 8LL * p.n_cube) >> 2;
     pivot = (int)((key - 8LL * p.n_cube) & 3);
@@ -1045,6 +1045,8 @@ __device__ __forceinline__ void warp_unit(const unsigned char* Yb, const unsigne
         for (int a = 0; a < 3; ++a) v[a] = t[a];
       }
     }
+    // outputs are written once: streaming stores (evict first) keep the
+    // vertex rows, which neighbouring groups read again, in L2
     dst += (long long)de * comps;
     if (CPLX) {
       using V2 = typename std::conditional<std::is_same<Out, float>::value, float2, double2>::type;
@@ -1054,11 +1056,11 @@ __device__ __forceinline__ void warp_unit(const unsigned char* Yb, const unsigne
         V2 o;
         o.x = (Out)v[k].x;
         o.y = (Out)v[k].y;
-        d2[k] = o;
+        __stcs(d2 + k, o);
       }
     } else {
 #pragma unroll
-      for (int k = 0; k < 3; ++k) dst[k] = (Out)v[k].x;
+      for (int k = 0; k < 3; ++k) __stcs(dst + k, (Out)v[k].x);
     }
   }
 }
@@ -1627,7 +1629,10 @@ __global__ void scan_apply_kernel(const int32_t* in, long long m, const int32_t*
                                   int32_t* out2);
 __global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cursor, int32_t* order);
 __global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
-                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split);
+                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split, const int32_t* dpos0,
+                                   const int32_t* dpos1);
+__global__ void group_count_kernel(const int32_t* counts, long long n_keys, int qmax, GroupSplit split, int cls,
+                                   int32_t* nd);
 
 cudaError_t preload_grouping_kernels() {
   cudaFuncAttributes a;
@@ -1637,6 +1642,7 @@ cudaError_t preload_grouping_kernels() {
   if ((e = cudaFuncGetAttributes(&a, scan_blocks_kernel)) != cudaSuccess) return e;
   if ((e = cudaFuncGetAttributes(&a, scan_apply_kernel)) != cudaSuccess) return e;
   if ((e = cudaFuncGetAttributes(&a, key_scatter_kernel)) != cudaSuccess) return e;
+  if ((e = cudaFuncGetAttributes(&a, group_count_kernel)) != cudaSuccess) return e;
   return cudaFuncGetAttributes(&a, make_groups_kernel);
 }
 
@@ -1892,27 +1898,54 @@ __global__ void key_scatter_kernel(const int32_t* key, long long n, int32_t* cur
   }
 }
 
-// One work descriptor per qmax q of every key.  With split.item_class set,
-// keys of class-1 items take split.qmax q per descriptor and go to the
+// Class of key k: 1 for keys of a class-1 item of the split, else 0.
+__device__ __forceinline__ int key_class(const GroupSplit& split, long long k) {
+  if (!split.item_class) return 0;
+  int lo = 0, hi = split.n_items - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(split.key_off + mid) <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  return __ldg(split.item_class + lo) == 1 ? 1 : 0;
+}
+
+// Work descriptors of every key of class cls (one per qm q), 0 elsewhere and
+// in the last bucket (failed q): m = n_keys + 1 entries.
+__global__ void group_count_kernel(const int32_t* counts, long long n_keys, int qmax, GroupSplit split, int cls,
+                                   int32_t* nd) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k <= n_keys;
+       k += (long long)gridDim.x * blockDim.x) {
+    int v = 0;
+    const int c = k < n_keys ? counts[k] : 0;
+    if (c > 0 && key_class(split, k) == cls) {
+      const int qm = cls ? split.qmax : qmax;
+      v = (c + qm - 1) / qm;
+    }
+    nd[k] = v;
+  }
+}
+
+// One work descriptor per qmax q of every key, at the key's place in the
+// exclusive scans dpos0 (class 0) and dpos1 (class 1) of the descriptor
+// counts, so descriptors follow key order (the gathers take them in that
+// order, and neighbouring keys share vertex rows).  With split.item_class
+// set, keys of class-1 items take split.qmax q per descriptor and go to the
 // second list, written downwards from split.groups_end.
 __global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets, long long n_keys, int qmax,
-                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split) {
+                                   GroupDesc* groups, int32_t* n_groups, GroupSplit split, const int32_t* dpos0,
+                                   const int32_t* dpos1) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *n_groups = dpos0[n_keys];
+    if (split.item_class) *split.n_groups = dpos1[n_keys];
+  }
   for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n_keys; k += (long long)gridDim.x * blockDim.x) {
     const int c = counts[k];
     if (c <= 0) continue;
-    bool second = false;
-    if (split.item_class) {
-      int lo = 0, hi = split.n_items - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (__ldg(split.key_off + mid) <= k) lo = mid;
-        else hi = mid - 1;
-      }
-      second = __ldg(split.item_class + lo) == 1;
-    }
+    const bool second = key_class(split, k) == 1;
     const int qm = second ? split.qmax : qmax;
     const int nd = (c + qm - 1) / qm;
-    const int slot = atomicAdd(second ? split.n_groups : n_groups, nd);
+    const int slot = second ? dpos1[k] : dpos0[k];
     for (int d = 0; d < nd; ++d) {
       GroupDesc g;
       g.key = (int32_t)k;
@@ -1927,7 +1960,7 @@ __global__ void make_groups_kernel(const int32_t* counts, const int32_t* offsets
 size_t group_scratch_ints(long long n_keys) {
   const long long m = n_keys + 1;
   const long long nb = (m + kScanThreads * kScanPer - 1) / (kScanThreads * kScanPer);
-  return (size_t)(3 * m + nb + 8);
+  return (size_t)(5 * m + nb + 8);
 }
 
 int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax, int32_t* scratch, int32_t* order,
@@ -1939,9 +1972,9 @@ int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax,
   int32_t* offsets = scratch + m;
   int32_t* cursor = scratch + 2 * m;
   int32_t* bsums = scratch + 3 * m;
+  int32_t* dpos0 = scratch + 3 * m + nb;
+  int32_t* dpos1 = dpos0 + m;
   cudaMemsetAsync(counts, 0, sizeof(int32_t) * m, s);
-  cudaMemsetAsync(n_groups, 0, sizeof(int32_t), s);
-  if (split.item_class) cudaMemsetAsync(split.n_groups, 0, sizeof(int32_t), s);
   long long blocks = (n + 255) / 256;
   if (blocks > 8192) blocks = 8192;
   key_hist_kernel<<<(unsigned)blocks, 256, 0, s>>>(key, n, counts);
@@ -1949,11 +1982,22 @@ int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax,
   scan_blocks_kernel<<<1, 32, 0, s>>>(bsums, (int)nb);
   scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(counts, m, bsums, offsets, cursor);
   key_scatter_kernel<<<(unsigned)blocks, 256, 0, s>>>(key, n, cursor, order);
-  long long kb = (n_keys + 255) / 256;
+  long long kb = (m + 255) / 256;
   if (kb > 8192) kb = 8192;
-  if (kb < 1) kb = 1;
-  make_groups_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, offsets, n_keys, qmax, groups, n_groups, split);
-  return 7;
+  int launches = 5;
+  // descriptor positions per class: counts into the free cursor array, then
+  // an exclusive scan
+  for (int cls = 0; cls < (split.item_class ? 2 : 1); ++cls) {
+    int32_t* dpos = cls ? dpos1 : dpos0;
+    group_count_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, n_keys, qmax, split, cls, cursor);
+    scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(cursor, m, bsums);
+    scan_blocks_kernel<<<1, 32, 0, s>>>(bsums, (int)nb);
+    scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, s>>>(cursor, m, bsums, dpos, nullptr);
+    launches += 4;
+  }
+  make_groups_kernel<<<(unsigned)kb, 256, 0, s>>>(counts, offsets, n_keys, qmax, groups, n_groups, split, dpos0,
+                                                  dpos1);
+  return launches + 1;
 }
 
 }  // namespace brx

@@ -71,6 +71,7 @@ struct brx_handle {
   int num_sms = 0;
   size_t smem_optin = 0;
   DevGeom g{};
+  const int32_t* rank_cube = nullptr;  // device, inverse of g.cube_rank
   std::vector<DevBuf> tables;
   brx_geometry host_geom{};
   std::vector<double> rot_cart;

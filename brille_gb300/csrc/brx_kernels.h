@@ -39,6 +39,7 @@ struct GatherParams {
   // trellis (group key decoding)
   int n_cube;
   const int32_t* cube_vertices;
+  const int32_t* rank_cube;  // group-key rank → cube index (Morton order of the cube nodes)
   const int32_t* tet_vertices;
   // vertex data
   const void* data;          // n_vertices × B × s (complex: interleaved pairs)

@@ -552,7 +552,7 @@ __device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, c
       int slot = 0;
       for (int j = 0; j < 8; ++j)
         if (__ldg(cv + 7 - j) == vi[0]) { slot = j; break; }
-      key = 8 * ni + slot;
+      key = 8 * __ldg(g.cube_rank + ni) + slot;
     } else {
       const int32_t* tv = g.tet_vertices + 4 * (long long)nt[1];
       int slot = 0;
