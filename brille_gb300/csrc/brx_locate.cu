@@ -498,40 +498,21 @@ __device__ __forceinline__ SmemZone stage_zone(const DevGeom& g, double* smem_d)
   return z;
 }
 
-// Move, wedge search and trellis locate of the q at Qq; writes its records
-// at index i and returns its status.  key_base/key_fail: the batch-wide group
-// key of the trellis's first key and of every failed q.
-__device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, const double* Qq, long long i, int mode,
-                                          const Records& r, int key_base, int key_fail) {
-  double Qi[3] = {Qq[0], Qq[1], Qq[2]};
-  double q[3];
-  int32_t tau[3] = {0, 0, 0}, rot[2] = {g.identity, g.identity};
-  int st = 0;
-  if (mode == 2) {
-    q[0] = Qi[0]; q[1] = Qi[1]; q[2] = Qi[2];
-  } else {
-    st = moveinto_one(g, z, Qi, q, tau);
-    if (!st && mode == 1) st = wedge_one(g, z, q, rot);
-  }
-  int32_t nt[2] = {-1, -1}, vi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+// Node weights and the remaining records (node, tetrahedron, weights,
+// status, group key) of the q at record index i whose trellis coordinates
+// x lie in node (node < 0: not found).  Returns its status.
+__device__ __forceinline__ int locate_finish(const DevGeom& g, long long node, const double x[3], long long i,
+                                             const Records& r, int key_base, int key_fail) {
+  int32_t nt[2] = {(int32_t)node, -1}, vi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int nw = 0;
-  if (!st) {
-    double x[3];
-    hkl_to_xyz(x, g.outer_B, q);
-    long long node = node_subscript(g, x);
-    nt[0] = (int32_t)node;
-    if (node < 0) {
-      st = BRX_ERR_NOT_FOUND;
-    } else {
-      int k = node_weights(g, node, x, &nt[1], vi, w);
-      if (k > 0) nw = k;
-      else st = (k == 0) ? BRX_ERR_NOT_FOUND : -k;
-    }
+  int nw = 0, st = 0;
+  if (node < 0) {
+    st = BRX_ERR_NOT_FOUND;
+  } else {
+    int k = node_weights(g, node, x, &nt[1], vi, w);
+    if (k > 0) nw = k;
+    else st = (k == 0) ? BRX_ERR_NOT_FOUND : -k;
   }
-  r.q_ir[3 * i] = q[0]; r.q_ir[3 * i + 1] = q[1]; r.q_ir[3 * i + 2] = q[2];
-  if (r.tau) { r.tau[3 * i] = tau[0]; r.tau[3 * i + 1] = tau[1]; r.tau[3 * i + 2] = tau[2]; }
-  r.rot[2 * i] = rot[0]; r.rot[2 * i + 1] = rot[1];
   r.node[2 * i] = nt[0]; r.node[2 * i + 1] = nt[1];
   r.nw[i] = nw;
 #pragma unroll
@@ -545,7 +526,6 @@ __device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, c
   r.status[i] = st;
   int32_t key = (int32_t)n_group_keys(g.n_cube, g.n_tets);  // failed q: last bucket
   if (!st) {
-    const long long node = nt[0];
     if (nt[1] < 0) {
       const int32_t ni = __ldg(g.node_index + node);
       const int32_t* cv = g.cube_vertices + 8 * (long long)ni;
@@ -565,19 +545,124 @@ __device__ __forceinline__ int locate_one(const DevGeom& g, const SmemZone& z, c
   return st;
 }
 
+// Failed move or wedge search: empty records with status st.
+__device__ __forceinline__ void locate_failed(long long i, int st, const Records& r, int key_fail) {
+  r.node[2 * i] = -1; r.node[2 * i + 1] = -1;
+  r.nw[i] = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) { r.vidx[8 * i + k] = 0; r.w[8 * i + k] = 0.0; }
+  if (r.w32) {
+    float4* w4 = reinterpret_cast<float4*>(r.w32 + 8 * i);
+    w4[0] = w4[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  r.status[i] = st;
+  r.key[i] = key_fail;
+}
+
+// Move and wedge search of the q at Qq (records q_ir, τ, R at index i) and
+// its trellis coordinates and node.  Returns the status of the move.
+__device__ __forceinline__ int locate_front(const DevGeom& g, const SmemZone& z, const double* Qq, long long i,
+                                            int mode, const Records& r, double x[3], long long* node) {
+  double Qi[3] = {Qq[0], Qq[1], Qq[2]};
+  double q[3];
+  int32_t tau[3] = {0, 0, 0}, rot[2] = {g.identity, g.identity};
+  int st = 0;
+  if (mode == 2) {
+    q[0] = Qi[0]; q[1] = Qi[1]; q[2] = Qi[2];
+  } else {
+    st = moveinto_one(g, z, Qi, q, tau);
+    if (!st && mode == 1) st = wedge_one(g, z, q, rot);
+  }
+  r.q_ir[3 * i] = q[0]; r.q_ir[3 * i + 1] = q[1]; r.q_ir[3 * i + 2] = q[2];
+  if (r.tau) { r.tau[3 * i] = tau[0]; r.tau[3 * i + 1] = tau[1]; r.tau[3 * i + 2] = tau[2]; }
+  r.rot[2 * i] = rot[0]; r.rot[2 * i + 1] = rot[1];
+  *node = -1;
+  if (!st) {
+    hkl_to_xyz(x, g.outer_B, q);
+    *node = node_subscript(g, x);
+  }
+  return st;
+}
+
+// q whose node is a polyhedron wait in a CTA queue and are finished
+// together, a full warp at a time: the tetrahedron path is long and taken
+// by few q, and per-lane it would hold every warp that has one such q.
+template <int CAP>
+struct PolyQueue {
+  int count;
+  long long rec[CAP];   // record index
+  long long qerr[CAP];  // index reported with an error
+  long long node[CAP];
+  double x[CAP][3];
+};
+
+template <int CAP>
+__device__ __forceinline__ void poly_push(PolyQueue<CAP>& pq, long long i, long long qerr, long long node,
+                                          const double x[3]) {
+  const int k = atomicAdd(&pq.count, 1);
+  pq.rec[k] = i;
+  pq.qerr[k] = qerr;
+  pq.node[k] = node;
+  pq.x[k][0] = x[0]; pq.x[k][1] = x[1]; pq.x[k][2] = x[2];
+}
+
+// All threads of the CTA: finish every queued q, then empty the queue.
+template <int CAP>
+__device__ __forceinline__ void poly_drain(PolyQueue<CAP>& pq, const DevGeom& g, const Records& r, int key_base,
+                                           int key_fail, ErrorWord* err) {
+  __syncthreads();
+  const int c = pq.count;
+  for (int k = threadIdx.x; k < c; k += blockDim.x) {
+    const double x[3] = {pq.x[k][0], pq.x[k][1], pq.x[k][2]};
+    const int st = locate_finish(g, pq.node[k], x, pq.rec[k], r, key_base, key_fail);
+    if (st) report(err, pq.qerr[k], st);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) pq.count = 0;
+  __syncthreads();
+}
+
+// One q: front, then either its cube (or failure) finished here or its
+// polyhedron queued.
+template <int CAP>
+__device__ __forceinline__ void locate_step(const DevGeom& g, const SmemZone& z, PolyQueue<CAP>& pq, const double* Qq,
+                                            long long i, long long qerr, int mode, const Records& r, int key_base,
+                                            int key_fail, ErrorWord* err) {
+  double x[3] = {0.0, 0.0, 0.0};
+  long long node = -1;
+  int st = locate_front(g, z, Qq, i, mode, r, x, &node);
+  if (st) {
+    locate_failed(i, st, r, key_fail);
+  } else if (node >= 0 && __ldg(g.node_type + node) == BRX_NODE_POLY) {
+    poly_push(pq, i, qerr, node, x);
+    return;
+  } else {
+    st = locate_finish(g, node, x, i, r, key_base, key_fail);
+  }
+  if (st) report(err, qerr, st);
+}
+
+constexpr int kPolyCap = 2 * kLocateThreads;
+
 // mode: 0 interpolate_at (moveinto), 1 ir_interpolate_at (ir_moveinto),
 // 2 no move (Q already in the trellis domain)
 __global__ void __launch_bounds__(kLocateThreads)
 locate_kernel(DevGeom g, const double* __restrict__ Q, long long n, long long base, int mode,
               Records r, ErrorWord* err) {
   extern __shared__ double smem_d[];
+  __shared__ PolyQueue<kPolyCap> pq;
   const SmemZone z = stage_zone(g, smem_d);
+  if (threadIdx.x == 0) pq.count = 0;
   __syncthreads();
   const int key_fail = (int)n_group_keys(g.n_cube, g.n_tets);
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int st = locate_one(g, z, Q + 3 * i, i, mode, r, 0, key_fail);
-    if (st) report(err, base + i, st);
+  // rounds of one q per thread, the same count for every thread of the CTA
+  for (long long i0 = blockIdx.x * (long long)blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
+    const long long i = i0 + threadIdx.x;
+    if (i < n) locate_step(g, z, pq, Q + 3 * i, i, base + i, mode, r, 0, key_fail, err);
+    __syncthreads();
+    if (pq.count >= (int)blockDim.x) poly_drain(pq, g, r, 0, key_fail, err);
   }
+  poly_drain(pq, g, r, 0, key_fail, err);
 }
 
 // Many trellises in one persistent launch.  Work comes in tiles of one
@@ -592,8 +677,10 @@ locate_batch_kernel(const DevGeom* __restrict__ geoms, const long long* __restri
                     const double* const* __restrict__ Qptr, int mode, Records r, ErrorWord* err) {
   extern __shared__ double smem_d[];
   __shared__ DevGeom s_geom;
+  __shared__ PolyQueue<2 * THREADS> pq;
   int cur = -1;
   SmemZone z{};
+  if (threadIdx.x == 0) pq.count = 0;
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const int4 tile = tiles[t];
     if (tile.x != cur) {
@@ -609,11 +696,15 @@ locate_batch_kernel(const DevGeom* __restrict__ geoms, const long long* __restri
     const double* Q = Qptr[cur];
     const long long qo = q_off[cur];
     const int kb = key_off[cur];
-    for (int k = threadIdx.x; k < tile.z; k += THREADS) {
+    for (int k0 = 0; k0 < tile.z; k0 += THREADS) {
+      const int k = k0 + threadIdx.x;
       const long long il = (long long)tile.y + k;
-      const int st = locate_one(g, z, Q + 3 * il, qo + il, mode, r, kb, key_fail);
-      if (st) report(err + cur, il, st);
+      if (k < tile.z) locate_step(g, z, pq, Q + 3 * il, qo + il, il, mode, r, kb, key_fail, err + cur);
+      __syncthreads();
+      if (pq.count >= THREADS) poly_drain(pq, g, r, kb, key_fail, err + cur);
     }
+    // the queue holds this item's q only
+    poly_drain(pq, g, r, kb, key_fail, err + cur);
   }
 }
 
