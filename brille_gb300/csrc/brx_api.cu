@@ -570,6 +570,33 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
   UP(G.node_type, G.n_nodes, g.node_type);
   UP(G.node_index, G.n_nodes, g.node_index);
   UP(G.cube_vertices, 8LL * G.n_cube, g.cube_vertices);
+  // cube corners on the two corner planes of every axis (cube_canon)
+  {
+    g.cube_canon = 0;
+    g.cube_pattern = 0;
+    bool canon = G.n_cube > 0;
+    int pattern = 0;
+    for (long long c = 0; c < G.n_cube && canon; ++c) {
+      const int32_t* cv = G.cube_vertices + 8 * c;
+      const double* a3 = G.vertex_xyz + 3 * (long long)cv[0];
+      const double* b3 = G.vertex_xyz + 3 * (long long)cv[7];
+      int pat = 0;
+      for (int i = 0; i < 8 && canon; ++i) {
+        const double* v = G.vertex_xyz + 3 * (long long)cv[i];
+        for (int d = 0; d < 3; ++d) {
+          if (a3[d] == b3[d]) { canon = false; break; }
+          if (v[d] == b3[d]) pat |= 1 << (3 * i + d);
+          else if (v[d] != a3[d]) { canon = false; break; }
+        }
+      }
+      if (c == 0) pattern = pat;
+      else if (pat != pattern) canon = false;
+    }
+    if (canon) {
+      g.cube_canon = 1;
+      g.cube_pattern = pattern;
+    }
+  }
   // Morton order of the cube nodes' (i, j, k) for the group keys
   {
     const long long nx = G.n_knots[0] - 1, ny = G.n_knots[1] - 1;
@@ -677,6 +704,8 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
     // BRX_EXACT_PREDICATES=1 turns the screens off (every predicate in FP64)
     const char* env = std::getenv("BRX_EXACT_PREDICATES");
     if (env && env[0] == '1') ok = false;
+    // the zero comparisons' screens assume the default tolerance's values
+    if (!(g.t_def.rel <= 1e-11 && g.t_def.abs_ == 5e-15)) ok = false;
     g.screen = ok ? 1 : 0;
     UP(plane.data(), plane.size(), g.face_plane32);
     UP(band.data(), band.size(), g.face_band32);

@@ -130,6 +130,11 @@ struct DevGeom {
   float wedge_band32;          // width of the wedge tolerance band
   const float* tet_plane32;    // n_tets × 4 × (a_x, a_y, a_z, c): barycentric w_j(x) = a_j·x + c_j
   int32_t screen;              // 0 disables the screens (exact FP64 everywhere)
+  // Every cube's corner i sits at corner 0's or corner 7's coordinate on
+  // each axis d, bit d of 3-bit field i of cube_pattern choosing corner 7:
+  // the cube weights then take |x_d − a_d| and |x_d − b_d| once per axis.
+  int32_t cube_canon;
+  int32_t cube_pattern;
   Tol t_main;               // (float_tolerance, digit)
   Tol t_def;                // (0, 1): the reference's default comparisons
 };

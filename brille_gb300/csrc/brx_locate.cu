@@ -333,6 +333,30 @@ __device__ __forceinline__ void load3(double out[3], const double* p) {
   out[0] = __ldg(p); out[1] = __ldg(p + 1); out[2] = __ldg(p + 2);
 }
 
+// approx(w, 0, t_def) and cmp_gt(w, 0, t_def) from the bits of w where w is
+// far from the tolerance band.  t_def has rel = 1e4·ε (2.2e-12) and abs =
+// 5e-15, so approx(w, 0) — |w| ≤ 5e-15 + 2.2e-12·|w| in FP64 — holds for
+// every |w| < 4e-15 and fails for every finite |w| > 1e-14; in between, and
+// for infinities and NaN, the FP64 test runs.  Integer compares keep the
+// FP64 pipe free.
+__device__ __forceinline__ bool approx0_def(const DevGeom& g, double w) {
+  if (g.screen) {
+    const long long b = __double_as_longlong(w) & 0x7fffffffffffffffLL;
+    if (b > __double_as_longlong(1e-14) && b < 0x7ff0000000000000LL) return false;
+    if (b < __double_as_longlong(4e-15)) return true;
+  }
+  return approx(w, 0.0, g.t_def);
+}
+__device__ __forceinline__ bool gt0_def(const DevGeom& g, double w) {
+  if (g.screen) {
+    const long long b = __double_as_longlong(w);
+    if (b < 0) return false;  // negative (or −NaN): w > 0 fails
+    if (b > __double_as_longlong(1e-14) && b < 0x7ff0000000000000LL) return true;
+    if (b < __double_as_longlong(4e-15)) return false;
+  }
+  return cmp_gt(w, 0.0, g.t_def);
+}
+
 __device__ double tet_contains(const DevGeom& g, long long t, const double x[3], double w[4], bool shortcut) {
   if (shortcut) {
     double s[4];
@@ -360,7 +384,7 @@ __device__ double tet_contains(const DevGeom& g, long long t, const double x[3],
   bool any_neg = false;
   double mn = w[0];
   for (int j = 0; j < 4; ++j) {
-    if (w[j] < 0.0 && !approx(w[j], 0.0, g.t_def)) any_neg = true;
+    if (w[j] < 0.0 && !approx0_def(g, w[j])) any_neg = true;
     if (w[j] < mn) mn = w[j];
   }
   return any_neg ? mn : 0.0;
@@ -399,13 +423,31 @@ __device__ int node_weights(const DevGeom& g, long long node, const double x[3],
     double vol = 1.0;
     for (int d = 0; d < 3; ++d) vol = dmul(vol, fabs(dsub(a[d], b[d])));
     int n = 0;
+    if (g.cube_canon) {
+      // corner i's factor on axis d is |x_d − a_d| or |x_d − b_d|, and
+      // ((1·f0)·f1)·f2 = (f0·f1)·f2 exactly: the same products, formed once
+      double da[3], db[3];
+      for (int d = 0; d < 3; ++d) {
+        da[d] = fabs(dsub(x[d], a[d]));
+        db[d] = fabs(dsub(x[d], b[d]));
+      }
+      double p01[4];
+      for (int k = 0; k < 4; ++k) p01[k] = dmul((k & 1) ? db[0] : da[0], (k & 2) ? db[1] : da[1]);
+      for (int i = 0; i < 8; ++i) {
+        const int bits = (g.cube_pattern >> (3 * i)) & 7;
+        const double p = dmul(p01[bits & 3], (bits & 4) ? db[2] : da[2]);
+        const double wi = __ddiv_rn(p, vol);
+        if (gt0_def(g, wi)) { vidx[n] = ids[7 - i]; w8[n] = wi; ++n; }
+      }
+      return n;
+    }
     for (int i = 0; i < 8; ++i) {
       double v[3];
       load3(v, g.vertex_xyz + 3 * (long long)ids[i]);
       double p = 1.0;
       for (int d = 0; d < 3; ++d) p = dmul(p, fabs(dsub(x[d], v[d])));
       double wi = __ddiv_rn(p, vol);
-      if (cmp_gt(wi, 0.0, g.t_def)) { vidx[n] = ids[7 - i]; w8[n] = wi; ++n; }
+      if (gt0_def(g, wi)) { vidx[n] = ids[7 - i]; w8[n] = wi; ++n; }
     }
     return n;
   }
@@ -423,7 +465,7 @@ __device__ int node_weights(const DevGeom& g, long long node, const double x[3],
         if (tet_contains(g, t, x, w, true) >= 0.0) {
           int n = 0;
           for (int j = 0; j < 4; ++j)
-            if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
+            if (!approx0_def(g, w[j])) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
           *tet_out = t;
           return n;
         }
@@ -436,7 +478,7 @@ __device__ int node_weights(const DevGeom& g, long long node, const double x[3],
       if (mn >= 0.0) {
         int n = 0;
         for (int j = 0; j < 4; ++j)
-          if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
+          if (!approx0_def(g, w[j])) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)t + j); w8[n] = w[j]; ++n; }
         *tet_out = t;
         return n;
       }
@@ -447,7 +489,7 @@ __device__ int node_weights(const DevGeom& g, long long node, const double x[3],
     if (val > 0.0) return -BRX_ERR_IMPOSSIBLE;
     int n = 0;
     for (int j = 0; j < 4; ++j)
-      if (!approx(w[j], 0.0, g.t_def)) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)best_i + j); w8[n] = w[j]; ++n; }
+      if (!approx0_def(g, w[j])) { vidx[n] = __ldg(g.tet_vertices + 4 * (long long)best_i + j); w8[n] = w[j]; ++n; }
     *tet_out = best_i;
     return n;
   }
