@@ -266,11 +266,27 @@ __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32
 // find_bin: the first knot greater than x (std::find_if in the reference)
 // found by bisection, which gives the same index because knots increase
 // strictly; a NaN compares false everywhere and lands past the end as there.
+// The comparisons run on integer keys of the doubles (the bit pattern,
+// negatives with their magnitude bits flipped), which order non-NaN values
+// as IEEE does once x's −0 is taken as +0; a NaN x compares in FP64.
+__device__ __forceinline__ long long order_key(long long b) { return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL); }
+
 __device__ __forceinline__ int find_bin(const double* e, int n, double x) {
   int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (__ldg(e + mid) > x) hi = mid; else lo = mid + 1;
+  long long xb = __double_as_longlong(x);
+  if ((xb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) {
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(e + mid) > x) hi = mid; else lo = mid + 1;
+    }
+  } else {
+    if (xb == (long long)0x8000000000000000ULL) xb = 0;
+    const long long xk = order_key(xb);
+    const long long* eb = reinterpret_cast<const long long*>(e);
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (order_key(__ldg(eb + mid)) > xk) hi = mid; else lo = mid + 1;
+    }
   }
   int d = lo;
   if (d > n - 1 && x < __ldg(e)) d = 0;
