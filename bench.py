@@ -710,7 +710,7 @@ def main():
         vh = torch.empty((ne, B), dtype=fdt, pin_memory=True)
         ch = torch.empty((ne, B, na, 3), dtype=cdt, pin_memory=True)
         # freshly pinned pages reach full link speed only after a few passes
-        for _ in range(max(3, args.warmup)):
+        for _ in range(max(6, args.warmup)):
             grid.query_into(Qh, ne, vh, ch, out_f32=out_f32)
         t0 = time.perf_counter()
         step_s = []
