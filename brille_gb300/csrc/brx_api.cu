@@ -592,7 +592,10 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
       if (c == 0) pattern = pat;
       else if (pat != pattern) canon = false;
     }
-    if (canon) {
+    // BRX_EXACT_PREDICATES=1 (every predicate in FP64, no screens) also
+    // keeps the per-corner cube weights, for comparison
+    const char* exact_env = std::getenv("BRX_EXACT_PREDICATES");
+    if (canon && !(exact_env && exact_env[0] == '1')) {
       g.cube_canon = 1;
       g.cube_pattern = pattern;
     }

@@ -271,10 +271,10 @@ __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32
 // as IEEE does once x's −0 is taken as +0; a NaN x compares in FP64.
 __device__ __forceinline__ long long order_key(long long b) { return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL); }
 
-__device__ __forceinline__ int find_bin(const double* e, int n, double x) {
+__device__ __forceinline__ int find_bin(const double* e, int n, double x, bool int_keys) {
   int lo = 0, hi = n;
   long long xb = __double_as_longlong(x);
-  if ((xb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) {
+  if (!int_keys || (xb & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL) {
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (__ldg(e + mid) > x) hi = mid; else lo = mid + 1;
@@ -308,7 +308,7 @@ __device__ __forceinline__ bool sub_ok_not_null(const DevGeom& g, const int s[3]
 
 __device__ long long node_subscript(const DevGeom& g, const double x[3]) {
   int sub[3], close[3], ns[3];
-  for (int d = 0; d < 3; ++d) sub[d] = find_bin(g.knots[d], g.n_knots[d], x[d]);
+  for (int d = 0; d < 3; ++d) sub[d] = find_bin(g.knots[d], g.n_knots[d], x[d], g.screen != 0);
   bool bad = !sub_ok_not_null(g, sub);
   if (bad) {
     int num_close = 0;

@@ -218,12 +218,14 @@ def test_permutation_table():
     assert np.abs(gc.reshape(oc.shape) - oc).max() < 1e-12
 
 
-def test_fp32_screens_match_exact_predicates():
-    """The FP32 screens of the locate stage change no decision: a handle
-    created with BRX_EXACT_PREDICATES=1 (all predicates in FP64) returns the
-    same indices on points within 1e-6 r.l.u. of every kind of boundary."""
+@pytest.mark.parametrize("name", ["hex16", "diamond2"])
+def test_fp32_screens_match_exact_predicates(name):
+    """The shortcuts of the locate stage change no decision and no bit: a
+    handle created with BRX_EXACT_PREDICATES=1 (all predicates in FP64, knot
+    comparisons in FP64, per-corner cube weights) returns the same records on
+    points within 1e-9 r.l.u. of every kind of boundary."""
     import os
-    c = crystal_case("hex16")
+    c = crystal_case(name)
     Q = np.concatenate([_queries(c, 4000, seed=21), boundary_q(c, 6000, seed=22, delta=1e-9)])
     a = _grid(c).locate(Q)
     os.environ["BRX_EXACT_PREDICATES"] = "1"
