@@ -248,6 +248,66 @@ class TrellisBuild:
     def n_nodes(self):
         return self.node_type.size
 
+    # ---------------------------------------------------------- persistence
+    # The reference persists a trellis through HDF5 (bz_trellis.hpp:198-224);
+    # here the flat tables go to one .npz file, with a fingerprint of the
+    # construction inputs so that a cache can tell a stale file.
+    _TABLES = ("vertices", "cube_vertices", "node_type", "node_index", "poly_tet_offset", "tet_vertices",
+               "tet_sphere", "tet_volume")
+
+    @staticmethod
+    def fingerprint(ir_vertices, ir_halfspaces, max_volume, always_triangulate=False):
+        """SHA-256 of the construction inputs (exact bytes)."""
+        import hashlib
+        h = hashlib.sha256()
+        h.update(np.ascontiguousarray(ir_vertices, float).tobytes())
+        h.update(np.ascontiguousarray(ir_halfspaces, float).tobytes())
+        h.update(np.float64(max_volume).tobytes())
+        h.update(b"t" if always_triangulate else b"f")
+        return h.hexdigest()
+
+    def save(self, path, fingerprint=""):
+        """Write the tables to path (.npz)."""
+        arrays = {k: getattr(self, k) for k in self._TABLES}
+        for d in range(3):
+            arrays[f"knots{d}"] = np.asarray(self.knots[d], float)
+        arrays["shape"] = np.asarray(self.shape, np.int64)
+        arrays["fingerprint"] = np.array(fingerprint)
+        np.savez(path, **arrays)
+
+    @classmethod
+    def load(cls, path, fingerprint=None):
+        """Tables saved by save(); with fingerprint given, a file made from
+        other inputs raises ValueError."""
+        z = np.load(path, allow_pickle=False)
+        if fingerprint is not None and str(z["fingerprint"]) != fingerprint:
+            raise ValueError(f"{path}: trellis tables were built from other inputs")
+        t = cls.__new__(cls)
+        for k in cls._TABLES:
+            setattr(t, k, z[k])
+        t.knots = [z[f"knots{d}"] for d in range(3)]
+        t.shape = tuple(int(x) for x in z["shape"])
+        nx, ny, nz = t.shape
+        if (t.node_type.size != nx * ny * nz or any(len(t.knots[d]) != t.shape[d] + 1 for d in range(3))
+                or t.poly_tet_offset.size < 1 or t.poly_tet_offset[-1] != len(t.tet_vertices)):
+            raise ValueError(f"{path}: inconsistent trellis tables")
+        return t
+
+    @classmethod
+    def cached(cls, ir_vertices, ir_halfspaces, max_volume, path, always_triangulate=False):
+        """Load the trellis for these inputs from path if it holds them, else
+        build it and write it there."""
+        import os
+        fp = cls.fingerprint(ir_vertices, ir_halfspaces, max_volume, always_triangulate)
+        if os.path.exists(path):
+            try:
+                return cls.load(path, fingerprint=fp)
+            except ValueError:
+                pass
+        t = cls(ir_vertices, ir_halfspaces, max_volume, always_triangulate)
+        t.save(path, fingerprint=fp)
+        return t
+
     def summary(self):
         return dict(vertices=len(self.vertices), cube=int(np.sum(self.node_type == NODE_CUBE)),
                     poly=int(np.sum(self.node_type == NODE_POLY)), tets=len(self.tet_vertices),
