@@ -450,6 +450,71 @@ def run_batch(args):
 LEARNED_COARSE = (("bz/625", 1 / 625), ("bz/200", 1 / 200))
 
 
+def run_sqw(args):
+    """The structure factor of the interpolated modes (the consumer brille
+    feeds) on the headline workload: values + S per q and mode from the
+    fused gather, against values + eigenvectors from ir_interpolate_at on
+    the same q, both with Q and outputs in HBM."""
+    import torch
+
+    from brille_gb300 import BZTrellisQdc
+
+    wl = build_workload(args.workload)
+    B, na = wl["w"].shape[1], wl["v"].shape[2]
+    grid = BZTrellisQdc(wl["bz"], trellis=wl["tr"])
+    grid.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage=args.storage)
+    rng = np.random.default_rng(5)
+    grid.set_atoms(rng.uniform(0.3, 1.0, na), np.asarray(wl["lat"].basis.positions, float))
+    n = args.q_per_step or WORKLOADS[args.workload][3]
+    dev = torch.device("cuda")
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1000)
+    Q = (torch.rand((n, 3), generator=gen, device=dev, dtype=torch.float64) * 2 - 1) * wl["q_range"]
+    vals = torch.empty((n, B), dtype=torch.float32, device=dev)
+    sf = torch.empty((n, B), dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(dev)
+    sp = stream.cuda_stream
+    if args.tuning:
+        grid.set_tuning([int(x) for x in args.tuning.split(",")])
+    elif not args.no_tune:
+        grid.tune(Q, out_f32=True, reps=2, stream=sp, values_out=vals,
+                  vectors_out=torch.empty((n, B, na, 3), dtype=torch.complex64, device=dev))
+        torch.cuda.empty_cache()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        grid.sync(sp)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        grid.profile(True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        grid.sync(sp)
+        torch.cuda.synchronize()
+        stage_ms = grid.stage_times()[0]
+        grid.profile(False)
+        return e0.elapsed_time(e1) / args.steps, [round(x / args.steps, 3) for x in stage_ms]
+
+    ms_sf, st_sf = timed(lambda: grid.structure_factor_into(Q, n, vals, sf, async_=True, stream=sp))
+    vecs = torch.empty((n, B, na, 3), dtype=torch.complex64, device=dev)
+    ms_v, st_v = timed(lambda: grid.query_into(Q, n, vals, vecs, out_f32=True, async_=True, stream=sp))
+    out = dict(mode="sqw", metric="q-points/s, values + structure factor per mode", value=n / (ms_sf / 1e3),
+               unit="q-points/s", ms_per_step=ms_sf, steps=args.steps, warmup=args.warmup,
+               stage_ms_per_step=dict(zip(["locate", "grouping", "values", "structure_factor"], st_sf)),
+               vectors_path=dict(value=n / (ms_v / 1e3), ms_per_step=ms_v,
+                                 stage_ms_per_step=dict(zip(["locate", "grouping", "values", "vectors"], st_v)),
+                                 note="the same q through ir_interpolate_at, eigenvectors written to HBM"),
+               speedup_vs_vectors=ms_v / ms_sf,
+               config=dict(workload=args.workload, q_per_step=n, modes=B, atoms=na, storage=args.storage,
+                           outputs="f32 values + f32 S per mode (8 B per q and mode) vs c64 eigenvectors "
+                                   f"({24 * na} B per q and mode)"),
+               data="synthetic (seeded BvK model, random atom weights), q uniform")
+    print(json.dumps(out), flush=True)
+
+
 def run_learned(args):
     """Learned residual on coarse trellises of the 2-atom FCC crystal
     (a = 4.96 Å, 28 amu, BZ/5000 for the fine trellis) against the plain
@@ -576,7 +641,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default gather shared-memory budgets")
     ap.add_argument("--tuning", default=None,
                     help="apply gather tuning values (5 integers, as config.tuning lists them) instead of tuning")
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned", "batch"],
+    ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned", "batch", "sqw"],
                     help="precision: FP32 and BF16 storage against the FP64 path; learned: the learned residual "
                          "on coarse trellises against the plain fine trellis")
     ap.add_argument("--train-q", type=int, default=0, help="learned mode: training samples (default 1e6)")
@@ -598,6 +663,8 @@ def main():
         return run_learned(args)
     if args.mode == "batch":
         return run_batch(args)
+    if args.mode == "sqw":
+        return run_sqw(args)
 
     import torch
 

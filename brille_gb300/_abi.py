@@ -63,6 +63,10 @@ class MlpDims(C.Structure):
 BRX_MLP_FP32 = 0x1
 
 
+class Atoms(C.Structure):
+    _fields_ = [("n_atoms", C.c_int32), ("weight", C.POINTER(C.c_double)), ("position", C.POINTER(C.c_double))]
+
+
 def _ptr(a, ctype):
     return a.ctypes.data_as(C.POINTER(ctype)) if a is not None and a.size else C.POINTER(ctype)()
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import Data, Geometry, LocateOut, MlpDims
+from ._abi import Atoms, Data, Geometry, LocateOut, MlpDims
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbrx.so")
@@ -76,6 +76,10 @@ def load(build_if_missing=True):
     lib.brx_mlp_forward.restype = C.c_int
     lib.brx_set_residual_model.argtypes = [h, md, vp, C.c_float, C.c_float, C.c_float]
     lib.brx_set_residual_model.restype = C.c_int
+    lib.brx_set_atoms.argtypes = [h, C.POINTER(Atoms)]
+    lib.brx_set_atoms.restype = C.c_int
+    lib.brx_ir_structure_factor.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    lib.brx_ir_structure_factor.restype = C.c_int
     bp = C.c_void_p
     lib.brx_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_int64), C.c_int32, C.c_uint32,
                                      C.POINTER(C.c_void_p)]

@@ -300,8 +300,10 @@ brx_status reset_errors(brx_handle* h, cudaStream_t s) {
 }
 
 // The whole query, chunked.  mode: 0 interpolate_at, 1 ir_interpolate_at.
+// sf: vecs_out receives the structure factor (float, n × B) instead of the
+// vectors (brx_ir_structure_factor).
 brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* vals_out, void* vecs_out,
-                     uint32_t flags, void* user_stream, const brx_locate_out* lout) {
+                     uint32_t flags, void* user_stream, const brx_locate_out* lout, bool sf = false) {
   if (!h) return BRX_ERR_INVALID_ARGUMENT;
   if (n < 0 || (n > 0 && !Q)) return fail(h, BRX_ERR_INVALID_ARGUMENT, "Q must be a non-null (n,3) array");
   BRX_CUDA(h, cudaSetDevice(h->device));
@@ -324,6 +326,16 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     }
   }
   const int kmode = no_move ? 2 : (ir ? 1 : 0);
+  if (sf) {
+    const Interp& c = h->vecs;
+    if (!c.present || !c.cplx || c.el[0] != 0 || c.el[2] != 0 || c.el[1] / 3 < 1 || c.el[1] / 3 > 32)
+      return fail(h, BRX_ERR_UNSUPPORTED, "the structure factor needs complex eigenvectors of 1-32 atoms and no "
+                                          "other elements");
+    if (c.store == ST_F64) return fail(h, BRX_ERR_UNSUPPORTED, "the structure factor needs FP32 or BF16 storage");
+    if (c.length_unit != BRX_LU_ANGSTROM || (ir && cmode != ROT_GAMMA))
+      return fail(h, BRX_ERR_UNSUPPORTED, "the structure factor needs Cartesian (Å) Γ-rotating eigenvectors");
+    if (h->sf_n != c.el[1] / 3) return fail(h, BRX_ERR_INVALID_ARGUMENT, "brx_set_atoms with one entry per atom first");
+  }
   if (n == 0) return BRX_OK;
 
   const bool q_host = host_ptr(Q);
@@ -348,7 +360,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   size_t out_q = 0;  // output bytes per q
   if (!locate_only) {
     out_q += (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
-    if (h->vecs.present) out_q += (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
+    if (h->vecs.present) out_q += sf ? (size_t)h->vecs.B * 4 : (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
   }
   long long chunk = 1LL << 24;
   // host outputs: chunks of about BRX_HOST_CHUNK_MB (default 512) MB of
@@ -376,7 +388,8 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     BRX_CUDA(h, cudaStreamWaitEvent(h->sc[1].stream, h->sc[0].done, 0));
   }
   const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
-  const size_t crow = h->vecs.present ? (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32) : 0;
+  const size_t crow = !h->vecs.present ? 0
+                      : sf ? (size_t)h->vecs.B * 4 : (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
   if (!locate_only && o_host) {
     for (int k = 0; k < nstreams; ++k) {
       BRX_CUDA(h, h->sc[k].vbuf.ensure(vrow * (size_t)chunk + 16));
@@ -442,7 +455,17 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       GatherParams p = gather_params(h, h->vecs, s, m, ir ? cmode : ROT_NONE, h->vecs.cplx, 1);
       p.out = cdst;
       p.MB = gather_pick_modes(p, h->vecs.store, h->vecs.cplx, smem_budget(h, 1));
-      h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h, 1), cs);
+      if (sf) {
+        p.sf_atoms = h->sf_n;
+        p.sf_Q = Qd;
+        p.sf_atom = static_cast<const double*>(h->sf_atoms.p);
+        p.sf_B = static_cast<const double*>(h->sf_B.p);
+        const int k = launch_structure_factor(p, h->vecs.store, h->num_sms, smem_budget(h, 1), cs);
+        if (k < 0) return fail(h, BRX_ERR_UNSUPPORTED, "the structure-factor gather does not fit this data");
+        h->launches += k;
+      } else {
+        h->launches += launch_gather(p, h->vecs.store, h->vecs.cplx, f32, h->num_sms, smem_budget(h, 1), cs);
+      }
     }
     if (ev[4]) {
       cudaEventRecord(ev[4], cs);
@@ -805,6 +828,8 @@ void brx_destroy(brx_handle* h) {
   h->mlp_b.release();
   h->mlp_x.release();
   h->mlp_wt.release();
+  h->sf_atoms.release();
+  h->sf_B.release();
   h->mlp_bt.release();
   if (h->err) cudaFree(h->err);
   if (h->err_host) cudaFreeHost(h->err_host);
@@ -960,6 +985,31 @@ brx_status brx_ir_interpolate_at(brx_handle* h, const double* Q, int64_t n, void
 brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out,
                               uint32_t flags, void* stream) {
   return run_query(h, 0, Q, n, values_out, vectors_out, flags, stream, nullptr);
+}
+
+brx_status brx_set_atoms(brx_handle* h, const brx_atoms* atoms) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!atoms || atoms->n_atoms < 1 || atoms->n_atoms > 32 || !atoms->weight || !atoms->position)
+    return fail(h, BRX_ERR_INVALID_ARGUMENT, "1-32 atoms with weights and positions are needed");
+  BRX_CUDA(h, cudaSetDevice(h->device));
+  std::vector<double> a(4 * (size_t)atoms->n_atoms);
+  for (int k = 0; k < atoms->n_atoms; ++k) {
+    a[4 * k] = atoms->weight[k];
+    for (int i = 0; i < 3; ++i) a[4 * k + 1 + i] = atoms->position[3 * k + i];
+  }
+  BRX_CUDA(h, h->sf_atoms.ensure(sizeof(double) * a.size()));
+  BRX_CUDA(h, cudaMemcpy(h->sf_atoms.p, a.data(), sizeof(double) * a.size(), cudaMemcpyHostToDevice));
+  BRX_CUDA(h, h->sf_B.ensure(sizeof(double) * 9));
+  BRX_CUDA(h, cudaMemcpy(h->sf_B.p, h->g.outer_B, sizeof(double) * 9, cudaMemcpyHostToDevice));
+  h->sf_n = atoms->n_atoms;
+  return BRX_OK;
+}
+
+brx_status brx_ir_structure_factor(brx_handle* h, const double* Q, int64_t n, void* values_out, float* sf_out,
+                                   uint32_t flags, void* stream) {
+  if (!h) return BRX_ERR_INVALID_ARGUMENT;
+  if (!sf_out && n > 0) return fail(h, BRX_ERR_INVALID_ARGUMENT, "output buffers must be provided");
+  return run_query(h, 1, Q, n, values_out, sf_out, flags, stream, nullptr, true);
 }
 
 brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir, uint32_t flags,

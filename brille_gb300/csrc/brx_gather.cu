@@ -872,13 +872,15 @@ constexpr int kWarpGatherMaxWarps = 8;
 constexpr long long kGatherSpin = 2000000000LL;
 
 struct WarpLayout {
-  size_t q, oq, w, M, rotf, ph, de, e, off, Y, mbar, total;
+  size_t q, oq, w, M, rotf, ph, de, e, off, sq, qc, Y, mbar, total;
   size_t ybuf;  // bytes of one staging buffer
 };
 
 // QM q per group; e_modes antiphase entries per slot and warp; na Γ phases
 // per q; ybuf bytes per staging buffer (two per warp)
-__host__ __device__ inline WarpLayout warp_layout(int QM, int e_modes, int na, long long ybuf, int warps) {
+// sf_atoms: atoms of the structure factor (0: vectors are written)
+__host__ __device__ inline WarpLayout warp_layout(int QM, int e_modes, int na, long long ybuf, int warps,
+                                                  int sf_atoms = 0) {
   WarpLayout L;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -896,6 +898,8 @@ __host__ __device__ inline WarpLayout warp_layout(int QM, int e_modes, int na, l
   L.de = take(4 * (size_t)nan * QM);
   L.e = take(4 * 2 * 8 * (size_t)e_modes * warps);
   L.off = take(2 * 8 * (size_t)e_modes * warps);
+  L.sq = take(8 * (size_t)sf_atoms * QM);    // c_k e^{2πi Q·x_k} per (q, atom)
+  L.qc = take(16 * (size_t)(sf_atoms > 0 ? QM : 0));  // Q·B per q
   L.ybuf = ((size_t)ybuf + 15) & ~size_t(15);
   L.Y = take(2 * L.ybuf * warps);
   L.mbar = take(16 * (size_t)warps);
@@ -1065,10 +1069,126 @@ __device__ __forceinline__ void warp_unit(const unsigned char* Yb, const unsigne
   }
 }
 
+// Structure factor of one block of modes (vector data only, mb·G ≤ 32
+// units, every lane of the warp taking part): per q the unit's Γ-rotated
+// eigenvector e_k of atom k, dotted with Q_c and weighted by c_k e^{2πi Q·x_k},
+// summed over the G atoms of the mode by a segmented shuffle reduction; the
+// mode's first lane writes |F|² at out[q·B + mode].
+template <int NS, typename St>
+__device__ __forceinline__ void warp_block_sf(const unsigned char* Yb, const unsigned char* so, int row_bytes, int MBw,
+                                              int mb, int G, const float* s_e, int pivot, const float2* s_w2,
+                                              const float2* s_M2, const int* s_rotf, const float* s_ph,
+                                              const int* s_de, const long long* s_oq, const float2* s_sq,
+                                              const float4* s_qc, int nsf, int count, int wslice, int qs, int wq,
+                                              bool gamma, int na, int b0, float* out) {
+  const int lane = threadIdx.x & 31;
+  const int U = mb * G;
+  const bool active = lane < qs * U;
+  const int u = active ? lane % U : 0;
+  const int lslice = active ? lane / U : 0;
+  const int mm = u / G, gi = u % G;
+  const int e0 = 3 * gi;
+  // the unit's corner rows with their antiphase (as warp_unit does)
+  float2 y[NS][3];
+#pragma unroll
+  for (int x = 0; x < NS; ++x) {
+    const bool usex = x >= pivot;
+    const float er = usex ? s_e[2 * (x * MBw + mm)] : 0.f, ei = usex ? s_e[2 * (x * MBw + mm) + 1] : 0.f;
+    const St* yp = reinterpret_cast<const St*>(Yb + (size_t)(x * MBw + mm) * row_bytes + so[x * MBw + mm]);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      float dr = 0.f, di = 0.f;
+      if (usex) ldY<float, St, true>(yp + (e0 + k) * 2, dr, di);
+      y[x][k] = make_float2(er * dr - ei * di, er * di + ei * dr);
+    }
+  }
+  const float2 zero = make_float2(0.f, 0.f);
+  const int jstep = wq * qs, jbase = wslice * qs;
+  const int trips = count > jbase ? (count - jbase + jstep - 1) / jstep : 0;
+  // this lane's term of F for q j: c_k e^{2πi Q·x_k} (Q_c · e_k)
+  auto term = [&](int j) -> float2 {
+    float2 wp[NS];
+#pragma unroll
+    for (int h = 0; h < NS / 2; ++h) {
+      const float4 w4 = reinterpret_cast<const float4*>(s_w2 + 8 * j)[h];
+      wp[2 * h] = make_float2(w4.x, w4.y);
+      wp[2 * h + 1] = make_float2(w4.z, w4.w);
+    }
+    float2 v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      v[k] = zero;
+#pragma unroll
+      for (int x = 0; x < NS; ++x) v[k] = __ffma2_rn(wp[x], y[x][k], v[k]);
+    }
+    int de = e0;
+    if (s_rotf[j]) {
+      float2 M[9];
+      const float4* m4 = reinterpret_cast<const float4*>(s_M2 + 10 * j);
+#pragma unroll
+      for (int h = 0; h < 4; ++h) {
+        const float4 tm = m4[h];
+        M[2 * h] = make_float2(tm.x, tm.y);
+        M[2 * h + 1] = make_float2(tm.z, tm.w);
+      }
+      M[8] = s_M2[10 * j + 8];
+      float2 tr[3];
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        tr[a] = __fmul2_rn(M[3 * a], v[0]);
+        tr[a] = __ffma2_rn(M[3 * a + 1], v[1], tr[a]);
+        tr[a] = __ffma2_rn(M[3 * a + 2], v[2], tr[a]);
+      }
+      if (gamma) {
+        de = s_de[j * na + gi];
+        const float2 ph = *reinterpret_cast<const float2*>(s_ph + 2 * (j * na + gi));
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+          v[a] = make_float2(ph.x * tr[a].x - ph.y * tr[a].y, ph.x * tr[a].y + ph.y * tr[a].x);
+      } else {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) v[a] = tr[a];
+      }
+    }
+    const float4 qc = s_qc[j];
+    const float2 d = make_float2(qc.x * v[0].x + qc.y * v[1].x + qc.z * v[2].x,
+                                 qc.x * v[0].y + qc.y * v[1].y + qc.z * v[2].y);
+    const float2 f = s_sq[j * nsf + de / 3];
+    return make_float2(f.x * d.x - f.y * d.y, f.x * d.y + f.y * d.x);
+  };
+  // two q per round: their reductions interleave (independent shuffle
+  // chains); segments of G lanes hold one mode's atoms of one q, and rounds
+  // with an offset of G or more are skipped (G is the same for every lane)
+  for (int t = 0; t < trips; t += 2) {
+    const int ja = jbase + t * jstep + lslice, jb = ja + jstep;
+    const bool la = active && ja < count, lb = active && t + 1 < trips && jb < count;
+    float2 ca = la ? term(ja) : zero;
+    float2 cb = lb ? term(jb) : zero;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      if (off >= G) continue;
+      const float ax = __shfl_down_sync(0xffffffffu, ca.x, off);
+      const float ay = __shfl_down_sync(0xffffffffu, ca.y, off);
+      const float bx = __shfl_down_sync(0xffffffffu, cb.x, off);
+      const float by = __shfl_down_sync(0xffffffffu, cb.y, off);
+      if (gi + off < G) {
+        ca.x += ax;
+        ca.y += ay;
+        cb.x += bx;
+        cb.y += by;
+      }
+    }
+    if (gi == 0) {
+      if (la) __stcs(out + s_oq[ja] + b0 + mm, ca.x * ca.x + ca.y * ca.y);
+      if (lb) __stcs(out + s_oq[jb] + b0 + mm, cb.x * cb.x + cb.y * cb.y);
+    }
+  }
+}
+
 // single: the one interpolator's parameters (gb.items null); otherwise a
 // batch whose groups carry their item's parameters.  gb.qmax, e_modes,
 // ph_atoms and ybuf give the shared-memory layout in either case.
-template <typename St, bool CPLX, typename Out>
+template <typename St, bool CPLX, typename Out, bool SF = false>
 __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kernel(GatherParams p, GatherBatch gb) {
   using Acc = float;
   constexpr int comps = CPLX ? 2 : 1;
@@ -1084,7 +1204,9 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
       reinterpret_cast<int*>(&s_par[1])[w] = reinterpret_cast<const int*>(&p)[w];
     }
   const int QM = gb.qmax;
-  const WarpLayout L = warp_layout(QM, gb.e_modes, gb.ph_atoms, gb.ybuf, nwarps);
+  const WarpLayout L = warp_layout(QM, gb.e_modes, gb.ph_atoms, gb.ybuf, nwarps, SF ? gb.sf_atoms : 0);
+  float2* s_sq = reinterpret_cast<float2*>(sm + L.sq);
+  float4* s_qc = reinterpret_cast<float4*>(sm + L.qc);
   long long* s_q = reinterpret_cast<long long*>(sm + L.q);
   long long* s_oq = reinterpret_cast<long long*>(sm + L.oq);
   float2* s_w2 = reinterpret_cast<float2*>(sm + L.w);
@@ -1162,7 +1284,7 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
     for (int j = tid; j < count; j += nth) {
       const long long qi = p.order[start + j];
       s_q[j] = qi;
-      s_oq[j] = (qi - p.q_base) * (long long)B * s * comps;
+      s_oq[j] = (qi - p.q_base) * (long long)B * (SF ? 1 : s * comps);
       Acc wsl[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       const int nw = p.nw[qi];
       for (int k = 0; k < nw; ++k) {
@@ -1221,6 +1343,36 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
         sincospif(2.0f * (float)frac, &sn, &cs);
         s_ph[2 * t] = cs;
         s_ph[2 * t + 1] = sn;
+      }
+    }
+    if constexpr (SF) {
+      // c_k e^{2πi Q·x_k} for every (q, atom), and Q·B per q (FP64, then FP32)
+      const int nsf = gb.sf_atoms;
+      for (int t = tid; t < count * nsf; t += nth) {
+        const int j = t / nsf, k = t - j * nsf;
+        const long long qi = p.order[start + j];
+        const double* Qv = p.sf_Q + 3 * qi;
+        const double* A = p.sf_atom + 4 * k;
+        double dq = 0.0;
+        dq = __dadd_rn(dq, __dmul_rn(Qv[0], A[1]));
+        dq = __dadd_rn(dq, __dmul_rn(Qv[1], A[2]));
+        dq = __dadd_rn(dq, __dmul_rn(Qv[2], A[3]));
+        const double frac = dq - rint(dq);
+        float sn, cs;
+        sincospif(2.0f * (float)frac, &sn, &cs);
+        const float ck = (float)A[0];
+        s_sq[t] = make_float2(ck * cs, ck * sn);
+      }
+      for (int j = tid; j < count; j += nth) {
+        const long long qi = p.order[start + j];
+        const double* Qv = p.sf_Q + 3 * qi;
+        double xyz[3];
+        for (int i = 0; i < 3; ++i) {
+          double acc = 0.0;
+          for (int k = 0; k < 3; ++k) acc = __dadd_rn(acc, __dmul_rn(p.sf_B[3 * k + i], Qv[k]));
+          xyz[i] = acc;
+        }
+        s_qc[j] = make_float4((float)xyz[0], (float)xyz[1], (float)xyz[2], 0.f);
       }
     }
     __syncthreads();
@@ -1288,7 +1440,16 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
       const int qs = U >= 32 ? 1 : 32 / U;
       const int lslice = U >= 32 ? 0 : lane / U;
       const int jstep = wq * qs, j0 = wslice * qs + lslice;
-      for (int u = U >= 32 ? lane : lane % U; u < U && lslice < qs; u += 32) {
+      if constexpr (SF) {
+        float* sfo = reinterpret_cast<float*>(p.out);
+        if (nslot == 8)
+          warp_block_sf<8, St>(Yb, so, row_bytes, MBw, mb, G, s_e, pivot, s_w2, s_M2, s_rotf, s_ph, s_de, s_oq,
+                               s_sq, s_qc, gb.sf_atoms, count, wslice, qs, wq, gamma, na, b0, sfo);
+        else
+          warp_block_sf<4, St>(Yb, so, row_bytes, MBw, mb, G, s_e, pivot, s_w2, s_M2, s_rotf, s_ph, s_de, s_oq,
+                               s_sq, s_qc, gb.sf_atoms, count, wslice, qs, wq, gamma, na, b0, sfo);
+      }
+      for (int u = U >= 32 ? lane : lane % U; !SF && u < U && lslice < qs; u += 32) {
         const int mm = u / G, gi = u % G, bb = b0 + mm;
         const int e0 = gi < p.nsc ? gi : p.nsc + 3 * (gi - p.nsc);
         const int ne = gi < p.nsc ? 1 : 3;
@@ -1500,7 +1661,7 @@ int gather_pick_modes(const GatherParams& p, int store_kind, bool cplx, size_t s
 // layout fields and warps; false when the classic kernel must run.  Raises
 // the kernel's shared-memory limit (not capturable: call before a stream
 // capture).
-template <typename St, bool CPLX, typename Out>
+template <typename St, bool CPLX, typename Out, bool SF = false>
 static bool warp_plan(const GatherParams* P, int n, int qmax, size_t budget, GatherBatch* gb, size_t* smem_out,
                       int* per_sm_out) {
   const int comps = CPLX ? 2 : 1;
@@ -1515,10 +1676,15 @@ static bool warp_plan(const GatherParams* P, int n, int qmax, size_t budget, Gat
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  for (int pass = 0; pass < 2; ++pass) {
+  // pass 0: the first shape within the budget; pass 1 (nothing fits the
+  // budget): of the shapes the device holds, the most resident warps per
+  // SM, then the most modes per block
+  int best_w = 0, best_cap = 0, best_res = 0;
+  for (int pass = 0; pass < 3; ++pass) {
     const size_t limit = pass == 0 ? std::min(budget, (size_t)optin) : (size_t)optin;
     for (int warps : {kWarpGatherMaxWarps, kWarpGatherMaxWarps / 2}) {
       for (int cap = mmax; cap >= 1; --cap) {
+        if (pass == 2 && (warps != best_w || cap != best_cap)) continue;
         long long yb = 16;
         for (int i = 0; i < n; ++i) {
           const GatherParams& p = P[i];
@@ -1526,18 +1692,29 @@ static bool warp_plan(const GatherParams* P, int n, int qmax, size_t budget, Gat
           const int m = std::min(std::min(std::max(1, 32 / G), p.B), cap);
           yb = std::max(yb, 8LL * m * ((((long long)p.s * comps * (long long)sizeof(St) + 15) & ~15LL) + 16));
         }
-        const size_t smem = warp_layout(qmax, cap, na, yb, warps).total;
+        const int nsf = SF ? P[0].sf_atoms : 0;
+        const size_t smem = warp_layout(qmax, cap, na, yb, warps, nsf).total;
         if (smem > limit) continue;
-        cudaFuncSetAttribute(warp_gather_kernel<St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(warp_gather_kernel<St, CPLX, Out, SF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         int per_sm = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_gather_kernel<St, CPLX, Out>, warps * 32, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, warp_gather_kernel<St, CPLX, Out, SF>, warps * 32,
+                                                      smem);
         if (per_sm < 1) break;
+        if (pass == 1) {
+          if (per_sm * warps > best_res) {
+            best_res = per_sm * warps;
+            best_w = warps;
+            best_cap = cap;
+          }
+          continue;
+        }
         gb->qmax = qmax;
         gb->e_modes = cap;
         gb->ph_atoms = na;
         gb->ybuf = yb;
         gb->warps = warps;
+        gb->sf_atoms = nsf;
         *smem_out = smem;
         *per_sm_out = per_sm;
         return true;
@@ -1560,6 +1737,26 @@ static bool launch_warp(const GatherParams& p, int num_sms, size_t budget, cudaS
   long long grid = (long long)num_sms * per_sm;
   if (grid > p.n) grid = p.n > 0 ? p.n : 1;
   warp_gather_kernel<St, CPLX, Out><<<(unsigned)grid, gb.warps * 32, smem, s>>>(p, gb);
+  return true;
+}
+
+// The structure-factor gather (FP32 / BF16 complex vector data, no scalars
+// beside the vectors, at most 32 atoms): false when it cannot run.
+template <typename St>
+static bool launch_sf_t(const GatherParams& p, int num_sms, size_t budget, cudaStream_t s) {
+  if (p.nsc != 0 || p.nmat != 0 || p.nvec < 1 || p.nvec > 32 || p.nvec != p.sf_atoms) return false;
+  GatherBatch gb{};
+  size_t smem = 0;
+  int per_sm = 0;
+  // the most resident warps (its records are larger than the vectors gather's)
+  (void)budget;
+  if (!warp_plan<St, true, float, true>(&p, 1, p.qmax, 0, &gb, &smem, &per_sm)) return false;
+  gb.groups = p.groups;
+  gb.n_groups = p.n_groups;
+  gb.counter = p.counter;
+  long long grid = (long long)num_sms * per_sm;
+  if (grid > p.n) grid = p.n > 0 ? p.n : 1;
+  warp_gather_kernel<St, true, float, true><<<(unsigned)grid, gb.warps * 32, smem, s>>>(p, gb);
   return true;
 }
 
@@ -1659,6 +1856,15 @@ cudaError_t preload_query_kernels() {
   if ((e = preload_store<float, __nv_bfloat16>()) != cudaSuccess) return e;
   if ((e = preload_grouping_kernels()) != cudaSuccess) return e;
   return preload_locate_kernel();
+}
+
+int launch_structure_factor(const GatherParams& p, int store_kind, int num_sms, size_t budget, cudaStream_t s) {
+  if (p.n <= 0) return 0;
+  if (store_kind == ST_F64) return -1;
+  cudaMemsetAsync(p.counter, 0, sizeof(int32_t), s);
+  const bool ok = store_kind == ST_F32 ? launch_sf_t<float>(p, num_sms, budget, s)
+                                       : launch_sf_t<__nv_bfloat16>(p, num_sms, budget, s);
+  return ok ? 1 : -1;
 }
 
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms, size_t budget,

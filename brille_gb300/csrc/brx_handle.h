@@ -111,6 +111,10 @@ struct brx_handle {
   DevBuf mlp_w, mlp_b, mlp_x;  // bf16 weights, biases, one sub-chunk of feature rows
   bool mlp_tc = false;         // dense layers on tcgen05 (else mma.sync)
   DevBuf mlp_wt, mlp_bt;       // the tcgen05 kernel's weights (core-matrix order) and padded biases
+  // structure factor (brx_set_atoms): c_k and fractional x_k per atom, and
+  // the reciprocal basis rows, on the device
+  int sf_n = 0;
+  DevBuf sf_atoms, sf_B;
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;

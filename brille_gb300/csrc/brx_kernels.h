@@ -73,6 +73,13 @@ struct GatherParams {
   // group keys are batch-wide, the trellis's own by key − key_base
   long long q_base;
   int key_base;
+  // structure factor instead of the vectors (sf_atoms > 0, FP32 warp gather
+  // only): per q and mode |Σ_k c_k e^{2πi Q·x_k} (Q_c·e_k)|² into out
+  // (float, n × B), Q_c = Q·B
+  int sf_atoms;
+  const double* sf_Q;     // the caller's Q (r.l.u.), chunk-local, n × 3
+  const double* sf_atom;  // sf_atoms × 4: c_k, then x_k (fractional)
+  const double* sf_B;     // 9: rows of the reciprocal basis (Å⁻¹)
 };
 
 // One persistent gather launch over the groups of many interpolators that
@@ -92,6 +99,7 @@ struct GatherBatch {
   long long ybuf;
   int warps;  // 0: the classic CTA-synchronous kernel; else the warp-independent one with this many warps
   int reverse;  // descriptor g at groups[-1 - g] (a list written downwards from its end)
+  int sf_atoms;  // structure-factor atoms (single interpolator only; 0: vectors)
 };
 
 // Second descriptor list of a batch's grouping: keys of class-1 items
@@ -124,6 +132,9 @@ int launch_grouping(const int32_t* key, long long n, long long n_keys, int qmax,
 size_t group_scratch_ints(long long n_keys);
 
 // Gather + rotate for one interpolator.  Returns the number of launches.
+// The vectors gather in structure-factor form (p.sf_atoms > 0, FP32 / BF16
+// storage): 1 on launch, -1 when the data do not fit it.
+int launch_structure_factor(const GatherParams& p, int store_kind, int num_sms, size_t budget, cudaStream_t s);
 int launch_gather(const GatherParams& p, int store_kind, bool cplx, bool out_f32, int num_sms,
                   size_t smem_budget, cudaStream_t s);
 size_t gather_smem_bytes(const GatherParams& p, int store_kind, bool cplx, int MB);

@@ -274,6 +274,45 @@ class _Grid:
         """(wrap/_common_grid.hpp:412-440; src/bz_trellis.hpp:113-129)"""
         return self._query(False, Q, do_not_move_points, out_f32)
 
+    def set_atoms(self, weights, positions):
+        """Atoms of the structure factor: weights c_k = b_k/sqrt(m_k) and
+        fractional positions x_k (n × 3) in the lattice of the query's r.l.u."""
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(-1)
+        x = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        if len(w) != len(x):
+            raise ValueError("one weight per atom position is needed")
+        self._atoms = (w, x)  # keeps the arrays alive for the call
+        a = _abi.Atoms(len(w), w.ctypes.data_as(C.POINTER(C.c_double)), x.ctypes.data_as(C.POINTER(C.c_double)))
+        h = self._handle()
+        check(load().brx_set_atoms(h, C.byref(a)), h)
+
+    def ir_structure_factor(self, Q, *, out_f32=True):
+        """(values, S) at Q: the interpolated values and, per q and mode, the
+        coherent one-phonon structure factor |Σ_k c_k e^{2πi Q·x_k} (Q_c·e_k)|²
+        of the interpolated eigenvectors (float32, n × B), without writing the
+        eigenvectors out.  set_atoms first."""
+        if self._fill is None:
+            raise RuntimeError("The interpolation data must be filled before interpolating.")
+        Q = np.ascontiguousarray(np.asarray(Q, dtype=np.float64))
+        if Q.ndim != 2 or Q.shape[1] != 3:
+            raise RuntimeError("Only (n,3) two-dimensional Q vectors supported in interpolating.")
+        n = Q.shape[0]
+        f = self._fill
+        vdt = np.complex64 if (out_f32 and f["vdtype"] == np.complex128) else (np.float32 if out_f32 else f["vdtype"])
+        vals = np.empty((n,) + tuple(f["vshape"]), dtype=vdt)
+        sf = np.empty((n, f["cshape"][0]), dtype=np.float32)
+        flags = _abi.BRX_FLAG_OUT_F32 if out_f32 else 0
+        h = self._handle()
+        check(load().brx_ir_structure_factor(h, Q.ctypes.data, n, vals.ctypes.data, sf.ctypes.data, flags, None), h)
+        return vals, sf
+
+    def structure_factor_into(self, Q, n, values_out, sf_out, *, out_f32=True, async_=False, stream=None):
+        """ir_structure_factor on caller-owned buffers (host or device)."""
+        flags = (_abi.BRX_FLAG_OUT_F32 if out_f32 else 0) | (_abi.BRX_FLAG_ASYNC if async_ else 0)
+        addr = lambda o: o if isinstance(o, int) else _ptr(o)  # noqa: E731
+        h = self._handle()
+        check(load().brx_ir_structure_factor(h, addr(Q), int(n), addr(values_out), addr(sf_out), flags, stream), h)
+
     def query_into(self, Q, n, values_out, vectors_out, *, ir=True, out_f32=False, no_move=False,
                    async_=False, stream=None):
         """Raw query on caller-owned buffers (numpy arrays, torch tensors or

@@ -179,6 +179,25 @@ brx_status brx_ir_interpolate_at(brx_handle* h, const double* Q, int64_t n,
                                  void* values_out, void* vectors_out,
                                  uint32_t flags, void* stream);
 
+/* Coherent one-phonon structure factor of the interpolated modes (no
+ * counterpart in the reference; the consumer that brille feeds): per q and
+ * mode j, S_j = |Σ_k c_k e^{2πi Q·x_k} (Q_c · e_jk)|², with Q_c = Q·B in Å⁻¹
+ * (B: rows of the reciprocal basis), e_jk the Γ-rotated Cartesian
+ * eigenvector of atom k as brx_ir_interpolate_at returns it, c_k = b_k/√m_k
+ * and x_k (fractional, in the lattice of Q's r.l.u.) from brx_set_atoms.
+ * The eigenvectors are never written out: values_out as for
+ * brx_ir_interpolate_at, sf_out n × B float32.  Needs FP32 or BF16 storage
+ * of complex eigenvectors of 1-32 atoms (no other elements) with
+ * LengthUnit Å and RotatesLike Γ. */
+typedef struct {
+  int32_t n_atoms;
+  const double* weight;    /* n_atoms: b_k / sqrt(m_k) */
+  const double* position;  /* n_atoms × 3, fractional */
+} brx_atoms;
+brx_status brx_set_atoms(brx_handle* h, const brx_atoms* atoms);
+brx_status brx_ir_structure_factor(brx_handle* h, const double* Q, int64_t n, void* values_out, float* sf_out,
+                                   uint32_t flags, void* stream);
+
 /* interpolate_at: first-zone move and interpolation, no rotation
  * (src/bz_trellis.hpp:113-129; wrap/_common_grid.hpp:412-440). */
 brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n,
