@@ -210,6 +210,21 @@ __device__ __forceinline__ bool wedge_candidate(const DevGeom& g, const float* m
   return all_ge || (g.wedge_le_ge && all_le);
 }
 
+// Is W_jᵀ q certainly inside the wedge?  True only when every normal puts
+// it strictly on the inner side (or, for a mirrored wedge, every normal on
+// the outer side) by more than the FP32 error margin: the exact dot products
+// are then of that sign, and the exact test would accept.
+__device__ __forceinline__ bool wedge_sure(const DevGeom& g, const float* m, float x0, float x1, float x2,
+                                           float margin) {
+  bool all_ge = true, all_le = true;
+  for (int i = 0; i < g.n_wedge; ++i) {
+    const float d = m[3 * i] * x0 + m[3 * i + 1] * x1 + m[3 * i + 2] * x2;
+    if (!(d > margin)) all_ge = false;
+    if (!(d < -margin)) all_le = false;
+  }
+  return all_ge || (g.wedge_le_ge && all_le);
+}
+
 __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32_t rot[2]) {
   double x[3], qj[3];
   hkl_to_xyz(x, g.outer_B, q);
@@ -217,13 +232,20 @@ __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32
     // FP32 screen of every operation first (the same work in every lane),
     // then exact tests of the survivors in the reference's order; each lane
     // walks its own candidate mask, so the exact tests run converged
+    // an operation certainly inside needs no exact test either: the first
+    // candidate in order that is certainly inside is the exact answer
     const float x0 = (float)x[0], x1 = (float)x[1], x2 = (float)x[2];
-    const float tol = screen_margin(fabsf(x0) + fabsf(x1) + fabsf(x2), 0.f) + g.wedge_band32;
-    const bool id_cand = wedge_candidate(g, z.wm + 3 * g.n_wedge * g.n_ops, x0, x1, x2, tol);
-    unsigned long long mask = 0ull;
+    const float margin = screen_margin(fabsf(x0) + fabsf(x1) + fabsf(x2), 0.f);
+    const float tol = margin + g.wedge_band32;
+    const float* wid = z.wm + 3 * g.n_wedge * g.n_ops;
+    const bool id_cand = wedge_candidate(g, wid, x0, x1, x2, tol);
+    unsigned long long mask = 0ull, sure = 0ull;
     for (int j = 0; j < g.n_ops; ++j)
-      if (wedge_candidate(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, tol)) mask |= 1ull << j;
-    if (id_cand && inside_wedge(g, z, x)) {
+      if (wedge_candidate(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, tol)) {
+        mask |= 1ull << j;
+        if (wedge_sure(g, z.wm + 3 * g.n_wedge * j, x0, x1, x2, margin)) sure |= 1ull << j;
+      }
+    if (id_cand && (wedge_sure(g, wid, x0, x1, x2, margin) || inside_wedge(g, z, x))) {
       rot[0] = rot[1] = g.identity;
       return 0;
     }
@@ -233,9 +255,13 @@ __device__ int wedge_one(const DevGeom& g, const SmemZone& z, double q[3], int32
       const int32_t* W = z.ops + 9 * j;
       int32_t Wt[9] = {W[0], W[3], W[6], W[1], W[4], W[7], W[2], W[5], W[8]};
       matvec_i(qj, Wt, q);
-      double xj[3];
-      hkl_to_xyz(xj, g.outer_B, qj);
-      if (inside_wedge(g, z, xj)) {
+      bool in = (sure >> j) & 1ull;
+      if (!in) {
+        double xj[3];
+        hkl_to_xyz(xj, g.outer_B, qj);
+        in = inside_wedge(g, z, xj);
+      }
+      if (in) {
         q[0] = qj[0]; q[1] = qj[1]; q[2] = qj[2];
         rot[1] = j;
         rot[0] = z.opinv[j];
