@@ -16,8 +16,8 @@ Reported (one JSON line from rank 0):
   cpu_baseline  the CPU oracle (a restatement of the reference's OpenMP
              path) on a bounded sample, on this host's cores
 
-`--impl reference` times that CPU implementation alone (the reference itself
-cannot be built here).
+`--impl reference` times that CPU implementation alone (the reference's own
+build needs HDF5 and generated headers that this toolchain lacks).
 """
 from __future__ import annotations
 
