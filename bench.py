@@ -515,6 +515,71 @@ def run_sqw(args):
     print(json.dumps(out), flush=True)
 
 
+def run_sort(args):
+    """sort() on the headline workload: the mode permutation of every vertex
+    pair that shares a node (brx_sort, FP64 costs on FP64 storage, exact
+    assignment), against the CPU oracle of the same computation on a bounded
+    sample of pairs on this host's cores."""
+    import torch
+
+    from brille_gb300 import BZTrellisQdc
+    from oracle import oracle as O
+
+    wl = build_workload(args.workload)
+    B, na = wl["w"].shape[1], wl["v"].shape[2]
+    grid = BZTrellisQdc(wl["bz"], trellis=wl["tr"])
+    grid.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage="f64")
+    t = time.time()
+    keys = grid.permutation_keys()
+    log(f"[setup] {keys.size} permutation keys in {time.time() - t:.1f}s")
+    pairs = keys.size // 2
+    stream = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dev_ms, wall_ms = [], []
+    for rep in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        e0.record(stream)
+        grid.sort(stream=stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if rep >= args.warmup:
+            wall_ms.append((time.perf_counter() - t) * 1e3)
+            dev_ms.append(e0.elapsed_time(e1))
+    k, perms = grid.permutation_table()
+    moved = int((perms != np.arange(B)).any(axis=1).sum())
+    ms = float(np.median(dev_ms))
+    # FP64 flops of the Hermitian products alone: B² pairs × s elements × 8
+    span = 3 * na
+    flops = pairs * B * B * span * 8.0
+    # CPU oracle on a bounded sample of pairs (both directions of each)
+    nv = len(wl["tr"].vertices)
+    i, j = keys // nv, keys % nv
+    fwd = np.nonzero(i < j)[0]
+    rng = np.random.default_rng(0)
+    take = np.sort(rng.choice(fwd, size=min(len(fwd), 4000), replace=False))
+    sample = np.unique(np.concatenate([keys[take], j[take] * nv + i[take]]))
+    vals = (np.ascontiguousarray(wl["w"][:, :, None]), (1, 0, 0), 0, (1, 1, 1))
+    vecs = (np.ascontiguousarray(wl["v"].reshape(nv, B, -1)), (0, span, 0), 0, (1, 1, 1))
+    threads = os.cpu_count() or 1
+    t = time.perf_counter()
+    ref = O.sort_permutations(vals, vecs, sample, threads=threads)
+    cpu_s = time.perf_counter() - t
+    pos = np.searchsorted(k, sample)
+    agree = float((perms[pos] == ref).all(axis=1).mean())
+    out = dict(mode="sort", metric="vertex pairs sorted per second", value=pairs / (ms / 1e3), unit="pairs/s",
+               ms_per_sort=ms, wall_ms_per_sort=float(np.median(wall_ms)), steps=args.steps, warmup=args.warmup,
+               pairs=int(pairs), keys=int(keys.size), non_identity_keys=moved,
+               fp64_hermitian_gflops=flops / (ms / 1e3) / 1e9,
+               cpu_baseline=dict(value=len(take) / cpu_s, unit="pairs/s", cores=threads, kind="port",
+                                 sample=f"{len(take)} random pairs of the same trellis (both keys each)"),
+               oracle_agreement=agree,
+               config=dict(workload=args.workload, modes=B, atoms=na, vertices=nv, storage="f64",
+                           costs="|Δω| + sin² of the Hermitian angle (the reference's defaults)"),
+               data="synthetic (seeded BvK model)")
+    print(json.dumps(out), flush=True)
+
+
 def run_learned(args):
     """Learned residual on coarse trellises of the 2-atom FCC crystal
     (a = 4.96 Å, 28 amu, BZ/5000 for the fine trellis) against the plain
@@ -641,7 +706,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="keep the default gather shared-memory budgets")
     ap.add_argument("--tuning", default=None,
                     help="apply gather tuning values (5 integers, as config.tuning lists them) instead of tuning")
-    ap.add_argument("--mode", default="throughput", choices=["throughput", "precision", "learned", "batch", "sqw"],
+    ap.add_argument("--mode", default="throughput",
+                    choices=["throughput", "precision", "learned", "batch", "sqw", "sort"],
                     help="precision: FP32 and BF16 storage against the FP64 path; learned: the learned residual "
                          "on coarse trellises against the plain fine trellis")
     ap.add_argument("--train-q", type=int, default=0, help="learned mode: training samples (default 1e6)")
@@ -665,6 +731,8 @@ def main():
         return run_batch(args)
     if args.mode == "sqw":
         return run_sqw(args)
+    if args.mode == "sort":
+        return run_sort(args)
 
     import torch
 

@@ -63,6 +63,10 @@ class MlpDims(C.Structure):
 BRX_MLP_FP32 = 0x1
 
 
+class SortCost(C.Structure):
+    _fields_ = [("scalar_fn", C.c_int32), ("vector_fn", C.c_int32), ("weight", C.c_double * 3)]
+
+
 class Atoms(C.Structure):
     _fields_ = [("n_atoms", C.c_int32), ("weight", C.POINTER(C.c_double)), ("position", C.POINTER(C.c_double))]
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import Atoms, Data, Geometry, LocateOut, MlpDims
+from ._abi import Atoms, Data, Geometry, LocateOut, MlpDims, SortCost
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbrx.so")
@@ -43,6 +43,12 @@ def load(build_if_missing=True):
     lib.brx_fill.restype = C.c_int
     lib.brx_set_permutations.argtypes = [h, C.c_int64, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]
     lib.brx_set_permutations.restype = C.c_int
+    lib.brx_sort.argtypes = [h, C.c_int64, C.c_void_p, C.POINTER(SortCost), C.POINTER(SortCost), C.c_void_p]
+    lib.brx_sort.restype = C.c_int
+    lib.brx_get_permutations.argtypes = [h, C.c_int64, C.c_void_p, C.c_void_p]
+    lib.brx_get_permutations.restype = C.c_int
+    lib.brx_permutation_count.argtypes = [h]
+    lib.brx_permutation_count.restype = C.c_int64
     for name in ("brx_ir_interpolate_at", "brx_interpolate_at"):
         f = getattr(lib, name)
         f.argtypes = [h, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]

@@ -81,6 +81,13 @@ def _elements(arr, el):
     return B, e, rot, lu
 
 
+def _cost_fns(el):
+    """(scalar, vector) cost-function codes of an elements vector: entries 5
+    and 6, default 0 (wrap/_interpolator.hpp:95-98)."""
+    el = np.asarray(el).astype(np.int64).ravel()
+    return (int(el[5]) if el.size > 5 else 0, int(el[6]) if el.size > 6 else 0)
+
+
 def _is_device(x):
     return hasattr(x, "data_ptr") and bool(getattr(x, "is_cuda", False))
 
@@ -189,7 +196,7 @@ class _Grid:
             pass
 
     # ----------------------------------------------------------------- fill
-    def fill(self, values, values_elements, *args, storage="f64"):
+    def fill(self, values, values_elements, *args, sort=None, storage="f64"):
         """fill(values, values_elements[, values_weights], vectors,
         vectors_elements[, vectors_weights][, sort])
         (wrap/_common_grid.hpp:26-47, 127-147)."""
@@ -205,10 +212,9 @@ class _Grid:
             rest = ()
         else:
             raise TypeError("fill() takes values and vectors with their element specifications")
-        sort = bool(rest[0]) if rest else False
-        if sort:
-            raise NotImplementedError("mode sorting on fill is not implemented; supply a permutation table "
-                                      "with set_permutations()")
+        if sort is not None and rest:
+            raise TypeError("fill() got multiple values for argument 'sort'")
+        sort = bool(rest[0]) if rest else bool(sort)
         vdt = np.complex128 if self.VALUE_COMPLEX else np.float64
         cdt = np.complex128 if self.VECTOR_COMPLEX else np.float64
         vals = _as_data(values, vdt)
@@ -234,8 +240,78 @@ class _Grid:
         self._fill = dict(values=vals, vectors=vecs,
                           vshape=tuple(vals.shape[1:]), cshape=None if vecs is None else tuple(vecs.shape[1:]),
                           vdtype=vdt, cdtype=cdt, values_weights=values_weights, vectors_weights=vectors_weights,
-                          storage=storage)
+                          storage=storage, B=Bv, values_fns=_cost_fns(values_elements),
+                          vectors_fns=None if vecs is None else _cost_fns(vectors_elements))
+        if sort:
+            self.sort()
         return True
+
+    def set_flags_weights(self, values_flags, values_weights, vectors_flags, vectors_weights, sort=False):
+        """Cost functions and relative cost weights of the values and vectors
+        (wrap/_common_grid.hpp:481-560; flags [RotatesLike, LengthUnit,
+        scalar cost function, vector cost function], decoded as set_check,
+        wrap/_interpolator.cpp:43-81), then sort() when asked."""
+        if self._fill is None:
+            raise RuntimeError("The interpolation data must be filled before setting cost information.")
+        f = self._fill
+        for name, flags, weights in (("values", values_flags, values_weights), ("vectors", vectors_flags,
+                                                                                 vectors_weights)):
+            fl = np.asarray(flags).astype(np.int64).ravel()
+            if fl.size > 0 and int(fl[0]) not in (0, 1, 2):
+                raise RuntimeError(f"Unknown RotatesLike value {int(fl[0])}")
+            if fl.size > 1 and int(fl[1]) not in (0, 1, 2, 3, 4):
+                raise RuntimeError(f"Unknown LengthUnit value {int(fl[1])}")
+            fns = (int(fl[2]) if fl.size > 2 else 0, int(fl[3]) if fl.size > 3 else 0)
+            w = [1.0, 1.0, 1.0]
+            for i, x in enumerate(np.asarray(weights, dtype=np.float64).ravel()[:3]):
+                w[i] = float(x)
+            if name == "values" or f["vectors"] is not None:
+                f[name + "_fns"] = fns
+                f[name + "_weights"] = tuple(w)
+        if sort:
+            self.sort()
+
+    def permutation_keys(self):
+        """The vertex pairs sort() visits (keys i*n_vertices+j, sorted)."""
+        if getattr(self, "_perm_keys", None) is None:
+            self._perm_keys = self.trellis.permutation_keys()
+        return self._perm_keys
+
+    def sort(self, *, stream=None):
+        """Find the mode permutation between every pair of vertices that share
+        a node, on the GPU (DualInterpolator::sort,
+        src/interpolatordual.hpp:398-434), and use it in every later query."""
+        if self._fill is None:
+            raise RuntimeError("The interpolation data must be filled before sorting.")
+        f = self._fill
+        keys = self.permutation_keys()
+
+        def cost(fns, weights):
+            c = _abi.SortCost()
+            c.scalar_fn, c.vector_fn = int(fns[0]), int(fns[1])
+            w = [1.0, 1.0, 1.0]
+            for i, x in enumerate(np.asarray(weights, dtype=np.float64).ravel()[:3]):
+                w[i] = float(x)
+            c.weight[:] = w
+            return c
+
+        vc = cost(f["values_fns"], f["values_weights"])
+        cc = cost(f["vectors_fns"], f["vectors_weights"]) if f["vectors"] is not None else None
+        h = self._handle()
+        check(load().brx_sort(h, keys.size, keys.ctypes.data, C.byref(vc), C.byref(cc) if cc is not None else None,
+                              stream), h)
+
+    def permutation_table(self):
+        """(keys, perms): every key i*n_vertices+j the handle holds and its
+        permutation of the modes (perms[k][b] is the mode of vertex j that
+        mode b of vertex i pairs with; identity where none is set)."""
+        h = self._handle()
+        n = int(load().brx_permutation_count(h))
+        B = int(self._fill["B"]) if self._fill is not None else 0
+        keys = np.zeros(n, np.int64)
+        perms = np.zeros((n, B), np.int32)
+        check(load().brx_get_permutations(h, n, keys.ctypes.data, perms.ctypes.data), h)
+        return keys, perms
 
     def set_permutations(self, keys, perm_ids, perms):
         """Mode permutations per vertex pair (keys i*n_vertices+j, sorted)."""

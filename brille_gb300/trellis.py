@@ -308,6 +308,27 @@ class TrellisBuild:
         t.save(path, fingerprint=fp)
         return t
 
+    def permutation_keys(self):
+        """Keys i*n_vertices+j of every ordered pair of distinct vertices that
+        share a cube node or one tetrahedron of a poly node, sorted: the pairs
+        whose mode permutations sort() determines (PolyTrellis::collect_keys
+        and collect_keys_node, src/trellis_poly_parallel.tpp:485-526;
+        permutation_table_keys_from_indicies, src/permutation_table.hpp:284-292)."""
+        n = np.int64(len(self.vertices))
+        keys = []
+        for groups in (self.cube_vertices, self.tet_vertices):
+            g = np.asarray(groups, np.int64)
+            if g.size == 0:
+                continue
+            m = g.shape[1]
+            a, b = np.nonzero(~np.eye(m, dtype=bool))
+            i, j = g[:, a].ravel(), g[:, b].ravel()
+            keep = i != j
+            keys.append(i[keep] * n + j[keep])
+        if not keys:
+            return np.zeros(0, np.int64)
+        return np.unique(np.concatenate(keys))
+
     def summary(self):
         return dict(vertices=len(self.vertices), cube=int(np.sum(self.node_type == NODE_CUBE)),
                     poly=int(np.sum(self.node_type == NODE_POLY)), tets=len(self.tet_vertices),

@@ -171,6 +171,37 @@ brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vecto
 brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* keys,
                                 const int32_t* perm_ids, int32_t n_perms, const int32_t* perms);
 
+/* sort(): find the mode permutation of every listed vertex pair on the GPU
+ * and keep it as the handle's permutation table, replacing
+ * DualInterpolator::sort (src/interpolatordual.hpp:398-434) with the cost
+ * matrix of cost_matrix/add_cost (:385-396, src/interpolator_cost.tpp:19-61)
+ * and an exact assignment where the reference runs LAPJV (:420-434).
+ * keys: i*n_vertices+j, strictly increasing, i != j, and j*n_vertices+i
+ * listed for every i*n_vertices+j (the reference's permutation keys: every
+ * ordered pair of distinct vertices of a cube node or of one tetrahedron,
+ * src/trellis_poly_parallel.tpp:485-526).  values_cost / vectors_cost may be
+ * NULL for the defaults (functions 0, weights 1).  Costs are FP64 on the
+ * stored data (FP32/BF16 storage: on the rounded data).  One vertex pair's
+ * rows and cost matrix must fit one CTA's shared memory (about 40·B² bytes
+ * for complex FP64 eigenvectors of B modes: B ≤ 76; FP32 storage: B ≤ 96).
+ * Synchronous on stream (NULL: the handle's stream). */
+typedef struct brx_sort_cost {
+  int32_t scalar_fn;  /* fill's elements[5]: 0, Σ|a−b| (the reference's only scalar cost) */
+  int32_t vector_fn;  /* fill's elements[6]: 1 |a−b|, 2 1−|a*·b|², 3 Euclidean angle,
+                         4 Hermitian angle, any other: sin² of the Hermitian angle
+                         (src/interpolator.hpp:246-300) */
+  double weight[3];   /* relative cost of scalar, vector and matrix elements (fill's weights) */
+} brx_sort_cost;
+brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* keys, const brx_sort_cost* values_cost,
+                    const brx_sort_cost* vectors_cost, void* stream);
+/* The permutation table as PermutationTable::safe_get reads it
+ * (src/permutation_table.hpp:193-198): the handle's n_keys keys and, per key,
+ * the permutation of n_branches modes (identity where none is set).
+ * n_keys must equal the handle's count (0 after brx_fill). */
+brx_status brx_get_permutations(brx_handle* h, int64_t n_keys, int64_t* keys_out, int32_t* perms_out);
+/* Number of permutation keys the handle holds. */
+int64_t brx_permutation_count(const brx_handle* h);
+
 /* ir_interpolate_at (src/bz_trellis.hpp:155-196; wrap/_common_grid.hpp:276-300).
  * Q: n × 3 float64 in conventional r.l.u.; values_out: n × B_v × span_v and
  * vectors_out: n × B_c × span_c in the input dtype (or float32/complex64 with

@@ -765,3 +765,281 @@ int orc_max_threads(void) {
   return 1;
 #endif
 }
+
+/* ---------------------------------------------------------------------------
+ * sort(): mode permutations of connected vertex pairs
+ * (DualInterpolator::sort / determine_permutation_ij / cost_matrix,
+ * src/interpolatordual.hpp:385-434; Interpolator::add_cost,
+ * src/interpolator_cost.tpp:19-61; set_cost_info, src/interpolator.hpp:246-300;
+ * utilities.tpp:249-431 for the cost functions, :567-598 for the antiphase).
+ *
+ * The cost arithmetic is the reference's, operation by operation: the phase
+ * of y is aligned to x with polar(1, −atan2(Im, Re)) of the Hermitian
+ * product over the whole branch, and every cost function runs on the phased
+ * copy.  One departure: for REAL vectors the reference leaves the phased
+ * copy uninitialised (inplace_antiphase is a no-op for real types,
+ * utilities.tpp:530), so its costs read garbage; here y is used unchanged.
+ *
+ * The assignment is solved exactly by shortest augmenting paths with row and
+ * column potentials (the Hungarian method in the form of Jonker and
+ * Volgenant's augmentation step), where the reference runs LAPJV
+ * (src/lapjv.hpp).  Both return an optimal assignment; they agree wherever
+ * the optimum is unique.  The scan order and the tie rule (the lowest column
+ * among equal reduced costs) are the ones the GPU kernel uses, so for equal
+ * cost matrices the two give the same assignment.
+ * ------------------------------------------------------------------------- */
+typedef struct orc_sort_side {
+  const void* data;   /* n_vertices × B × s doubles (complex: pairs) */
+  int32_t cplx;
+  int32_t s, e0, e1, e2;
+  int32_t vf;         /* vector cost function (reference numbering) */
+  int32_t phase;      /* align phases first (vectors of a DualInterpolator) */
+  double w[3];
+} orc_sort_side;
+
+static double clamp_cos(double c, int* bad) {
+  tol_t one = tols(0.0, 1);
+  double act = fabs(c);
+  if (approx(act, 1.0, one) && act > 1.0) {
+    c /= act;
+    act = fabs(c);
+  }
+  if (act > 1.0) *bad = 1;
+  return c;
+}
+
+static double cos_ratio(double num, double nA, double nB, int* bad) {
+  double c;
+  if (nA != 0.0 && nB != 0.0) c = num / (nA * nB);
+  else c = (nA != 0.0 || nB != 0.0) ? 0.0 : 1.0;
+  return clamp_cos(c, bad);
+}
+
+/* vector cost of n complex elements (utilities.tpp:280-431) */
+static double vec_cost_c(int vf, int n, const double* a, const double* b, int* bad) {
+  if (vf == 1) { /* vector_distance */
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) {
+      double dr = a[2 * i] - b[2 * i], di = a[2 * i + 1] - b[2 * i + 1];
+      s += dr * dr + di * di;
+    }
+    return sqrt(s);
+  }
+  if (vf == 3) { /* euclidean_angle */
+    double AB = 0.0, nA = 0.0, nB = 0.0;
+    for (int i = 0; i < n; ++i) {
+      AB += a[2 * i] * b[2 * i] + a[2 * i + 1] * b[2 * i + 1];
+      nA += a[2 * i] * a[2 * i] + a[2 * i + 1] * a[2 * i + 1];
+      nB += b[2 * i] * b[2 * i] + b[2 * i + 1] * b[2 * i + 1];
+    }
+    return acos(cos_ratio(AB, sqrt(nA), sqrt(nB), bad));
+  }
+  /* hermitian_product(a, b), (a, a), (b, b) */
+  double hr = 0.0, hi = 0.0, aa = 0.0, bb = 0.0;
+  for (int i = 0; i < n; ++i) {
+    hr += a[2 * i] * b[2 * i] + a[2 * i + 1] * b[2 * i + 1];
+    hi += a[2 * i] * b[2 * i + 1] - a[2 * i + 1] * b[2 * i];
+    aa += a[2 * i] * a[2 * i] + a[2 * i + 1] * a[2 * i + 1];
+    bb += b[2 * i] * b[2 * i] + b[2 * i + 1] * b[2 * i + 1];
+  }
+  double vp = hr * hr + hi * hi; /* vector_product */
+  if (vf == 2) return 1.0 - vp;
+  double th = acos(cos_ratio(sqrt(vp), sqrt(aa), sqrt(bb), bad)); /* hermitian_angle */
+  if (vf == 4) return th;
+  double s = sin(th);
+  return s * s;
+}
+
+/* vector cost of n real elements (utilities.tpp:249-278, 383-405) */
+static double vec_cost_r(int vf, int n, const double* a, const double* b, int* bad) {
+  if (vf == 1) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) {
+      double d = a[i] - b[i];
+      s += d * d;
+    }
+    return sqrt(s);
+  }
+  if (vf == 2) {
+    double h = 0.0;
+    for (int i = 0; i < n; ++i) h += a[i] * b[i];
+    return 1.0 - h;
+  }
+  double AA = 0.0, BB = 0.0, AB = 0.0;
+  for (int i = 0; i < n; ++i) {
+    AA += a[i] * a[i];
+    BB += b[i] * b[i];
+    AB += a[i] * b[i];
+  }
+  double th = acos(cos_ratio(AB, sqrt(AA), sqrt(BB), bad)); /* vector_angle */
+  if (vf == 3 || vf == 4) return th;
+  double s = sin(th);
+  return s * s;
+}
+
+/* add_cost for one (row x of vertex i, row y of vertex j); ph: scratch of s complex */
+static double side_cost(const orc_sort_side* S, const double* x, const double* y, double* ph, int* bad) {
+  const int e0 = S->e0, e1 = S->e1, e2 = S->e2, s = S->s;
+  double sc = 0.0, vc = 0.0, mc = 0.0;
+  if (S->cplx) {
+    const double* yy = y;
+    if (S->phase) { /* inplace_antiphase */
+      double rd = 0.0, id = 0.0;
+      for (int k = 0; k < s; ++k) {
+        rd += x[2 * k] * y[2 * k] + x[2 * k + 1] * y[2 * k + 1];
+        id += x[2 * k] * y[2 * k + 1] - x[2 * k + 1] * y[2 * k];
+      }
+      double t = -1.0 * atan2(id, rd);
+      double er = cos(t), ei = sin(t);
+      for (int k = 0; k < s; ++k) {
+        ph[2 * k] = er * y[2 * k] - ei * y[2 * k + 1];
+        ph[2 * k + 1] = er * y[2 * k + 1] + ei * y[2 * k];
+      }
+      yy = ph;
+    }
+    for (int k = 0; k < e0; ++k) {
+      double dr = x[2 * k] - yy[2 * k], di = x[2 * k + 1] - yy[2 * k + 1];
+      sc += sqrt(dr * dr + di * di);
+    }
+    if (e1) vc = vec_cost_c(S->vf, e1, x + 2 * e0, yy + 2 * e0, bad);
+    for (int m = 0; m < e2 / 9; ++m) mc += vec_cost_c(1, 9, x + 2 * (e0 + e1 + 9 * m), yy + 2 * (e0 + e1 + 9 * m), bad);
+  } else {
+    for (int k = 0; k < e0; ++k) sc += fabs(x[k] - y[k]);
+    if (e1) vc = vec_cost_r(S->vf, e1, x + e0, y + e0, bad);
+    for (int m = 0; m < e2 / 9; ++m) mc += vec_cost_r(1, 9, x + e0 + e1 + 9 * m, y + e0 + e1 + 9 * m, bad);
+  }
+  return S->w[0] * sc + S->w[1] * vc + S->w[2] * mc;
+}
+
+/* cost_matrix(i, j): rows the modes of i, columns the modes of j */
+static int cost_matrix(const orc_sort_side* sides, int n_sides, int B, int64_t i, int64_t j, double* C, double* ph) {
+  int bad = 0;
+  for (int q = 0; q < B * B; ++q) C[q] = 0.0;
+  for (int sd = 0; sd < n_sides; ++sd) {
+    const orc_sort_side* S = sides + sd;
+    const int row = S->s * (S->cplx ? 2 : 1);
+    const double* d = (const double*)S->data;
+    for (int a = 0; a < B; ++a)
+      for (int b = 0; b < B; ++b)
+        C[a * B + b] += side_cost(S, d + ((size_t)i * B + a) * row, d + ((size_t)j * B + b) * row, ph, &bad);
+  }
+  return bad;
+}
+
+/* Exact assignment of the n×n matrix C: p[j] (1-based, j = 1..n) is the row
+ * matched to column j.  Returns 0, or 1 when no finite column is reachable. */
+int orc_assign(const double* C, int n, int32_t* p_out) {
+  double* u = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* v = (double*)calloc((size_t)n + 1, sizeof(double));
+  double* minv = (double*)malloc(sizeof(double) * ((size_t)n + 1));
+  int* p = (int*)calloc((size_t)n + 1, sizeof(int));
+  int* way = (int*)calloc((size_t)n + 1, sizeof(int));
+  char* used = (char*)malloc((size_t)n + 1);
+  int rc = 0;
+  for (int i = 1; i <= n && !rc; ++i) {
+    for (int j = 0; j <= n; ++j) {
+      minv[j] = DBL_MAX;
+      used[j] = 0;
+    }
+    p[0] = i;
+    int j0 = 0;
+    for (int step = 0;; ++step) {
+      used[j0] = 1;
+      int i0 = p[j0], j1 = 0;
+      double delta = DBL_MAX;
+      for (int j = 1; j <= n; ++j) {
+        if (used[j]) continue;
+        double cur = (C[(size_t)(i0 - 1) * n + (j - 1)] - u[i0]) - v[j];
+        if (cur < minv[j]) {
+          minv[j] = cur;
+          way[j] = j0;
+        }
+        if (minv[j] < delta) {
+          delta = minv[j];
+          j1 = j;
+        }
+      }
+      if (j1 == 0 || step > n) {
+        rc = 1;
+        break;
+      }
+      for (int j = 0; j <= n; ++j) {
+        if (used[j]) {
+          u[p[j]] += delta;
+          v[j] -= delta;
+        } else {
+          minv[j] -= delta;
+        }
+      }
+      j0 = j1;
+      if (p[j0] == 0) break;
+    }
+    if (rc) break;
+    do {
+      int j1 = way[j0];
+      p[j0] = p[j1];
+      j0 = j1;
+    } while (j0);
+  }
+  for (int j = 1; j <= n; ++j) p_out[j - 1] = p[j];
+  free(u);
+  free(v);
+  free(minv);
+  free(p);
+  free(way);
+  free(used);
+  return rc;
+}
+
+static int64_t key_index(const int64_t* keys, int64_t n, int64_t key) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    int64_t mid = (lo + hi) >> 1;
+    if (keys[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  return (lo < n && keys[lo] == key) ? lo : -1;
+}
+
+/* sort() over sorted keys: perm_out (n_keys × B) row k is the permutation of
+ * key k (row → column for i < j, column → row for the reverse key).
+ * cost_out, when given, receives the cost matrix of every key with i < j.
+ * Returns 0, BRX_ERR_INVALID_ARGUMENT for a missing reverse key, or
+ * BRX_ERR_IMPOSSIBLE (a cosine above 1, no finite assignment). */
+int orc_sort(const orc_sort_side* sides, int n_sides, int B, int64_t nv, int64_t n_keys, const int64_t* keys,
+             int32_t* perm_out, double* cost_out, int threads) {
+  int rc = 0;
+  set_threads(threads);
+#pragma omp parallel
+  {
+    double* C = (double*)malloc(sizeof(double) * (size_t)B * B);
+    int smax = 1;
+    for (int sd = 0; sd < n_sides; ++sd)
+      if (sides[sd].s > smax) smax = sides[sd].s;
+    double* ph = (double*)malloc(sizeof(double) * 2 * (size_t)smax);
+    int32_t* p = (int32_t*)malloc(sizeof(int32_t) * (size_t)B);
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t k = 0; k < n_keys; ++k) {
+      int64_t i = keys[k] / nv, j = keys[k] % nv;
+      if (i >= j) continue;
+      int64_t kr = key_index(keys, n_keys, j * nv + i);
+      int e = 0;
+      if (kr < 0) e = BRX_ERR_INVALID_ARGUMENT;
+      else if (cost_matrix(sides, n_sides, B, i, j, C, ph) || orc_assign(C, B, p)) e = BRX_ERR_IMPOSSIBLE;
+      if (e) {
+#pragma omp critical
+        if (!rc) rc = e;
+        continue;
+      }
+      if (cost_out) memcpy(cost_out + (size_t)k * B * B, C, sizeof(double) * (size_t)B * B);
+      for (int c = 0; c < B; ++c) {
+        perm_out[(size_t)k * B + (p[c] - 1)] = c;
+        perm_out[(size_t)kr * B + c] = p[c] - 1;
+      }
+    }
+    free(C);
+    free(ph);
+    free(p);
+  }
+  return rc;
+}

@@ -130,3 +130,61 @@ class Oracle:
     @staticmethod
     def max_threads():
         return lib().orc_max_threads()
+
+
+class OrcSortSide(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("cplx", C.c_int32), ("s", C.c_int32), ("e0", C.c_int32), ("e1", C.c_int32),
+                ("e2", C.c_int32), ("vf", C.c_int32), ("phase", C.c_int32), ("w", C.c_double * 3)]
+
+
+def sort_permutations(values, vectors, keys, threads=0, return_costs=False):
+    """sort() on the CPU: per key the permutation of the modes (row → column
+    for i < j, column → row for the reverse key), as brx_sort computes it.
+
+    values / vectors: (array (V, B, span) float64 or complex128, elements[3],
+    vector cost function, weights[3]); vectors may be None.  Returns perm
+    (n_keys × B int32) and, with return_costs, the cost matrices of the keys
+    with i < j (n_keys × B × B, zero elsewhere)."""
+    keys = np.ascontiguousarray(keys, np.int64)
+    sides, keep = [], []
+    for k, spec in enumerate((values, vectors)):
+        if spec is None:
+            continue
+        arr, el, vf, w = spec
+        arr = np.ascontiguousarray(arr)
+        cplx = np.iscomplexobj(arr)
+        arr = np.ascontiguousarray(arr, np.complex128 if cplx else np.float64)
+        keep.append(arr)
+        s = OrcSortSide()
+        s.data = arr.ctypes.data
+        s.cplx = int(cplx)
+        s.e0, s.e1, s.e2 = (int(x) for x in el)
+        s.s = s.e0 + s.e1 + s.e2
+        s.vf = int(vf)
+        s.phase = int(k == 1)
+        s.w[:] = [float(x) for x in w]
+        sides.append(s)
+    V, B = keep[0].shape[0], keep[0].shape[1]
+    arr_t = OrcSortSide * len(sides)
+    sa = arr_t(*sides)
+    perm = np.zeros((keys.size, B), np.int32)
+    costs = np.zeros((keys.size, B, B)) if return_costs else None
+    rc = lib().orc_sort(sa, C.c_int(len(sides)), C.c_int(B), C.c_int64(V), C.c_int64(keys.size),
+                        C.c_void_p(keys.ctypes.data), C.c_void_p(perm.ctypes.data),
+                        C.c_void_p(costs.ctypes.data) if costs is not None else C.c_void_p(), C.c_int(threads))
+    if rc:
+        raise RuntimeError(f"orc_sort failed with status {rc}")
+    return (perm, costs) if return_costs else perm
+
+
+def assign(cost):
+    """Exact assignment of a square cost matrix: col_of_row[r] for each row."""
+    cost = np.ascontiguousarray(cost, np.float64)
+    n = cost.shape[0]
+    p = np.zeros(n, np.int32)
+    rc = lib().orc_assign(C.c_void_p(cost.ctypes.data), C.c_int(n), C.c_void_p(p.ctypes.data))
+    if rc:
+        raise RuntimeError("no finite assignment")
+    out = np.empty(n, np.int64)
+    out[p - 1] = np.arange(n)
+    return out

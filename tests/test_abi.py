@@ -33,7 +33,7 @@ def test_struct_layout_matches_header(tmp_path):
     """ctypes mirrors of brx_geometry / brx_data / brx_locate_out have the C
     sizes and field offsets."""
     fields = {"brx_geometry": _abi.Geometry, "brx_data": _abi.Data, "brx_locate_out": _abi.LocateOut,
-              "brx_mlp_dims": _abi.MlpDims}
+              "brx_mlp_dims": _abi.MlpDims, "brx_sort_cost": _abi.SortCost}
     src = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in fields.items():
         src.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
