@@ -64,7 +64,7 @@ struct SortSide {
   int reals;         // reals per row: s, or 2s for complex
   int rs;            // padded row stride in staged units (odd)
   int off_i, off_j;  // staged rows of vertex i / j: byte offsets in the warp region
-  int off_ni, off_nj;  // vector-part squared norms per row (double): byte offsets
+  int off_ni, off_nj;  // per row of i / j: vector-part |x|², |x| and 1/|x|² (0 for a zero row), B doubles each
 };
 
 struct SortParams {
@@ -109,10 +109,28 @@ __device__ __forceinline__ double cos_of(double num, double na, double nb, const
   return c;
 }
 
+// Vector-part norms of one row: |x|², |x| and 1/|x|² (0 for a zero row).
+struct RowNorm {
+  double n2, n, inv2;
+};
+
+// sin² of the angle whose cosine has the square num2·inv2x·inv2y (the
+// reference's sin(acos(c))², src/interpolator.hpp:287-294, as 1 − c²): the
+// zero-norm rule and the snap of c ≈ ±1 are the reference's; only where c²
+// exceeds 1 is c itself formed to decide between the snap and an error.
+__device__ __forceinline__ double sin2_of(double num2, const RowNorm& x, const RowNorm& y, const brx::Tol& one,
+                                          bool* bad) {
+  if (x.n2 == 0.0 || y.n2 == 0.0) return (x.n2 != 0.0 || y.n2 != 0.0) ? 1.0 : 0.0;
+  const double c2 = num2 * x.inv2 * y.inv2;
+  if (c2 <= 1.0) return 1.0 - c2;
+  const double c = cos_of(sqrt(num2), x.n, y.n, one, bad);
+  return 1.0 - c * c;
+}
+
 // Interpolator::add_cost for one (row a of vertex i, row b of vertex j)
 // (src/interpolator_cost.tpp:19-61): w0·scalar + w1·vector + w2·matrix cost.
 template <typename T>
-__device__ double pair_cost(const SortSide& S, const T* x, const T* y, double xx, double yy,
+__device__ double pair_cost(const SortSide& S, const T* x, const T* y, const RowNorm& nx, const RowNorm& ny,
                             const brx::Tol& one, bool* bad) {
   double sc = 0.0, vc = 0.0, mc = 0.0;
   const int e0 = S.e0, e1 = S.e1, e2 = S.e2, s = S.s;
@@ -159,18 +177,14 @@ __device__ double pair_cost(const SortSide& S, const T* x, const T* y, double xx
         case 2:  // 1 − |⟨x, e·y⟩|²
           vc = 1.0 - (vr * vr + vi * vi);
           break;
-        case 3: {  // Euclidean angle of the 2n-real vectors x and e·y
-          const double c = cos_of(er * vr - ei * vi, sqrt(xx), sqrt(yy), one, bad);
-          vc = acos(c);
+        case 3:  // Euclidean angle of the 2n-real vectors x and e·y
+          vc = acos(cos_of(er * vr - ei * vi, nx.n, ny.n, one, bad));
           break;
-        }
         case 4:  // Hermitian angle
-          vc = acos(cos_of(sqrt(vr * vr + vi * vi), sqrt(xx), sqrt(yy), one, bad));
+          vc = acos(cos_of(sqrt(vr * vr + vi * vi), nx.n, ny.n, one, bad));
           break;
-        default: {  // sin² of the Hermitian angle
-          const double t = sin(acos(cos_of(sqrt(vr * vr + vi * vi), sqrt(xx), sqrt(yy), one, bad)));
-          vc = t * t;
-        }
+        default:  // sin² of the Hermitian angle
+          vc = sin2_of(vr * vr + vi * vi, nx, ny, one, bad);
       }
     }
     for (int m = 0; m < e2 / 9; ++m) {
@@ -191,17 +205,9 @@ __device__ double pair_cost(const SortSide& S, const T* x, const T* y, double xx
       } else {
         double ab = 0.0;
         for (int k = e0; k < e0 + e1; ++k) ab += (double)x[k] * (double)y[k];
-        if (S.vf == 2) {
-          vc = 1.0 - ab;
-        } else {
-          const double c = cos_of(ab, sqrt(xx), sqrt(yy), one, bad);
-          if (S.vf == 3 || S.vf == 4) {
-            vc = acos(c);
-          } else {
-            const double t = sin(acos(c));
-            vc = t * t;
-          }
-        }
+        if (S.vf == 2) vc = 1.0 - ab;
+        else if (S.vf == 3 || S.vf == 4) vc = acos(cos_of(ab, nx.n, ny.n, one, bad));
+        else vc = sin2_of(ab * ab, nx, ny, one, bad);
       }
     }
     for (int m = 0; m < e2 / 9; ++m) {
@@ -216,14 +222,25 @@ __device__ double pair_cost(const SortSide& S, const T* x, const T* y, double xx
   return (S.w0 * sc + S.w1 * vc) + S.w2 * mc;
 }
 
-// Copy the B rows of one vertex into padded shared-memory rows and form the
-// squared norms of their vector parts.
+// Copy the B rows of one vertex into padded shared-memory rows (four loads
+// in flight per lane) and form the norms of their vector parts.
 template <typename T>
-__device__ void stage_rows(const SortSide& S, int B, long long vtx, T* dst, double* nrm, int lane) {
+__device__ void stage_rows(const SortSide& S, int B, long long vtx, T* dst, RowNorm* nrm, int lane) {
   const long long base = vtx * (long long)B * S.reals;
-  for (int idx = lane; idx < B * S.reals; idx += 32) {
-    const int r = idx / S.reals, c = idx - r * S.reals;
-    dst[r * S.rs + c] = load_elem<T>(S.data, S.store, base + idx);
+  const int total = B * S.reals;
+  for (int i0 = lane; i0 < total; i0 += 128) {
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (i0 + 32 * u < total) v[u] = load_elem<T>(S.data, S.store, base + i0 + 32 * u);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = i0 + 32 * u;
+      if (idx < total) {
+        const int r = idx / S.reals;
+        dst[r * S.rs + (idx - r * S.reals)] = v[u];
+      }
+    }
   }
   __syncwarp();
   const int m = S.cplx ? 2 : 1;
@@ -231,7 +248,9 @@ __device__ void stage_rows(const SortSide& S, int B, long long vtx, T* dst, doub
     double n2 = 0.0;
     const T* row = dst + r * S.rs;
     for (int k = m * S.e0; k < m * (S.e0 + S.e1); ++k) n2 += (double)row[k] * (double)row[k];
-    nrm[r] = n2;
+    nrm[r].n2 = n2;
+    nrm[r].n = sqrt(n2);
+    nrm[r].inv2 = n2 > 0.0 ? 1.0 / n2 : 0.0;
   }
 }
 
@@ -341,7 +360,13 @@ __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortPara
   int* p = reinterpret_cast<int*>(minv + (B + 1));
   int* way = p + (B + 1);
   int* used = way + (B + 1);
-  for (long long k = (long long)blockIdx.x * (blockDim.x >> 5) + wib; k < P.n_keys; k += nw) {
+  // each warp takes a contiguous run of keys: consecutive keys share vertex
+  // i, whose rows stay staged
+  const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
+  const long long per = (P.n_keys + nw - 1) / nw;
+  const long long k_end = min(P.n_keys, (gw + 1) * per);
+  long long staged_i = -1;
+  for (long long k = gw * per; k < k_end; ++k) {
     const long long key = P.keys[k];
     const long long i = key / P.n_vertices, j = key - i * P.n_vertices;
     // every key needs its reverse (the reference's overwrite of j·N+i fails without it)
@@ -353,9 +378,11 @@ __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortPara
     if (i >= j) continue;
     for (int sd = 0; sd < P.n_sides; ++sd) {
       const SortSide& S = P.side[sd];
-      stage_rows<T>(S, B, i, reinterpret_cast<T*>(region + S.off_i), reinterpret_cast<double*>(region + S.off_ni), lane);
-      stage_rows<T>(S, B, j, reinterpret_cast<T*>(region + S.off_j), reinterpret_cast<double*>(region + S.off_nj), lane);
+      if (i != staged_i)
+        stage_rows<T>(S, B, i, reinterpret_cast<T*>(region + S.off_i), reinterpret_cast<RowNorm*>(region + S.off_ni), lane);
+      stage_rows<T>(S, B, j, reinterpret_cast<T*>(region + S.off_j), reinterpret_cast<RowNorm*>(region + S.off_nj), lane);
     }
+    staged_i = i;
     __syncwarp();
     bool bad = false;
     for (int q = lane; q < B * B; q += 32) {
@@ -365,9 +392,9 @@ __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortPara
         const SortSide& S = P.side[sd];
         const T* x = reinterpret_cast<const T*>(region + S.off_i) + a * S.rs;
         const T* y = reinterpret_cast<const T*>(region + S.off_j) + b * S.rs;
-        const double xx = reinterpret_cast<const double*>(region + S.off_ni)[a];
-        const double yy = reinterpret_cast<const double*>(region + S.off_nj)[b];
-        c += pair_cost<T>(S, x, y, xx, yy, P.one, &bad);
+        const RowNorm nx = reinterpret_cast<const RowNorm*>(region + S.off_ni)[a];
+        const RowNorm ny = reinterpret_cast<const RowNorm*>(region + S.off_nj)[b];
+        c += pair_cost<T>(S, x, y, nx, ny, P.one, &bad);
       }
       C[q] = c;
     }
@@ -478,8 +505,8 @@ extern "C" brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* key
     SortSide& S = P.side[sd];
     S.off_i = take(esz * B * S.rs);
     S.off_j = take(esz * B * S.rs);
-    S.off_ni = take(sizeof(double) * B);
-    S.off_nj = take(sizeof(double) * B);
+    S.off_ni = take(3 * sizeof(double) * B);
+    S.off_nj = take(3 * sizeof(double) * B);
   }
   P.off_c = take(sizeof(double) * B * B);
   P.off_lap = take(sizeof(double) * 3 * (B + 1) + sizeof(int) * 3 * (B + 1));
