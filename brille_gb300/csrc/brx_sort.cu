@@ -10,19 +10,21 @@
 // src/utilities.tpp:249-431,567-598).  The row → column assignment becomes
 // the permutation of key i·N+j and the column → row assignment that of j·N+i.
 //
-// Here one warp owns one pair at a time:
-//  1. both vertices' rows of values and vectors are copied into the warp's
+// Here one CTA owns one pair at a time (four warps, one per scheduler, or
+// one warp when B < 16), over a contiguous run of keys so that consecutive
+// pairs of one vertex keep its rows staged:
+//  1. both vertices' rows of values and vectors are copied into the CTA's
 //     shared memory (FP64 storage as double, FP32/BF16 storage as float),
 //     rows padded to an odd stride so that lanes reading different rows hit
 //     different banks;
-//  2. the cost matrix is formed in FP64 with the lanes over (row, column)
+//  2. the cost matrix is formed in FP64 with the threads over (row, column)
 //     pairs.  The antiphase e^{-iθ} of the vectors is conj(h)/|h| of the
 //     Hermitian product h over the whole branch, and the vector-part costs
 //     use |⟨x, e·y⟩| = |⟨x, y⟩| and Re⟨x, e·y⟩ = Re(e·⟨x, y⟩), which equal the
 //     reference's costs up to rounding; scalars, matrices and the distance
 //     cost are formed element by element against e·y as the reference does;
-//  3. the assignment is solved exactly by the shortest augmenting path method
-//     with row and column potentials: lanes scan columns, a shuffle argmin
+//  3. warp 0 solves the assignment exactly by the shortest augmenting path
+//     method with row and column potentials: lanes scan columns, a shuffle argmin
 //     (ties to the lower column) picks the next column, lanes update the
 //     potentials of their columns, lane 0 walks the augmenting path.  The
 //     optimum is the one LAPJV finds wherever it is unique;
@@ -49,7 +51,8 @@ using namespace brx_detail;
 
 namespace {
 
-constexpr int kMaxSortWarps = 8;
+constexpr int kMaxSortWarps = 4;
+constexpr int kPairWarps = 4;
 constexpr unsigned kFull = 0xffffffffu;
 
 // one interpolator (values or vectors) as the cost kernel sees it
@@ -77,7 +80,6 @@ struct SortParams {
   int32_t* perm_out;  // n_keys × B
   int32_t* nonid;     // n_keys
   int32_t* status;    // [0] brx_status of the first failure, [1] its key index
-  int warp_bytes;
   int off_c;          // B×B cost matrix (double)
   int off_lap;        // u, v, minv (double, B+1 each), then p, way, used (int, B+1 each)
   brx::Tol one;       // approx_float::scalar(·, 1.0) tolerance
@@ -223,28 +225,30 @@ __device__ double pair_cost(const SortSide& S, const T* x, const T* y, const Row
 }
 
 // Copy the B rows of one vertex into padded shared-memory rows (four loads
-// in flight per lane) and form the norms of their vector parts.
+// in flight per thread) and form the norms of their vector parts; all
+// threads of the CTA take part.
 template <typename T>
-__device__ void stage_rows(const SortSide& S, int B, long long vtx, T* dst, RowNorm* nrm, int lane) {
+__device__ void stage_rows(const SortSide& S, int B, long long vtx, T* dst, RowNorm* nrm) {
+  const int tid = threadIdx.x, nt = blockDim.x;
   const long long base = vtx * (long long)B * S.reals;
   const int total = B * S.reals;
-  for (int i0 = lane; i0 < total; i0 += 128) {
+  for (int i0 = tid; i0 < total; i0 += 4 * nt) {
     T v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u)
-      if (i0 + 32 * u < total) v[u] = load_elem<T>(S.data, S.store, base + i0 + 32 * u);
+      if (i0 + nt * u < total) v[u] = load_elem<T>(S.data, S.store, base + i0 + nt * u);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int idx = i0 + 32 * u;
+      const int idx = i0 + nt * u;
       if (idx < total) {
         const int r = idx / S.reals;
         dst[r * S.rs + (idx - r * S.reals)] = v[u];
       }
     }
   }
-  __syncwarp();
+  __syncthreads();
   const int m = S.cplx ? 2 : 1;
-  for (int r = lane; r < B; r += 32) {
+  for (int r = tid; r < B; r += nt) {
     double n2 = 0.0;
     const T* row = dst + r * S.rs;
     for (int k = m * S.e0; k < m * (S.e0 + S.e1); ++k) n2 += (double)row[k] * (double)row[k];
@@ -345,13 +349,13 @@ __device__ long long find_key(const long long* keys, long long n, long long key)
   return (lo < n && keys[lo] == key) ? lo : -1;
 }
 
+// One vertex pair at a time per CTA (one warp for B < 16, else four: one per
+// scheduler, so that the FP64 cost matrix keeps every FP64 pipe of the SM
+// fed); warp 0 then solves the assignment and writes both permutations.
 template <typename T>
 __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortParams P) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  unsigned char* region = smem + (size_t)wib * P.warp_bytes;
-  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  extern __shared__ __align__(16) unsigned char region[];
+  const int tid = threadIdx.x, lane = tid & 31;
   const int B = P.B;
   double* C = reinterpret_cast<double*>(region + P.off_c);
   double* u = reinterpret_cast<double*>(region + P.off_lap);
@@ -360,32 +364,32 @@ __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortPara
   int* p = reinterpret_cast<int*>(minv + (B + 1));
   int* way = p + (B + 1);
   int* used = way + (B + 1);
-  // each warp takes a contiguous run of keys: consecutive keys share vertex
+  // each CTA takes a contiguous run of keys: consecutive keys share vertex
   // i, whose rows stay staged
-  const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
-  const long long per = (P.n_keys + nw - 1) / nw;
-  const long long k_end = min(P.n_keys, (gw + 1) * per);
+  const long long per = (P.n_keys + gridDim.x - 1) / gridDim.x;
+  const long long k_end = min(P.n_keys, ((long long)blockIdx.x + 1) * per);
   long long staged_i = -1;
-  for (long long k = gw * per; k < k_end; ++k) {
+  for (long long k = (long long)blockIdx.x * per; k < k_end; ++k) {
     const long long key = P.keys[k];
     const long long i = key / P.n_vertices, j = key - i * P.n_vertices;
     // every key needs its reverse (the reference's overwrite of j·N+i fails without it)
     const long long kr = find_key(P.keys, P.n_keys, j * P.n_vertices + i);
     if (kr < 0) {
-      if (lane == 0) record(P, BRX_ERR_INVALID_ARGUMENT, k);
+      if (tid == 0) record(P, BRX_ERR_INVALID_ARGUMENT, k);
       continue;
     }
     if (i >= j) continue;
+    __syncthreads();  // the previous pair's assignment is done with the shared rows
     for (int sd = 0; sd < P.n_sides; ++sd) {
       const SortSide& S = P.side[sd];
       if (i != staged_i)
-        stage_rows<T>(S, B, i, reinterpret_cast<T*>(region + S.off_i), reinterpret_cast<RowNorm*>(region + S.off_ni), lane);
-      stage_rows<T>(S, B, j, reinterpret_cast<T*>(region + S.off_j), reinterpret_cast<RowNorm*>(region + S.off_nj), lane);
+        stage_rows<T>(S, B, i, reinterpret_cast<T*>(region + S.off_i), reinterpret_cast<RowNorm*>(region + S.off_ni));
+      stage_rows<T>(S, B, j, reinterpret_cast<T*>(region + S.off_j), reinterpret_cast<RowNorm*>(region + S.off_nj));
     }
     staged_i = i;
-    __syncwarp();
+    __syncthreads();
     bool bad = false;
-    for (int q = lane; q < B * B; q += 32) {
+    for (int q = tid; q < B * B; q += blockDim.x) {
       const int a = q / B, b = q - a * B;
       double c = 0.0;
       for (int sd = 0; sd < P.n_sides; ++sd) {
@@ -398,35 +402,33 @@ __global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortPara
       }
       C[q] = c;
     }
-    if (__any_sync(kFull, bad)) {
-      if (lane == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
-      __syncwarp();
+    if (__syncthreads_or(bad)) {  // also the barrier after which C is complete
+      if (tid == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
       continue;
     }
-    __syncwarp();
-    if (!assign_warp(C, B, u, v, minv, p, way, used, lane)) {
-      if (lane == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
-      __syncwarp();
-      continue;
-    }
-    bool moved = false, unmatched = false;
-    for (int jj = 1 + lane; jj <= B; jj += 32) {
-      const int r = p[jj] - 1;
-      if (r < 0 || r >= B) {
-        unmatched = true;
-        continue;
+    if (tid < 32) {
+      if (!assign_warp(C, B, u, v, minv, p, way, used, lane)) {
+        if (lane == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
+      } else {
+        bool moved = false, unmatched = false;
+        for (int jj = 1 + lane; jj <= B; jj += 32) {
+          const int r = p[jj] - 1;
+          if (r < 0 || r >= B) {
+            unmatched = true;
+            continue;
+          }
+          P.perm_out[k * B + r] = jj - 1;   // row (mode of i) → column (mode of j)
+          P.perm_out[kr * B + jj - 1] = r;  // column → row
+          moved |= (r != jj - 1);
+        }
+        if (__any_sync(kFull, unmatched) && lane == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
+        const bool any = __any_sync(kFull, moved);
+        if (lane == 0) {
+          P.nonid[k] = any;
+          P.nonid[kr] = any;
+        }
       }
-      P.perm_out[k * B + r] = jj - 1;   // row (mode of i) → column (mode of j)
-      P.perm_out[kr * B + jj - 1] = r;  // column → row
-      moved |= (r != jj - 1);
     }
-    if (__any_sync(kFull, unmatched) && lane == 0) record(P, BRX_ERR_IMPOSSIBLE, k);
-    const bool any = __any_sync(kFull, moved);
-    if (lane == 0) {
-      P.nonid[k] = any;
-      P.nonid[kr] = any;
-    }
-    __syncwarp();
   }
 }
 
@@ -510,12 +512,11 @@ extern "C" brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* key
   }
   P.off_c = take(sizeof(double) * B * B);
   P.off_lap = take(sizeof(double) * 3 * (B + 1) + sizeof(int) * 3 * (B + 1));
-  const size_t warp_bytes = (off + 15) & ~(size_t)15;
-  if (warp_bytes > h->smem_optin)
+  const size_t pair_bytes = (off + 15) & ~(size_t)15;
+  if (pair_bytes > h->smem_optin)
     return fail(h, BRX_ERR_UNSUPPORTED,
-                "sort: one vertex pair needs " + std::to_string(warp_bytes) + " bytes of shared memory (more than " +
+                "sort: one vertex pair needs " + std::to_string(pair_bytes) + " bytes of shared memory (more than " +
                     std::to_string(h->smem_optin) + "); use FP32 storage or fewer branches");
-  P.warp_bytes = (int)warp_bytes;
   BRX_CUDA(h, cudaSetDevice(h->device));
   cudaStream_t cs = stream ? static_cast<cudaStream_t>(stream) : h->sc[0].stream;
   h->n_keys = 0;
@@ -545,15 +546,16 @@ extern "C" brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* key
   P.perm_out = static_cast<int32_t*>(d_out.p);
   P.nonid = static_cast<int32_t*>(d_flag.p);
   P.status = static_cast<int32_t*>(d_status.p);
-  const int warps = (int)std::max<size_t>(1, std::min<size_t>(kMaxSortWarps, h->smem_optin / warp_bytes));
-  const size_t dyn = warp_bytes * warps;
+  // one pair per CTA: four warps (one per scheduler) once the cost matrix
+  // has enough entries to share, one below
+  const int warps = B * B >= 256 ? kPairWarps : 1;
+  const size_t dyn = pair_bytes;
   const void* fn = f64 ? (const void*)sort_pairs_kernel<double> : (const void*)sort_pairs_kernel<float>;
   BRX_CUDA(h, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn));
   int per_sm = 0;
   BRX_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * warps, dyn));
-  const long long pairs = (n_keys + 1) / 2;
   long long grid = (long long)std::max(1, per_sm) * h->num_sms;
-  grid = std::max<long long>(1, std::min<long long>(grid, (pairs + warps - 1) / warps));
+  grid = std::max<long long>(1, std::min<long long>(grid, n_keys));
   if (f64) sort_pairs_kernel<double><<<(unsigned)grid, 32 * warps, dyn, cs>>>(P);
   else sort_pairs_kernel<float><<<(unsigned)grid, 32 * warps, dyn, cs>>>(P);
   BRX_CUDA(h, cudaGetLastError());
