@@ -477,3 +477,109 @@ class BZTrellisQdc(_Grid):
 class BZTrellisQcc(_Grid):
     VALUE_COMPLEX = True
     VECTOR_COMPLEX = True
+
+
+class _MeshGrid(_Grid):
+    """BZMeshQ*: a tetrahedral mesh of the irreducible polyhedron
+    (wrap/_mesh.hpp:29-53, src/bz_mesh.hpp:45-140).  ``max_size`` bounds the
+    tetrahedron volume in Å⁻³ (−1: the polyhedron's vertices alone),
+    ``max_points`` the vertex count; ``num_levels`` is accepted for
+    compatibility: the reference's coarser layers only speed its search, which
+    the knot grid of the mesh tables does here.  Queries run on the same GPU
+    path as the trellis."""
+
+    def __init__(self, bz: BrillouinZone, max_size=-1.0, num_levels=3, max_points=-1, *, mesh=None, device=0,
+                 float_tolerance=1e-12, digit=1000):
+        from .mesh import MeshTrellis
+
+        if mesh is None:
+            mesh = MeshTrellis(bz.ir_vertices, float(max_size), int(max_points))
+        self.num_levels = int(num_levels)
+        super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
+
+    @property
+    def BrillouinZone(self):
+        return self.bz
+
+    @property
+    def tetrahedra(self):
+        return self.trellis.mesh_tetrahedra.copy()
+
+
+class _NestGrid(_Grid):
+    """BZNestQ*: the leaves of a nested tetrahedral refinement of the
+    irreducible polyhedron (wrap/_nest.hpp:29-72, src/bz_nest.hpp,
+    src/nest.hpp:302-320).  The second argument is the maximum leaf volume in
+    Å⁻³ (a float) or a number density (an int: the polyhedron's volume over
+    it); ``max_branchings`` is accepted for compatibility: the reference's
+    tree only speeds its search, which the knot grid of the mesh tables does
+    here.  Queries run on the same GPU path as the trellis."""
+
+    def __init__(self, bz: BrillouinZone, max_volume, max_branchings=5, *, mesh=None, device=0,
+                 float_tolerance=1e-12, digit=1000):
+        from .mesh import MeshTrellis
+
+        if isinstance(max_volume, (int, np.integer)) and not isinstance(max_volume, bool):
+            if max_volume < 1:
+                raise ValueError("the number density must be positive")
+            vol = bz.ir_volume / float(max_volume)
+        else:
+            vol = float(max_volume)
+        if mesh is None:
+            mesh = MeshTrellis(bz.ir_vertices, vol)
+        self.max_branchings = int(max_branchings)
+        super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
+
+    @property
+    def BrillouinZone(self):
+        return self.bz
+
+    @property
+    def all_invA(self):
+        return self.invA
+
+    @property
+    def all_rlu(self):
+        return self.rlu
+
+    @property
+    def tetrahedra(self):
+        return self.trellis.mesh_tetrahedra.copy()
+
+    @property
+    def bytes_per_point(self):
+        """Bytes of the device tables per vertex (vertex data not counted)."""
+        t = self.trellis
+        total = (t.vertices.nbytes + t.tet_vertices.nbytes + t.tet_sphere.nbytes + t.tet_volume.nbytes +
+                 t.node_type.nbytes + t.node_index.nbytes + t.poly_tet_offset.nbytes)
+        return total / max(1, len(t.vertices))
+
+
+class BZMeshQdd(_MeshGrid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = False
+
+
+class BZMeshQdc(_MeshGrid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = True
+
+
+class BZMeshQcc(_MeshGrid):
+    VALUE_COMPLEX = True
+    VECTOR_COMPLEX = True
+
+
+class BZNestQdd(_NestGrid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = False
+
+
+class BZNestQdc(_NestGrid):
+    VALUE_COMPLEX = False
+    VECTOR_COMPLEX = True
+
+
+class BZNestQcc(_NestGrid):
+    VALUE_COMPLEX = True
+    VECTOR_COMPLEX = True

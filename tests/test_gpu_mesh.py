@@ -1,0 +1,84 @@
+"""BZMeshQ / BZNestQ on the GPU against the oracle, through the C ABI.
+
+The mesh grids hand the trellis kernels tables with poly nodes only (every
+tetrahedron listed in each knot cell its bounding box touches).  Bars as for
+the trellis: locate indices and FP64 weights bit-exact, FP64 eigenvalues
+bit-exact, FP64 eigenvectors within 1e-12; sort() permutations equal to the
+oracle's where the optimum is unique.
+"""
+import numpy as np
+import pytest
+
+from brille_gb300 import workloads as W
+from brille_gb300.bz import BrillouinZone
+from brille_gb300.grid import BZMeshQdc, BZNestQdc
+from oracle import oracle as O
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid(kind, name):
+    lat, masses = {"diamond2": W.diamond_primitive, "hex16": W.hexagonal16}[name]()
+    bz = BrillouinZone(lat)
+    g = BZMeshQdc(bz, bz.ir_volume / 300) if kind == "mesh" else BZNestQdc(bz, 300)
+    model = W.bvk_for(lat, masses)
+    w, v = model.modes(g.trellis.vertices @ np.linalg.inv(lat.B))
+    return g, lat, w, v
+
+
+def _queries(g, lat, n=4000, seed=0):
+    rng = np.random.default_rng(seed)
+    Q = rng.uniform(-2, 2, (n, 3))
+    # points on mesh tetrahedron faces and at vertices, in r.l.u.
+    m = g.trellis
+    t = m.mesh_tetrahedra[rng.integers(0, len(m.mesh_tetrahedra), n // 4)]
+    bc = rng.dirichlet([1, 1, 1], size=len(t))
+    face = np.einsum("nk,nkd->nd", bc, m.vertices[t[:, :3]])
+    vert = m.vertices[rng.integers(0, len(m.vertices), n // 4)]
+    return np.concatenate([Q, face @ np.linalg.inv(lat.B), vert @ np.linalg.inv(lat.B)])
+
+
+@pytest.mark.parametrize("kind", ["mesh", "nest"])
+@pytest.mark.parametrize("name", ["diamond2", "hex16"])
+def test_mesh_locate_bit_exact(kind, name):
+    g, lat, _, _ = _grid(kind, name)
+    Q = _queries(g, lat)
+    got = g.locate(Q, ir=True)
+    ref = Oracle(g.tables).move_locate(Q, ir=True)
+    for k in ("status", "q_ir", "tau", "rot", "node", "n_weights", "vertex", "weight"):
+        assert np.array_equal(got[k], ref[k]), k
+    assert not got["status"].any()
+
+
+@pytest.mark.parametrize("kind", ["mesh", "nest"])
+def test_mesh_ir_interpolate_fp64(kind):
+    g, lat, w, v = _grid(kind, "diamond2")
+    nv, B = w.shape
+    g.fill(w, [1, 0, 0, 0, 3], v, [0, 3 * v.shape[2], 0, 2, 1])
+    Q = _queries(g, lat, seed=2)
+    gv, gc = g.ir_interpolate_at(Q)
+    ov, oc, rc, st = Oracle(g.tables).interpolate_at(Q, (w[:, :, None], [1, 0, 0], 0, 3),
+                                                     (v.reshape(nv, B, -1), [0, 3 * v.shape[2], 0], 2, 1))
+    assert rc == 0 and (st == 0).all()
+    assert np.array_equal(gv, ov[:, :, 0])
+    assert np.abs(gc.reshape(oc.shape) - oc).max() < 1e-12
+
+
+def test_mesh_sort():
+    g, lat, w, v = _grid("mesh", "diamond2")
+    nv, B = w.shape
+    g.fill(w, [1, 0, 0, 0, 3], v, [0, 3 * v.shape[2], 0, 2, 1], sort=True)
+    keys, perms = g.permutation_table()
+    assert np.array_equal(keys, g.trellis.permutation_keys())
+    ref, costs = O.sort_permutations((w[:, :, None], (1, 0, 0), 0, (1, 1, 1)),
+                                     (v.reshape(nv, B, -1), (0, 3 * v.shape[2], 0), 0, (1, 1, 1)), keys,
+                                     return_costs=True)
+    diff = np.nonzero((perms != ref).any(axis=1))[0]
+    for k in diff:
+        i, j = keys[k] // nv, keys[k] % nv
+        kk = k if i < j else np.searchsorted(keys, j * nv + i)
+        c = costs[kk]
+        opt = c[np.arange(B), ref[kk]].sum()
+        assert c[np.arange(B), perms[kk]].sum() <= opt + 1e-9 * (1 + abs(opt))
+    assert len(diff) <= max(2, len(keys) // 100)

@@ -1,0 +1,119 @@
+"""BZMeshQ / BZNestQ tables on the CPU: the mesh, its bucketing into trellis
+form, and the oracle's answers on it.
+
+The mesh grids reuse the trellis query path: their tetrahedra are listed in
+poly nodes of a knot grid (brille_gb300.mesh.MeshTrellis).  These tests pin
+the tables: the mesh covers the irreducible polyhedron exactly with
+positively oriented tetrahedra within the volume limit; every point of the
+polyhedron is located in a tetrahedron that contains it; a linear field is
+reproduced exactly (the reference's known-answer test for its grids,
+wrap/tests/test_4_interpolation.py:143-263); the permutation keys are the
+mesh's tetrahedron edges (TetTriLayer::collect_keys,
+src/triangulation_layers.hpp:242-258).
+"""
+import numpy as np
+import pytest
+
+from brille_gb300 import workloads as W
+from brille_gb300.bz import BrillouinZone
+from brille_gb300.mesh import MeshTrellis, delaunay_mesh
+from brille_gb300.tables import geometry_tables
+from oracle.oracle import Oracle
+
+
+def _bz(name):
+    lat, _ = {"diamond2": W.diamond_primitive, "hex16": W.hexagonal16}[name]()
+    return BrillouinZone(lat)
+
+
+@pytest.mark.parametrize("name", ["diamond2", "hex16"])
+def test_mesh_covers_polyhedron(name):
+    bz = _bz(name)
+    vmax = bz.ir_volume / 400
+    m = MeshTrellis(bz.ir_vertices, vmax)
+    T, v = m.mesh_tetrahedra, m.vertices
+    q = v[T]
+    o = np.einsum("ij,ij->i", q[:, 0] - q[:, 3], np.cross(q[:, 1] - q[:, 3], q[:, 2] - q[:, 3]))
+    assert (o > 0).all()
+    assert np.isclose(np.sum(o) / 6, bz.ir_volume, rtol=1e-9)
+    assert (o / 6 <= vmax * (1 + 1e-12)).all()
+    # every listed entry is one mesh tetrahedron with its own sphere and volume
+    assert np.array_equal(m.tet_vertices, T[m.tet_mesh_index])
+    assert np.allclose(m.tet_volume, o[m.tet_mesh_index] / 6)
+    assert m.node_type.size == np.prod(m.shape)
+
+
+def test_max_points_stops_refinement():
+    bz = _bz("diamond2")
+    v, t, vol = delaunay_mesh(bz.ir_vertices, bz.ir_volume / 5000, max_points=200)
+    assert len(v) <= 200 + len(t)  # the last round may add up to one point per tetrahedron it split
+    v2, _, _ = delaunay_mesh(bz.ir_vertices, -1)
+    assert len(v2) == len(np.unique(bz.ir_vertices, axis=0))
+
+
+@pytest.mark.parametrize("name", ["diamond2", "hex16"])
+def test_oracle_locates_every_point(name):
+    bz = _bz(name)
+    m = MeshTrellis(bz.ir_vertices, bz.ir_volume / 300)
+    t = geometry_tables(bz, m)
+    rng = np.random.default_rng(3)
+    Q = rng.uniform(-1.5, 1.5, (3000, 3))
+    rec = Oracle(t).move_locate(Q, ir=True)
+    assert (rec["status"] == 0).all()
+    tet = rec["node"][:, 1]
+    assert (tet >= 0).all()
+    x = rec["q_ir"] @ bz.lattice.B
+    # barycentric coordinates of x in the located mesh tetrahedron
+    p = m.vertices[m.tet_vertices[tet]]
+    M = np.stack([p[:, 0] - p[:, 3], p[:, 1] - p[:, 3], p[:, 2] - p[:, 3]], axis=-1)
+    lam = np.linalg.solve(M, (x - p[:, 3])[..., None])[..., 0]
+    lam = np.concatenate([lam, 1 - lam.sum(axis=1, keepdims=True)], axis=1)
+    assert lam.min() > -1e-9
+    assert np.allclose(rec["weight"].sum(axis=1), 1.0)
+
+
+@pytest.mark.parametrize("cls", ["mesh", "nest"])
+def test_linear_field_exact(cls):
+    """Values f = a·x + c at the vertices interpolate to f(q_ir) exactly (up
+    to rounding) anywhere in the polyhedron."""
+    from brille_gb300.grid import BZMeshQdd, BZNestQdd
+
+    bz = _bz("diamond2")
+    grid = BZMeshQdd(bz, bz.ir_volume / 200) if cls == "mesh" else BZNestQdd(bz, 200)
+    t = grid.tables
+    a, c = np.array([0.3, -1.2, 2.5]), 0.7
+    f = grid.trellis.vertices @ a + c
+    rng = np.random.default_rng(5)
+    Q = rng.uniform(-1, 1, (2000, 3))
+    vo, _, rc, st = Oracle(t).interpolate_at(Q, (f[:, None, None].copy(), [1, 0, 0], 0, 3), None, ir=True)
+    assert rc == 0 and (st == 0).all()
+    q_ir = Oracle(t).move(Q, ir=True)[0]
+    want = (q_ir @ bz.lattice.B) @ a + c
+    assert np.abs(vo[:, 0, 0] - want).max() < 1e-12 * (1 + np.abs(want).max())
+
+
+def test_nest_density_and_volume():
+    from brille_gb300.grid import BZNestQdc
+
+    bz = _bz("diamond2")
+    by_density = BZNestQdc(bz, 100)
+    by_volume = BZNestQdc(bz, bz.ir_volume / 100)
+    assert np.array_equal(by_density.invA, by_volume.invA)
+    assert np.array_equal(by_density.tetrahedra, by_volume.tetrahedra)
+    assert by_density.all_rlu.shape == by_density.rlu.shape
+    assert by_density.bytes_per_point > 0
+    with pytest.raises(ValueError):
+        BZNestQdc(bz, 0)
+
+
+def test_mesh_permutation_keys():
+    bz = _bz("diamond2")
+    m = MeshTrellis(bz.ir_vertices, bz.ir_volume / 100)
+    n = len(m.vertices)
+    want = set()
+    for tet in m.mesh_tetrahedra:
+        for a in tet:
+            for b in tet:
+                if a != b:
+                    want.add(int(a) * n + int(b))
+    assert np.array_equal(m.permutation_keys(), np.array(sorted(want), np.int64))
