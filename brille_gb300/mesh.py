@@ -17,8 +17,8 @@ Set-up code (host).  The reference offers two grids besides the trellis:
 Either way the answer is the finest-level tetrahedron that contains q and its
 barycentric weights; the coarser levels only speed the search.  Here the
 finest level is built directly and bucketed for the GPU instead: the
-tetrahedra are listed in every cell of a regular knot grid that their bounding
-boxes touch, so that the trellis tables (``include/brx.h``) describe the mesh
+tetrahedra are listed in every cell of a regular knot grid that they may meet,
+so that the trellis tables (``include/brx.h``) describe the mesh
 with poly nodes only and the trellis locate kernel answers the query (cell
 from the knots, then the first listed tetrahedron that contains q).
 
@@ -96,8 +96,9 @@ def delaunay_mesh(points, max_volume=-1.0, max_points=-1, max_rounds=200):
 class MeshTrellis(TrellisBuild):
     """A tetrahedral mesh of the irreducible polyhedron in trellis form: a
     knot grid whose non-empty cells are poly nodes listing every tetrahedron
-    whose bounding box touches the cell (a tetrahedron appears once per such
-    cell; ``mesh_tetrahedra`` holds each once).  Cells are cell_factor times
+    that may meet the cell (its bounding box touches the cell and none of its
+    face planes separates the two; a tetrahedron appears once per such cell,
+    ``mesh_tetrahedra`` holds each once).  Cells are cell_factor times
     the cube root of the mean tetrahedron volume on a side."""
 
     def __init__(self, ir_vertices, max_volume=-1.0, max_points=-1, cell_factor=2.0):  # noqa: D401
@@ -135,6 +136,28 @@ class MeshTrellis(TrellisBuild):
         ci = np.repeat(c0[:, 0], count) + local % sx
         cj = np.repeat(c0[:, 1], count) + (local // sx) % sy
         ck = np.repeat(c0[:, 2], count) + local // (sx * sy)
+        # drop the cells that one face plane of the tetrahedron separates from
+        # it (all eight box corners strictly beyond the plane): a sound test,
+        # it never drops a cell the tetrahedron meets
+        keep = np.ones(len(tet_of), bool)
+        kx, ky, kz = self.knots
+        corners = np.stack(np.meshgrid([0, 1], [0, 1], [0, 1], indexing="ij"), axis=-1).reshape(8, 3)
+        for f, opp in ((0, 3), (1, 2), (2, 1), (3, 0)):
+            face = [a for a in range(4) if a != opp]
+            a, b, c = (verts[tets[:, x]] for x in face)
+            nrm = np.cross(b - a, c - a)
+            # orient outward: away from the opposite vertex
+            sgn = np.sign(np.einsum("ij,ij->i", nrm, verts[tets[:, opp]] - a))
+            nrm = -nrm * sgn[:, None]
+            nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+            off = np.einsum("ij,ij->i", nrm, a)
+            n_e, o_e = nrm[tet_of], off[tet_of]
+            dmin = np.full(len(tet_of), np.inf)
+            for cc in corners:
+                x = np.stack([kx[ci + cc[0]], ky[cj + cc[1]], kz[ck + cc[2]]], axis=1)
+                dmin = np.minimum(dmin, np.einsum("ij,ij->i", n_e, x) - o_e)
+            keep &= ~(dmin > eps)
+        ci, cj, ck, tet_of = ci[keep], cj[keep], ck[keep], tet_of[keep]
         cell = ci + nx * (cj + ny * ck)
         order = np.lexsort((tet_of, cell))
         cell, tet_of = cell[order], tet_of[order]
