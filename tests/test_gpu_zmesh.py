@@ -82,3 +82,27 @@ def test_mesh_sort():
         opt = c[np.arange(B), ref[kk]].sum()
         assert c[np.arange(B), perms[kk]].sum() <= opt + 1e-9 * (1 + abs(opt))
     assert len(diff) <= max(2, len(keys) // 100)
+
+
+def test_nb_vector_field_nest_known_answer_gpu():
+    """src/tests/nest_test.cpp:45-150 on the GPU: Nb (Im-3m), leaf volume
+    0.01 Å⁻³, f = Q stored as a reciprocal-lattice 3-vector, returned to
+    2e-14 at irreducible points with and without the move."""
+    from brille_gb300.crystal import Basis, Lattice, spacegroup
+    from brille_gb300.grid import BZNestQdd
+
+    a = 3.2598
+    lat = Lattice(((a, a, a), (90, 90, 90)), symmetry=spacegroup("Im-3m"), basis=Basis([[0, 0, 0]], [0]))
+    bz = BrillouinZone(lat)
+    g = BZNestQdd(bz, 0.01, 5)
+    xyz = g.trellis.vertices
+    rng = np.random.default_rng(11)
+    lo, hi = bz.ir_vertices.min(axis=0), bz.ir_vertices.max(axis=0)
+    x = rng.uniform(lo, hi, (20000, 3))
+    hs = bz.ir_halfspaces
+    x = x[np.all(x @ hs[:, :3].T + hs[:, 3] < -1e-6, axis=1)][:200]
+    Q = x @ np.linalg.inv(lat.B)
+    g.fill(np.ones(len(xyz)), [1, 0, 0, 0, 3], np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0, 0, 4])
+    for no_move in (True, False):
+        _, vecs = g.ir_interpolate_at(Q, do_not_move_points=no_move)
+        assert np.abs(vecs.reshape(len(Q), 3) - x).max() < 2e-14

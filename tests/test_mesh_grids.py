@@ -117,3 +117,36 @@ def test_mesh_permutation_keys():
                 if a != b:
                     want.add(int(a) * n + int(b))
     assert np.array_equal(m.permutation_keys(), np.array(sorted(want), np.int64))
+
+
+@pytest.mark.parametrize("cls", ["nest", "mesh"])
+def test_nb_vector_field_nest_known_answer(cls):
+    """src/tests/nest_test.cpp:45-150: Nb (Im-3m, a = 3.2598 Å), leaf volume
+    0.01 Å⁻³, the vector field f = Q (Cartesian) stored as one branch of a
+    3-vector; at random points of the irreducible polyhedron interpolation
+    returns Q to 2e-14, with and without the move (the points are already
+    irreducible, so R is the identity and τ = 0)."""
+    from brille_gb300.crystal import Basis, Lattice, spacegroup
+    from brille_gb300.grid import BZMeshQdd, BZNestQdd
+
+    a = 3.2598
+    lat = Lattice(((a, a, a), (90, 90, 90)), symmetry=spacegroup("Im-3m"), basis=Basis([[0, 0, 0]], [0]))
+    bz = BrillouinZone(lat)
+    g = BZNestQdd(bz, 0.01, 5) if cls == "nest" else BZMeshQdd(bz, 0.01)
+    xyz = g.trellis.vertices
+    o = Oracle(g.tables)
+    rng = np.random.default_rng(11)
+    # random points of the irreducible polyhedron (rejection from its box),
+    # kept off its surface so that rounding cannot move them out
+    lo, hi = bz.ir_vertices.min(axis=0), bz.ir_vertices.max(axis=0)
+    x = rng.uniform(lo, hi, (20000, 3))
+    hs = bz.ir_halfspaces
+    inside = np.all(x @ hs[:, :3].T + hs[:, 3] < -1e-6, axis=1)
+    x = x[inside][:200]
+    Q = x @ np.linalg.inv(lat.B)
+    vals = (np.ones((len(xyz), 1, 1)), [1, 0, 0], 0, 3)
+    vecs = (np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0], 0, 4)
+    for no_move in (True, False):
+        _, co, rc, st = o.interpolate_at(Q, vals, vecs, ir=True, no_move=no_move)
+        assert rc == 0 and (st == 0).all()
+        assert np.abs(co[:, 0, :] - x).max() < 2e-14

@@ -189,3 +189,10 @@ def test_oracle_recovers_shuffles():
     keys = case["tr"].permutation_keys()
     perm = O.sort_permutations((ws[:, :, None], (1, 0, 0), 0, (1, 1, 1)), (vs, (0, 6, 0), 0, (1, 1, 1)), keys)
     assert np.array_equal(perm, expected_perms(keys, sigma))
+
+
+def test_munkres_known_answer():
+    """src/tests/munkres_test.cpp: the cost matrix
+    [[1, 2, 3], [2, 4, 6], [3, 6, 9]] is assigned rows → columns [2, 1, 0]."""
+    c = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [3.0, 6.0, 9.0]])
+    assert O.assign(c).tolist() == [2, 1, 0]
