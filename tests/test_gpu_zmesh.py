@@ -106,3 +106,22 @@ def test_nb_vector_field_nest_known_answer_gpu():
     for no_move in (True, False):
         _, vecs = g.ir_interpolate_at(Q, do_not_move_points=no_move)
         assert np.abs(vecs.reshape(len(Q), 3) - x).max() < 2e-14
+
+
+def test_nb_vector_field_along_face_gpu():
+    """src/tests/nest_test.cpp:223-290 on the GPU: 99 points along the
+    diagonal of the irreducible polyhedron's bounding box return Q to 2e-10."""
+    from brille_gb300.crystal import Basis, Lattice, spacegroup
+    from brille_gb300.grid import BZNestQdd
+
+    a = 3.2598
+    lat = Lattice(((a, a, a), (90, 90, 90)), symmetry=spacegroup("Im-3m"), basis=Basis([[0, 0, 0]], [0]))
+    bz = BrillouinZone(lat)
+    g = BZNestQdd(bz, 0.01)
+    xyz = g.trellis.vertices
+    rlu = bz.ir_vertices @ np.linalg.inv(lat.B)
+    v_min, v_del = rlu.min(axis=0), rlu.max(axis=0) - rlu.min(axis=0)
+    Q = np.array([v_min + v_del * (i + 1) * (0.64 / 99) for i in range(99)])
+    g.fill(np.ones(len(xyz)), [1, 0, 0, 0, 3], np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0, 0, 4])
+    _, vecs = g.ir_interpolate_at(Q)
+    assert np.abs(vecs.reshape(len(Q), 3) - Q @ lat.B).max() < 2e-10

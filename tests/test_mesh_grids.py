@@ -150,3 +150,28 @@ def test_nb_vector_field_nest_known_answer(cls):
         _, co, rc, st = o.interpolate_at(Q, vals, vecs, ir=True, no_move=no_move)
         assert rc == 0 and (st == 0).all()
         assert np.abs(co[:, 0, :] - x).max() < 2e-14
+
+
+@pytest.mark.parametrize("cls", ["nest", "mesh"])
+def test_nb_vector_field_along_face(cls):
+    """src/tests/nest_test.cpp:223-290: the same Nb field at 99 points along
+    the diagonal of the irreducible polyhedron's bounding box in r.l.u. (a
+    line on one of its faces), moved and rotated as needed, returns Q to
+    2e-10."""
+    from brille_gb300.crystal import Basis, Lattice, spacegroup
+    from brille_gb300.grid import BZMeshQdd, BZNestQdd
+
+    a = 3.2598
+    lat = Lattice(((a, a, a), (90, 90, 90)), symmetry=spacegroup("Im-3m"), basis=Basis([[0, 0, 0]], [0]))
+    bz = BrillouinZone(lat)
+    g = BZNestQdd(bz, 0.01) if cls == "nest" else BZMeshQdd(bz, 0.01)
+    xyz = g.trellis.vertices
+    rlu = bz.ir_vertices @ np.linalg.inv(lat.B)
+    v_min, v_del = rlu.min(axis=0), rlu.max(axis=0) - rlu.min(axis=0)
+    step = 0.64 / 99
+    Q = np.array([v_min + v_del * (i + 1) * step for i in range(99)])
+    vals = (np.ones((len(xyz), 1, 1)), [1, 0, 0], 0, 3)
+    vecs = (np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0], 0, 4)
+    _, co, rc, st = Oracle(g.tables).interpolate_at(Q, vals, vecs, ir=True)
+    assert rc == 0 and (st == 0).all()
+    assert np.abs(co[:, 0, :] - Q @ lat.B).max() < 2e-10
