@@ -35,7 +35,7 @@ from __future__ import annotations
 import numpy as np
 from scipy.spatial import Delaunay
 
-from .trellis import NODE_POLY, TrellisBuild, _orient, circumsphere
+from .trellis import NODE_POLY, TrellisBuild, _orient, circumspheres
 
 
 def _circumcentres(q):
@@ -171,11 +171,8 @@ class MeshTrellis(TrellisBuild):
         self.poly_tet_offset = np.append(first, len(cell)).astype(np.int32)
         self.tet_mesh_index = tet_of.astype(np.int32)  # mesh tetrahedron of each listed entry
         self.tet_vertices = tets[tet_of]
-        spheres = np.empty((len(tets), 4))
-        for t in range(len(tets)):
-            c, r = circumsphere(verts[tets[t]])
-            spheres[t, :3], spheres[t, 3] = c, r
-        self.tet_sphere = spheres[tet_of]
+        c, r = circumspheres(verts[tets])
+        self.tet_sphere = np.concatenate([c, r[:, None]], axis=1)[tet_of]
         self.tet_volume = vol[tet_of]
         self.shape = (nx, ny, nz)
 

@@ -69,6 +69,32 @@ def _orient(p0, p1, p2, p3):
     return np.dot(p0 - p3, np.cross(p1 - p3, p2 - p3))
 
 
+def orient_many(q):
+    """orient3d of tetrahedra q (n, 4, 3): six times the signed volume."""
+    return np.einsum("ij,ij->i", q[:, 0] - q[:, 3], np.cross(q[:, 1] - q[:, 3], q[:, 2] - q[:, 3]))
+
+
+def circumspheres(q):
+    """Centres (n, 3) and radii (n,) of the spheres through tetrahedra q (n, 4, 3)."""
+    a = q[:, 1:] - q[:, :1]
+    rhs = 0.5 * np.sum(a * a, axis=2)
+    c = np.linalg.solve(a, rhs[..., None])[..., 0]
+    return q[:, 0] + c, np.linalg.norm(c, axis=1)
+
+
+def oriented_tets(points, tets):
+    """tets (n, 4) reordered to positive orientation, with their circumsphere
+    rows (centre x, y, z, radius) and volumes."""
+    tets = np.array(tets, dtype=np.int64).reshape(-1, 4)
+    if len(tets) == 0:
+        return tets.astype(np.int32), np.zeros((0, 4)), np.zeros(0)
+    o = orient_many(points[tets])
+    flip = o < 0
+    tets[flip] = tets[flip][:, [0, 2, 1, 3]]
+    c, r = circumspheres(points[tets])
+    return tets.astype(np.int32), np.concatenate([c, r[:, None]], axis=1), np.abs(o) / 6.0
+
+
 class TrellisBuild:
     """Flat trellis tables (numpy) ready for the query-path C ABI."""
 
@@ -134,35 +160,26 @@ class TrellisBuild:
         self.vertices = all_pts[keep]
         self.cube_vertices = np.array(
             [[inv[lin[p]] for p in cell] for cell in cube_pts], dtype=np.int32).reshape(-1, 8)
-        tets, spheres, vols, tet_off = [], [], [], [0]
+        tets, tet_off = [], [0]
         poly_node_ids = []
         for (lin_idx, cand), off in zip(poly_cells, offsets):
             gid = inv[np.arange(off, off + len(cand))]
-            p = self.vertices[gid]
-            local = self._tetrahedralise(p, tol)
-            if not local:
+            local = self._tetrahedralise(self.vertices[gid], tol)
+            if len(local) == 0:
                 continue
             poly_node_ids.append(lin_idx)
-            for t in local:
-                q = p[list(t)]
-                o = _orient(q[0], q[1], q[2], q[3])
-                if o < 0:
-                    t = (t[0], t[2], t[1], t[3])
-                    q = p[list(t)]
-                c, r = circumsphere(q)
-                tets.append([gid[t[0]], gid[t[1]], gid[t[2]], gid[t[3]]])
-                spheres.append([c[0], c[1], c[2], r])
-                vols.append(abs(o) / 6.0)
-            tet_off.append(len(tets))
+            tets.append(gid[local])
+            tet_off.append(tet_off[-1] + len(local))
+        tets, spheres, vols = oriented_tets(self.vertices, np.concatenate(tets) if tets else np.zeros((0, 4), int))
         for n, lin_idx in enumerate(poly_node_ids):
             node_type[lin_idx] = NODE_POLY
             node_index[lin_idx] = n
         self.node_type = node_type
         self.node_index = node_index
         self.poly_tet_offset = np.array(tet_off, dtype=np.int32)
-        self.tet_vertices = np.array(tets, dtype=np.int32).reshape(-1, 4)
-        self.tet_sphere = np.array(spheres, dtype=float).reshape(-1, 4)
-        self.tet_volume = np.array(vols, dtype=float)
+        self.tet_vertices = tets
+        self.tet_sphere = spheres
+        self.tet_volume = vols
         self.shape = (nx, ny, nz)
 
     @staticmethod
@@ -232,17 +249,14 @@ class TrellisBuild:
 
     @staticmethod
     def _tetrahedralise(p, tol):
+        """Delaunay simplices (m, 4) of the points p that are not flat."""
         try:
             tri = Delaunay(p, qhull_options="Qbb Qc Qz Q12 Qt")
         except Exception:
-            return []
-        out = []
+            return np.zeros((0, 4), np.int64)
         span = np.max(np.ptp(p, axis=0))
-        for s in tri.simplices:
-            q = p[s]
-            if abs(_orient(q[0], q[1], q[2], q[3])) > 1e-12 * span ** 3:
-                out.append(tuple(int(x) for x in s))
-        return out
+        s = tri.simplices
+        return s[np.abs(orient_many(p[s])) > 1e-12 * span ** 3]
 
     @property
     def n_nodes(self):
@@ -350,21 +364,11 @@ class PointTrellis(TrellisBuild):
         self.knots = [np.array([lo[d] - pad, hi[d] + pad]) for d in range(3)]
         self.vertices = p.copy()
         self.cube_vertices = np.zeros((0, 8), np.int32)
-        tets, spheres, vols = [], [], []
-        for t in self._tetrahedralise(p, 1e-12):
-            q = p[list(t)]
-            o = _orient(q[0], q[1], q[2], q[3])
-            if o < 0:
-                t = (t[0], t[2], t[1], t[3])
-                q = p[list(t)]
-            c, r = circumsphere(q)
-            tets.append(list(t))
-            spheres.append([c[0], c[1], c[2], r])
-            vols.append(abs(o) / 6.0)
+        tets, spheres, vols = oriented_tets(p, self._tetrahedralise(p, 1e-12))
         self.node_type = np.array([NODE_POLY], np.int32)
         self.node_index = np.array([0], np.int32)
         self.poly_tet_offset = np.array([0, len(tets)], np.int32)
-        self.tet_vertices = np.array(tets, np.int32)
-        self.tet_sphere = np.array(spheres)
-        self.tet_volume = np.array(vols)
+        self.tet_vertices = tets
+        self.tet_sphere = spheres
+        self.tet_volume = vols
         self.shape = (1, 1, 1)
