@@ -184,7 +184,10 @@ brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* ke
  * stored data (FP32/BF16 storage: on the rounded data).  One vertex pair's
  * rows and cost matrix must fit one CTA's shared memory (about 40·B² bytes
  * for complex FP64 eigenvectors of B modes: B ≤ 76; FP32 storage: B ≤ 96).
- * Synchronous on stream (NULL: the handle's stream). */
+ * Synchronous on stream (NULL: the handle's stream).  Invalid keys or cost
+ * codes are rejected before the old table is touched; a failure after that
+ * (a reverse key missing, a cost matrix without a finite assignment) leaves
+ * the handle with no permutation table, as after brx_fill. */
 typedef struct brx_sort_cost {
   int32_t scalar_fn;  /* fill's elements[5]: 0, Σ|a−b| (the reference's only scalar cost) */
   int32_t vector_fn;  /* fill's elements[6]: 1 |a−b|, 2 1−|a*·b|², 3 Euclidean angle,
