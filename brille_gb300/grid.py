@@ -88,6 +88,22 @@ def _cost_fns(el):
     return (int(el[5]) if el.size > 5 else 0, int(el[6]) if el.size > 6 else 0)
 
 
+def table_from_moved(keys, moved, perms, n_branches):
+    """(keys, perm_ids, perms) for brx_set_permutations from sorted keys, a
+    mask of the keys whose permutation is not the identity and those
+    permutations in key order: id 0 is the identity, the moved keys take
+    ids 1, 2, … in order."""
+    keys = np.ascontiguousarray(keys, np.int64)
+    moved = np.asarray(moved, bool)
+    perms = np.asarray(perms, np.int32).reshape(-1, n_branches)
+    if moved.shape != keys.shape or int(moved.sum()) != len(perms):
+        raise ValueError("the mask and the permutations do not match the keys")
+    ids = np.zeros(len(keys), np.int32)
+    ids[moved] = np.arange(1, len(perms) + 1, dtype=np.int32)
+    table = np.concatenate([np.arange(n_branches, dtype=np.int32)[None, :], perms])
+    return keys, ids, table
+
+
 def _is_device(x):
     return hasattr(x, "data_ptr") and bool(getattr(x, "is_cuda", False))
 
@@ -300,6 +316,27 @@ class _Grid:
         h = self._handle()
         check(load().brx_sort(h, keys.size, keys.ctypes.data, C.byref(vc), C.byref(cc) if cc is not None else None,
                               stream), h)
+
+    def save_permutations(self, path):
+        """Write the permutation table to an .npz file: the keys, and the
+        permutations of the keys that are not the identity (the reference
+        keeps its table in the grid's HDF5 file, src/permutation_table.hpp)."""
+        keys, perms = self.permutation_table()
+        moved = (perms != np.arange(perms.shape[1], dtype=perms.dtype)).any(axis=1) if len(keys) else np.zeros(0, bool)
+        np.savez(path, keys=keys, moved=moved, perms=perms[moved], n_vertices=len(self.trellis.vertices),
+                 n_branches=int(self._fill["B"]))
+
+    def load_permutations(self, path):
+        """Read a table written by save_permutations into this grid (filled
+        with data of the same vertex and mode counts)."""
+        if self._fill is None:
+            raise RuntimeError("The interpolation data must be filled before setting permutations.")
+        d = np.load(path)
+        if int(d["n_vertices"]) != len(self.trellis.vertices) or int(d["n_branches"]) != int(self._fill["B"]):
+            raise ValueError(f"{path}: the table belongs to a grid of {int(d['n_vertices'])} vertices and "
+                             f"{int(d['n_branches'])} modes")
+        keys, ids, table = table_from_moved(d["keys"], d["moved"], d["perms"], int(d["n_branches"]))
+        self.set_permutations(keys, ids, table)
 
     def permutation_table(self):
         """(keys, perms): every key i*n_vertices+j the handle holds and its

@@ -196,3 +196,24 @@ def test_munkres_known_answer():
     [[1, 2, 3], [2, 4, 6], [3, 6, 9]] is assigned rows → columns [2, 1, 0]."""
     c = np.array([[1.0, 2.0, 3.0], [2.0, 4.0, 6.0], [3.0, 6.0, 9.0]])
     assert O.assign(c).tolist() == [2, 1, 0]
+
+
+def test_table_from_moved_round_trip():
+    """save_permutations keeps only the permutations that move a mode;
+    table_from_moved rebuilds a table that answers every key as before."""
+    from brille_gb300.grid import table_from_moved
+
+    rng = np.random.default_rng(9)
+    B, n = 7, 50
+    keys = np.sort(rng.choice(10_000, n, replace=False)).astype(np.int64)
+    perms = np.tile(np.arange(B, dtype=np.int32), (n, 1))
+    moved = rng.uniform(size=n) < 0.4
+    for k in np.nonzero(moved)[0]:
+        while (perms[k] == np.arange(B)).all():
+            perms[k] = rng.permutation(B)
+    k2, ids, table = table_from_moved(keys, moved, perms[moved], B)
+    assert np.array_equal(k2, keys)
+    assert np.array_equal(table[ids], perms)
+    assert (table[0] == np.arange(B)).all()
+    with pytest.raises(ValueError):
+        table_from_moved(keys, moved, perms[moved][:-1], B)
