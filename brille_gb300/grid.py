@@ -15,6 +15,7 @@ Additions, all keyword-only: ``storage`` on fill ("f64" as given, "f32",
 from __future__ import annotations
 
 import ctypes as C
+from enum import IntEnum
 
 import numpy as np
 
@@ -88,6 +89,13 @@ def _cost_fns(el):
     return (int(el[5]) if el.size > 5 else 0, int(el[6]) if el.size > 6 else 0)
 
 
+class NodeType(IntEnum):
+    """Trellis node types (src/enums.hpp:73; include/brx.h BRX_NODE_*)."""
+    null = 0
+    cube = 1
+    poly = 2
+
+
 def table_from_moved(keys, moved, perms, n_branches):
     """(keys, perm_ids, perms) for brx_set_permutations from sorted keys, a
     mask of the keys whose permutation is not the identity and those
@@ -154,12 +162,17 @@ class _Grid:
     VALUE_COMPLEX = False
     VECTOR_COMPLEX = True
 
-    def __init__(self, bz: BrillouinZone, max_volume=None, always_triangulate=False, *, trellis=None,
-                 device=0, float_tolerance=1e-12, digit=1000):
+    def __init__(self, bz: BrillouinZone, node_volume_fraction=0.1, always_triangulate=False, *, max_volume=None,
+                 trellis=None, device=0, float_tolerance=1e-12, digit=1000):
+        """(wrap/_trellis.hpp:36-38) The reference's ``node_volume_fraction``
+        is handed to its PolyTrellis as the maximum node volume in Å⁻³
+        (src/trellis_poly.hpp:148-160), and so it is here; ``max_volume`` is
+        the same number under its own name and wins when given."""
         if trellis is None:
-            if max_volume is None:
-                raise ValueError("max_volume is required")
-            trellis = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, max_volume, always_triangulate)
+            vol = float(node_volume_fraction if max_volume is None else max_volume)
+            if not vol > 0:
+                raise ValueError("the maximum node volume must be positive")
+            trellis = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, vol, always_triangulate)
         self.bz = bz
         self.trellis = trellis
         self.tables = geometry_tables(bz, trellis, gamma=True, float_tolerance=float_tolerance, digit=digit)
@@ -184,6 +197,57 @@ class _Grid:
     @property
     def tetrahedra(self):
         return self.trellis.tet_vertices.copy()
+
+    @property
+    def BrillouinZone(self):
+        return self.bz
+
+    def _rlu(self, xyz):
+        return xyz @ np.linalg.inv(self.bz.lattice.B)
+
+    @property
+    def inner_invA(self):
+        """Vertices of the cube nodes (wrap/_trellis.hpp:45-47)."""
+        idx = np.unique(self.trellis.cube_vertices)
+        return self.trellis.vertices[idx]
+
+    @property
+    def outer_invA(self):
+        """Vertices of the poly nodes' tetrahedra (wrap/_trellis.hpp:48-50)."""
+        idx = np.unique(self.trellis.tet_vertices)
+        return self.trellis.vertices[idx]
+
+    @property
+    def inner_rlu(self):
+        return self._rlu(self.inner_invA)
+
+    @property
+    def outer_rlu(self):
+        return self._rlu(self.outer_invA)
+
+    def all_node_types(self):
+        """Type of every node in linear order i + nx(j + ny k)
+        (wrap/_trellis.hpp:96-98)."""
+        return [NodeType(int(t)) for t in self.trellis.node_type]
+
+    def node_at_type(self, subscript):
+        """Type of the node at subscript (i, j, k) (wrap/_trellis.hpp:84-86)."""
+        nx, ny, nz = self.trellis.shape
+        i, j, k = (int(x) for x in subscript)
+        if not (0 <= i < nx and 0 <= j < ny and 0 <= k < nz):
+            raise IndexError(f"node subscript {subscript} outside {self.trellis.shape}")
+        return NodeType(int(self.trellis.node_type[i + nx * (j + ny * k)]))
+
+    def node_containing_type(self, Q):
+        """Type of the node whose cell holds each Q (r.l.u., not moved), as
+        the query's locate finds it (wrap/_trellis.hpp:88-94); NodeType.null
+        where no node holds Q."""
+        rec = self.locate(np.asarray(Q, dtype=np.float64).reshape(-1, 3), ir=False, do_not_move_points=True)
+        node = rec["node"][:, 0]
+        out = []
+        for n in node:
+            out.append(NodeType(int(self.trellis.node_type[n])) if n >= 0 else NodeType.null)
+        return out
 
     @property
     def values(self):
@@ -535,10 +599,6 @@ class _MeshGrid(_Grid):
         super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
 
     @property
-    def BrillouinZone(self):
-        return self.bz
-
-    @property
     def tetrahedra(self):
         return self.trellis.mesh_tetrahedra.copy()
 
@@ -566,10 +626,6 @@ class _NestGrid(_Grid):
             mesh = MeshTrellis(bz.ir_vertices, vol)
         self.max_branchings = int(max_branchings)
         super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
-
-    @property
-    def BrillouinZone(self):
-        return self.bz
 
     @property
     def all_invA(self):

@@ -125,3 +125,19 @@ def test_nb_vector_field_along_face_gpu():
     g.fill(np.ones(len(xyz)), [1, 0, 0, 0, 3], np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0, 0, 4])
     _, vecs = g.ir_interpolate_at(Q)
     assert np.abs(vecs.reshape(len(Q), 3) - Q @ lat.B).max() < 2e-10
+
+
+def test_node_containing_type():
+    """node_containing_type (wrap/_trellis.hpp:88-94) on a trellis and a mesh
+    grid: the type of the node the oracle's locate finds for each point."""
+    from brille_gb300.grid import BZTrellisQdc, NodeType
+
+    lat, _ = W.diamond_primitive()
+    bz = BrillouinZone(lat)
+    for g in (BZTrellisQdc(bz, bz.ir_volume / 300), BZMeshQdc(bz, bz.ir_volume / 300)):
+        Q = Oracle(g.tables).move(np.random.default_rng(3).uniform(-1, 1, (500, 3)), ir=True)[0]
+        got = g.node_containing_type(Q)
+        node = Oracle(g.tables).move_locate(Q, ir=False, no_move=True)["node"][:, 0]
+        want = [NodeType(int(g.trellis.node_type[n])) if n >= 0 else NodeType.null for n in node]
+        assert got == want
+        assert all(t != NodeType.null for t in got)

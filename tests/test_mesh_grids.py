@@ -175,3 +175,25 @@ def test_nb_vector_field_along_face(cls):
     _, co, rc, st = Oracle(g.tables).interpolate_at(Q, vals, vecs, ir=True)
     assert rc == 0 and (st == 0).all()
     assert np.abs(co[:, 0, :] - Q @ lat.B).max() < 2e-10
+
+
+def test_trellis_accessors():
+    """The reference's BZTrellisQ accessors (wrap/_trellis.hpp:36-98):
+    node_volume_fraction (the maximum node volume in Å⁻³), inner/outer
+    vertices, node types."""
+    from brille_gb300.grid import BZTrellisQdc, NodeType
+
+    bz = _bz("diamond2")
+    g = BZTrellisQdc(bz, node_volume_fraction=bz.ir_volume / 100)
+    t = g.trellis
+    assert len(g.all_node_types()) == t.node_type.size
+    nx, ny, _ = t.shape
+    for lin in (0, t.node_type.size // 2, t.node_type.size - 1):
+        sub = (lin % nx, (lin // nx) % ny, lin // (nx * ny))
+        assert g.node_at_type(sub) == NodeType(int(t.node_type[lin]))
+    with pytest.raises(IndexError):
+        g.node_at_type(t.shape)
+    assert set(map(tuple, g.inner_invA)) == set(map(tuple, t.vertices[np.unique(t.cube_vertices)]))
+    assert np.allclose(g.outer_rlu @ bz.lattice.B, g.outer_invA)
+    with pytest.raises(ValueError):
+        BZTrellisQdc(bz, 0.0)
