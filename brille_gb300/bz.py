@@ -177,6 +177,51 @@ class BrillouinZone:
             out.append(o.min() > -1e-12)
         return np.array(out)
 
+    # ------------------------------------------------- moves, on the GPU
+    def _mover(self):
+        """A query handle whose trellis is the irreducible polyhedron alone:
+        its locate kernel runs the move and wedge stages of the query path."""
+        if getattr(self, "_move_grid", None) is None:
+            from .grid import BZTrellisQdd
+            from .trellis import PointTrellis
+
+            self._move_grid = BZTrellisQdd(self, trellis=PointTrellis(self.ir_vertices))
+        return self._move_grid
+
+    def _move(self, Q, ir, message):
+        Q = np.asarray(Q, dtype=np.float64)
+        if Q.shape[-1] != 3:
+            raise RuntimeError("The last dimension must have size 3")
+        rec = self._mover().locate(Q.reshape(-1, 3), ir=ir)
+        # 4: move failed, 5: outside the irreducible zone; locate statuses
+        # of the stand-in trellis do not concern the move
+        if np.isin(rec["status"], (4, 5)).any():
+            raise RuntimeError(message)
+        return rec
+
+    def moveinto(self, Q, threads=0):
+        """(q, tau) with Q = q + tau, q inside the first zone and tau integer,
+        all in r.l.u. (BrillouinZone::moveinto, src/bz_move.cpp:103-163;
+        wrap/_bz.cpp:401-432), computed by the query path's FP64 G-shift
+        kernel; ``threads`` is accepted for compatibility."""
+        Q = np.asarray(Q, dtype=np.float64)
+        rec = self._move(Q, False, "failed to move all Q into the first Brillouin Zone")
+        return rec["q_ir"].reshape(Q.shape), rec["tau"].reshape(Q.shape)
+
+    def ir_moveinto(self, Q, threads=0):
+        """(q_ir, tau, R, R⁻¹): the irreducible q_ir, the lattice vector tau
+        and the point operations (direct-lattice integer matrices, one 3×3
+        per Q) with Q = Rᵀ q_ir + tau (BrillouinZone::ir_moveinto,
+        src/bz_move.cpp:257-295; wrap/_bz.cpp:434-496), computed by the query
+        path's G-shift and wedge-search kernel; ``threads`` is accepted for
+        compatibility."""
+        Q = np.asarray(Q, dtype=np.float64)
+        rec = self._move(Q, True, "Moving points into irreducible zone failed.")
+        W = np.asarray(self.pointgroup.W, dtype=np.int32)
+        shape = Q.shape[:-1] + (3, 3)
+        return (rec["q_ir"].reshape(Q.shape), rec["tau"].reshape(Q.shape), W[rec["rot"][:, 0]].reshape(shape),
+                W[rec["rot"][:, 1]].reshape(shape))
+
     @property
     def ir_volume(self):
         from scipy.spatial import ConvexHull
