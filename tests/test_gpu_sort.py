@@ -124,20 +124,3 @@ def test_sort_errors_and_refill():
         unsorted = np.array([5, 3], np.int64)
         check(lib.brx_sort(h, 2, unsorted.ctypes.data, None, None, None), h)
 
-
-def test_save_and_load_permutations(tmp_path):
-    case = crystal_case("diamond2", 1 / 300)
-    ws, vs, sigma = shuffled(case)
-    g = _grid(case)
-    g.fill(ws, [1, 0, 0, 0, 3], vs, [0, 6, 0, 2, 1], sort=True)
-    keys, perms = g.permutation_table()
-    path = tmp_path / "perms.npz"
-    g.save_permutations(path)
-    g2 = _grid(case)
-    g2.fill(ws, [1, 0, 0, 0, 3], vs, [0, 6, 0, 2, 1])
-    g2.load_permutations(path)
-    k2, p2 = g2.permutation_table()
-    assert np.array_equal(k2, keys) and np.array_equal(p2, perms)
-    Q = np.random.default_rng(2).uniform(-1, 1, (2000, 3))
-    a, b = g.ir_interpolate_at(Q), g2.ir_interpolate_at(Q)
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
