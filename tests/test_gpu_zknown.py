@@ -30,3 +30,14 @@ def test_complex_scalars_gpu():
     Q = points()
     vals, _ = g.interpolate_at(Q)
     assert np.abs(np.squeeze(vals) - h(Q)).max() < 1e-12
+
+
+def test_iron_self_consistency_gpu():
+    """test_4_interpolation.py:248-262 on the GPU."""
+    from tests.test_known_answers import fe_dispersion, fe_grid
+
+    g = fe_grid()
+    Q = g.rlu
+    g.fill(fe_dispersion(Q), (1,), Q, (0, 3))
+    vals, _ = g.ir_interpolate_at(Q, False, False)
+    assert np.allclose(np.squeeze(vals), fe_dispersion(Q))

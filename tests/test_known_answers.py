@@ -73,3 +73,28 @@ def test_complex_scalars_interpolate_at():
     assert rc == 0 and (st == 0).all()
     # complex values keep their phase; complex vectors are phase-aligned to the pivot vertex
     assert np.abs(vo[:, 0, 0] - h(Q)).max() < 1e-12
+
+
+def fe_dispersion(Q, J=-16.0, d=0.01):
+    """Nearest-neighbour spin waves of bcc iron (wrap/tests/test_4_interpolation.py)."""
+    return d + 8 * J * (1 - np.cos(np.pi * Q[:, 0]) * np.cos(np.pi * Q[:, 1]) * np.cos(np.pi * Q[:, 2]))
+
+
+def fe_grid():
+    from brille_gb300.crystal import spacegroup
+    from brille_gb300.grid import BZTrellisQdc
+
+    lat = Lattice(((2.87,) * 3, (90, 90, 90)), symmetry=spacegroup("Im-3m"))
+    return BZTrellisQdc(BrillouinZone(lat), 0.125)
+
+
+def test_iron_self_consistency():
+    """test_4_interpolation.py:248-262: bcc Fe spin waves stored at the
+    trellis vertices are returned at the vertices by ir_interpolate_at."""
+    g = fe_grid()
+    Q = g.rlu
+    w = fe_dispersion(Q)
+    vo, _, rc, st = Oracle(g.tables).interpolate_at(Q, (w[:, None, None].copy(), [1, 0, 0], 0, 3),
+                                                    (np.ascontiguousarray(Q[:, None, :]).astype(complex), [0, 3, 0], 0, 3))
+    assert rc == 0 and (st == 0).all()
+    assert np.allclose(vo[:, 0, 0], w)
