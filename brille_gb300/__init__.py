@@ -12,7 +12,9 @@ from .bz import BrillouinZone  # noqa: F401
 from .grid import (BZMeshQcc, BZMeshQdc, BZMeshQdd, BZNestQcc, BZNestQdc, BZNestQdd,  # noqa: F401
                    BZTrellisQcc, BZTrellisQdc, BZTrellisQdd)
 from ._lib import BrxError  # noqa: F401
+from .approx import ApproxConfig, real_space_tolerance, reciprocal_space_tolerance  # noqa: F401
 
 __all__ = ["Basis", "Lattice", "PointSymmetry", "Symmetry", "spacegroup", "BrillouinZone",
            "BZTrellisQdd", "BZTrellisQdc", "BZTrellisQcc", "BZMeshQdd", "BZMeshQdc", "BZMeshQcc",
-           "BZNestQdd", "BZNestQdc", "BZNestQcc", "BrxError"]
+           "BZNestQdd", "BZNestQdc", "BZNestQcc", "BrxError", "ApproxConfig", "real_space_tolerance",
+           "reciprocal_space_tolerance"]

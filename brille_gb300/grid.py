@@ -162,12 +162,20 @@ class _Grid:
     VALUE_COMPLEX = False
     VECTOR_COMPLEX = True
 
-    def __init__(self, bz: BrillouinZone, node_volume_fraction=0.1, always_triangulate=False, *, max_volume=None,
-                 trellis=None, device=0, float_tolerance=1e-12, digit=1000):
+    def __init__(self, bz: BrillouinZone, node_volume_fraction=0.1, always_triangulate=False, approx_config=None, *,
+                 max_volume=None, trellis=None, device=0, float_tolerance=None, digit=None):
         """(wrap/_trellis.hpp:36-38) The reference's ``node_volume_fraction``
         is handed to its PolyTrellis as the maximum node volume in Å⁻³
         (src/trellis_poly.hpp:148-160), and so it is here; ``max_volume`` is
-        the same number under its own name and wins when given."""
+        the same number under its own name and wins when given.  Tolerances:
+        ``approx_config`` (an ApproxConfig), else the global configuration
+        (brille_gb300.approx); ``float_tolerance`` / ``digit`` override
+        either."""
+        from . import approx
+
+        cfg = approx_config if approx_config is not None else approx.config
+        float_tolerance = cfg.reciprocal_space_tolerance if float_tolerance is None else float_tolerance
+        digit = cfg.digits if digit is None else digit
         if trellis is None:
             vol = float(node_volume_fraction if max_volume is None else max_volume)
             if not vol > 0:
@@ -590,7 +598,7 @@ class _MeshGrid(_Grid):
     path as the trellis."""
 
     def __init__(self, bz: BrillouinZone, max_size=-1.0, num_levels=3, max_points=-1, *, mesh=None, device=0,
-                 float_tolerance=1e-12, digit=1000):
+                 float_tolerance=None, digit=None):
         from .mesh import MeshTrellis
 
         if mesh is None:
@@ -613,7 +621,7 @@ class _NestGrid(_Grid):
     here.  Queries run on the same GPU path as the trellis."""
 
     def __init__(self, bz: BrillouinZone, max_volume, max_branchings=5, *, mesh=None, device=0,
-                 float_tolerance=1e-12, digit=1000):
+                 float_tolerance=None, digit=None):
         from .mesh import MeshTrellis
 
         if isinstance(max_volume, (int, np.integer)) and not isinstance(max_volume, bool):

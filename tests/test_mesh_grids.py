@@ -197,3 +197,25 @@ def test_trellis_accessors():
     assert np.allclose(g.outer_rlu @ bz.lattice.B, g.outer_invA)
     with pytest.raises(ValueError):
         BZTrellisQdc(bz, 0.0)
+
+
+def test_approx_config():
+    """ApproxConfig and the global tolerances (wrap/_approx.cpp:7-40) reach
+    the grid's device tables."""
+    import brille_gb300 as b
+    from brille_gb300.grid import BZTrellisQdd
+
+    c = b.ApproxConfig()
+    assert (c.digits, c.real_space_tolerance, c.reciprocal_space_tolerance) == (1000, 1e-10, 1e-10)
+    bz = _bz("diamond2")
+    g = BZTrellisQdd(bz, bz.ir_volume / 50, False, b.ApproxConfig(100, 1e-9, 1e-8))
+    assert g.tables["float_tolerance"] == 1e-8 and g.tables["digit"] == 100
+    assert b.reciprocal_space_tolerance() == 1e-12
+    b.reciprocal_space_tolerance(3e-12)
+    try:
+        g2 = BZTrellisQdd(bz, bz.ir_volume / 50)
+        assert g2.tables["float_tolerance"] == 3e-12 and g2.tables["digit"] == 1000
+    finally:
+        b.reciprocal_space_tolerance(1e-12)
+    with pytest.raises(ValueError):
+        b.ApproxConfig(0)
