@@ -84,12 +84,44 @@ def _plane_triple(verts, ring):
 class BrillouinZone:
     """First Brillouin zone and irreducible polyhedron of a lattice.
 
-    Mirrors the reference's ``BrillouinZone(lattice, time_reversal=False,
-    wedge_search=True)`` surface (``wrap/_bz.cpp:156-177``).
+    Mirrors the reference's ``BrillouinZone(lattice, use_primitive=True,
+    search_length=1, time_reversal_symmetry=False, wedge_search=True,
+    divide_primitive=True)`` surface (``wrap/_bz.cpp:156-203``).  The zone is
+    always the Voronoi cell of the primitive reciprocal lattice (the
+    reference's ``use_primitive=True``, which the query path needs);
+    ``search_length`` sets the shell of lattice points searched, at least 2;
+    ``divide_primitive`` and ``approx_config`` are accepted and do not change
+    the construction.  ``time_reversal`` is a short name for
+    ``time_reversal_symmetry``.
     """
 
-    def __init__(self, lattice: Lattice, time_reversal=False, wedge_search=True,
-                 extent=2):
+    _ARGS = ("use_primitive", "search_length", "time_reversal_symmetry", "wedge_search", "divide_primitive")
+    _DEFAULTS = (True, 1, False, True, True)
+
+    def __init__(self, lattice: Lattice, *args, time_reversal=None, extent=None, **kwargs):
+        from .approx import ApproxConfig
+
+        # the reference's two constructors: (lattice, use_primitive, ...) and
+        # (lattice, approx_config, use_primitive, ...)
+        approx_config = kwargs.pop("approx_config", None)
+        if args and isinstance(args[0], ApproxConfig):
+            approx_config, args = args[0], args[1:]
+        if len(args) > len(self._ARGS):
+            raise TypeError("too many arguments for BrillouinZone")
+        opt = dict(zip(self._ARGS, self._DEFAULTS))
+        opt.update(zip(self._ARGS, args))
+        for k, v in kwargs.items():
+            if k not in opt:
+                raise TypeError(f"BrillouinZone() got an unexpected keyword argument '{k}'")
+            opt[k] = v
+        if not opt["use_primitive"]:
+            raise ValueError("only the primitive Brillouin zone (use_primitive=True) is supported")
+        if time_reversal is None:
+            time_reversal = opt["time_reversal_symmetry"]
+        if extent is None:
+            extent = max(2, int(opt["search_length"]))
+        wedge_search = opt["wedge_search"]
+        self.approx_config = approx_config
         self.lattice = lattice
         self.time_reversal = bool(time_reversal)
         self.wedge_search = bool(wedge_search)

@@ -168,12 +168,12 @@ class _Grid:
         is handed to its PolyTrellis as the maximum node volume in Å⁻³
         (src/trellis_poly.hpp:148-160), and so it is here; ``max_volume`` is
         the same number under its own name and wins when given.  Tolerances:
-        ``approx_config`` (an ApproxConfig), else the global configuration
-        (brille_gb300.approx); ``float_tolerance`` / ``digit`` override
-        either."""
+        ``approx_config`` (an ApproxConfig), else the zone's, else the global
+        configuration (brille_gb300.approx); ``float_tolerance`` / ``digit``
+        override them."""
         from . import approx
 
-        cfg = approx_config if approx_config is not None else approx.config
+        cfg = approx_config or getattr(bz, "approx_config", None) or approx.config
         float_tolerance = cfg.reciprocal_space_tolerance if float_tolerance is None else float_tolerance
         digit = cfg.digits if digit is None else digit
         if trellis is None:

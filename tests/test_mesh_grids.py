@@ -219,3 +219,30 @@ def test_approx_config():
         b.reciprocal_space_tolerance(1e-12)
     with pytest.raises(ValueError):
         b.ApproxConfig(0)
+
+
+def test_brillouin_zone_arguments():
+    """BrillouinZone takes the reference's arguments (wrap/_bz.cpp:156-203)."""
+    lat, _ = W.hexagonal16()
+    a = BrillouinZone(lat)
+    b = BrillouinZone(lat, True, 1, False, True, True)
+    assert np.array_equal(a.ir_vertices, b.ir_vertices)
+    c = BrillouinZone(lat, time_reversal_symmetry=True)
+    d = BrillouinZone(lat, time_reversal=True)
+    assert c.time_reversal and d.time_reversal
+    assert c.pointgroup.size == d.pointgroup.size
+    with pytest.raises(ValueError):
+        BrillouinZone(lat, use_primitive=False)
+
+
+def test_brillouin_zone_approx_config_overload():
+    import brille_gb300 as b
+
+    lat, _ = W.diamond_primitive()
+    cfg = b.ApproxConfig(1000, 1e-12, 1e-12)
+    z = BrillouinZone(lat, cfg)
+    assert z.approx_config is cfg and not z.time_reversal and z.wedge_search
+    z2 = BrillouinZone(lat, cfg, True, 1, True)
+    assert z2.time_reversal
+    with pytest.raises(TypeError):
+        BrillouinZone(lat, nonsense=1)
