@@ -246,3 +246,28 @@ def test_brillouin_zone_approx_config_overload():
     assert z2.time_reversal
     with pytest.raises(TypeError):
         BrillouinZone(lat, nonsense=1)
+
+
+@pytest.mark.parametrize("kind", ["mesh", "nest"])
+@pytest.mark.parametrize("name", ["diamond2", "hex16"])
+def test_mesh_boundary_points_locate(kind, name):
+    """Points at the irreducible polyhedron's vertices, on its faces and
+    within 1e-9 r.l.u. of them locate without error (the trellis bar of
+    src/tests/trellis_test.cpp:351-372, on the mesh tables)."""
+    from brille_gb300.grid import BZMeshQdd, BZNestQdd
+
+    bz = _bz(name)
+    g = BZMeshQdd(bz, bz.ir_volume / 300) if kind == "mesh" else BZNestQdd(bz, 300)
+    rng = np.random.default_rng(8)
+    v = bz.ir_vertices
+    pts = [v]
+    for f in bz.ir_faces:
+        ring = v[list(f)]
+        w = rng.dirichlet(np.ones(len(ring)), 20)
+        pts.append(w @ ring)
+    x = np.concatenate(pts)
+    x = np.concatenate([x, x + rng.uniform(-1e-9, 1e-9, x.shape)])
+    Q = x @ np.linalg.inv(bz.lattice.B)
+    rec = Oracle(g.tables).move_locate(Q, ir=True)
+    assert (rec["status"] == 0).all()
+    assert np.allclose(rec["weight"].sum(axis=1), 1.0)
