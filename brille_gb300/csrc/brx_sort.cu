@@ -51,8 +51,7 @@ using namespace brx_detail;
 
 namespace {
 
-constexpr int kMaxSortWarps = 4;
-constexpr int kPairWarps = 4;
+constexpr int kPairWarps = 4;  // warps of a CTA that owns a pair with B ≥ 16
 constexpr unsigned kFull = 0xffffffffu;
 
 // one interpolator (values or vectors) as the cost kernel sees it
@@ -353,7 +352,7 @@ __device__ long long find_key(const long long* keys, long long n, long long key)
 // scheduler, so that the FP64 cost matrix keeps every FP64 pipe of the SM
 // fed); warp 0 then solves the assignment and writes both permutations.
 template <typename T>
-__global__ void __launch_bounds__(32 * kMaxSortWarps) sort_pairs_kernel(SortParams P) {
+__global__ void __launch_bounds__(32 * kPairWarps) sort_pairs_kernel(SortParams P) {
   extern __shared__ __align__(16) unsigned char region[];
   const int tid = threadIdx.x, lane = tid & 31;
   const int B = P.B;
