@@ -183,7 +183,8 @@ brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* ke
  * NULL for the defaults (functions 0, weights 1).  Costs are FP64 on the
  * stored data (FP32/BF16 storage: on the rounded data).  One vertex pair's
  * rows and cost matrix must fit one CTA's shared memory (about 40·B² bytes
- * for complex FP64 eigenvectors of B modes: B ≤ 76; FP32 storage: B ≤ 96).
+ * for phonon data, B modes of B complex elements: B ≤ 74 with FP64
+ * storage, B ≤ 95 with FP32 storage).
  * Synchronous on stream (NULL: the handle's stream).  Invalid keys or cost
  * codes are rejected before the old table is touched; a failure after that
  * (a reverse key missing, a cost matrix without a finite assignment) leaves
