@@ -82,6 +82,45 @@ def _elements(arr, el):
     return B, e, rot, lu
 
 
+_FILL_NAMES = ("values_data", "values_elements", "values_weights", "vectors_data", "vectors_elements",
+               "vectors_weights", "sort")
+
+
+def _fill_arguments(args, kwargs):
+    """The arguments of fill() by name.  Positional forms, as the reference
+    binds them: (values, elements), (values, elements, vectors, elements
+    [, sort]) and (values, elements, weights, vectors, elements, weights
+    [, sort]); keywords fill in or replace nothing twice."""
+    n = len(args)
+    if n in (0, 1, 2):
+        names = _FILL_NAMES[:n]
+    elif n in (3, 4, 5):
+        names = ("values_data", "values_elements", "vectors_data", "vectors_elements", "sort")[:n]
+    elif n in (6, 7):
+        names = _FILL_NAMES[:n]
+    else:
+        raise TypeError("fill() takes at most 7 positional arguments")
+    if n == 3:
+        raise TypeError("fill() needs the vectors' elements with the vectors")
+    out = dict(zip(names, args))
+    for k, v in kwargs.items():
+        if k not in _FILL_NAMES:
+            raise TypeError(f"fill() got an unexpected keyword argument '{k}'")
+        if k in out:
+            raise TypeError(f"fill() got multiple values for argument '{k}'")
+        out[k] = v
+    if "values_data" not in out or "values_elements" not in out:
+        raise TypeError("fill() needs values_data and values_elements")
+    if ("vectors_data" in out) != ("vectors_elements" in out):
+        raise TypeError("fill() needs vectors_data and vectors_elements together")
+    out.setdefault("values_weights", (1.0, 1.0, 1.0))
+    out.setdefault("vectors_weights", (1.0, 1.0, 1.0))
+    out.setdefault("vectors_data", None)
+    out.setdefault("vectors_elements", None)
+    out["sort"] = bool(out.get("sort", False))
+    return out
+
+
 def _cost_fns(el):
     """(scalar, vector) cost-function codes of an elements vector: entries 5
     and 6, default 0 (wrap/_interpolator.hpp:95-98)."""
@@ -284,25 +323,15 @@ class _Grid:
             pass
 
     # ----------------------------------------------------------------- fill
-    def fill(self, values, values_elements, *args, sort=None, storage="f64"):
-        """fill(values, values_elements[, values_weights], vectors,
-        vectors_elements[, vectors_weights][, sort])
-        (wrap/_common_grid.hpp:26-47, 127-147)."""
-        values_weights = vectors_weights = (1.0, 1.0, 1.0)
-        vectors = vectors_elements = None
-        if len(args) >= 4:
-            values_weights, vectors, vectors_elements, vectors_weights = args[:4]
-            rest = args[4:]
-        elif len(args) >= 2:
-            vectors, vectors_elements = args[:2]
-            rest = args[2:]
-        elif len(args) == 0:
-            rest = ()
-        else:
-            raise TypeError("fill() takes values and vectors with their element specifications")
-        if sort is not None and rest:
-            raise TypeError("fill() got multiple values for argument 'sort'")
-        sort = bool(rest[0]) if rest else bool(sort)
+    def fill(self, *args, storage="f64", **kwargs):
+        """fill(values_data, values_elements[, values_weights], vectors_data,
+        vectors_elements[, vectors_weights][, sort]), positionally or by the
+        reference's keyword names (wrap/_common_grid.hpp:26-47, 127-147); the
+        vectors may be left out for values-only data."""
+        a = _fill_arguments(args, kwargs)
+        values, values_elements, values_weights = a["values_data"], a["values_elements"], a["values_weights"]
+        vectors, vectors_elements, vectors_weights = a["vectors_data"], a["vectors_elements"], a["vectors_weights"]
+        sort = a["sort"]
         vdt = np.complex128 if self.VALUE_COMPLEX else np.float64
         cdt = np.complex128 if self.VECTOR_COMPLEX else np.float64
         vals = _as_data(values, vdt)

@@ -271,3 +271,26 @@ def test_mesh_boundary_points_locate(kind, name):
     rec = Oracle(g.tables).move_locate(Q, ir=True)
     assert (rec["status"] == 0).all()
     assert np.allclose(rec["weight"].sum(axis=1), 1.0)
+
+
+def test_fill_arguments():
+    """fill() takes the reference's positional forms and keyword names
+    (wrap/_common_grid.hpp:26-47, 127-147)."""
+    from brille_gb300.grid import _fill_arguments as fa
+
+    a = fa(("v", "ve", "c", "ce"), {})
+    assert (a["vectors_data"], a["vectors_elements"], a["sort"]) == ("c", "ce", False)
+    a = fa(("v", "ve", "c", "ce", True), {})
+    assert a["sort"] is True
+    a = fa(("v", "ve", "vw", "c", "ce", "cw", True), {})
+    assert (a["values_weights"], a["vectors_weights"], a["sort"]) == ("vw", "cw", True)
+    a = fa((), dict(values_data="v", values_elements="ve", vectors_data="c", vectors_elements="ce", sort=1))
+    assert a["vectors_data"] == "c" and a["sort"] is True
+    a = fa(("v", "ve"), {})
+    assert a["vectors_data"] is None
+    a = fa(("v", "ve", "c", "ce"), dict(sort=True, values_weights=(2, 1, 1)))
+    assert a["sort"] and a["values_weights"] == (2, 1, 1)
+    for args, kw in ((("v", "ve", "c"), {}), (("v", "ve", "c", "ce", True), dict(sort=True)),
+                     (("v",), {}), (("v", "ve"), dict(bogus=1)), (("v", "ve"), dict(vectors_data="c"))):
+        with pytest.raises(TypeError):
+            fa(args, kw)
