@@ -231,12 +231,40 @@ class Lattice:
     ``Lattice(((a, b, c), (alpha, beta, gamma)))``.
     """
 
-    def __init__(self, vectors, symmetry: Symmetry | None = None, basis: Basis | None = None):
+    def __init__(self, vectors, symmetry: Symmetry | None = None, basis: Basis | None = None, *,
+                 spacegroup=None, real_space=True, row_vectors=True):
+        """Also the reference's Python forms (brille/lattice.py:10-120):
+        ``values`` as (lengths, angles) — angles in radians when none
+        exceeds π, else degrees — or basis vectors (``row_vectors``);
+        ``spacegroup`` by name (str) as the second positional argument or
+        by keyword; ``symmetry`` as (rotations, translations) and ``basis``
+        as (positions, types) tuples; ``real_space=False`` for reciprocal
+        lattice parameters (Å⁻¹)."""
+        if isinstance(symmetry, str):
+            spacegroup, symmetry = symmetry, None
+        if spacegroup is not None:
+            if symmetry is not None:
+                raise ValueError("give either a spacegroup or a symmetry, not both")
+            symmetry = spacegroup_by_name(spacegroup)
+        if symmetry is not None and not isinstance(symmetry, Symmetry):
+            W, w = symmetry
+            symmetry = Symmetry(np.asarray(W, dtype=np.int32).reshape(-1, 3, 3), np.asarray(w, float).reshape(-1, 3))
+        if basis is not None and not isinstance(basis, Basis):
+            basis = Basis(*basis) if isinstance(basis, (tuple, list)) and len(basis) == 2 else Basis(basis)
         arr = vectors
+        if isinstance(arr, (tuple, list)) and len(arr) == 1:
+            arr = arr[0]
         if isinstance(arr, (tuple, list)) and len(arr) == 2 and np.size(arr[0]) == 3 and np.size(arr[1]) == 3:
-            A = _lattice_matrix(arr[0], arr[1])
+            angles = np.asarray(arr[1], dtype=float)
+            if not (angles > np.pi).any():
+                angles = np.degrees(angles)
+            A = _lattice_matrix(arr[0], angles)
         else:
             A = np.asarray(arr, dtype=float).reshape(3, 3)
+            if not row_vectors:
+                A = A.T
+        if not real_space:
+            A = TWO_PI * np.linalg.inv(A).T  # the given rows are the reciprocal basis
         self.A = A
         self.B = TWO_PI * np.linalg.inv(A).T
         if symmetry is None:
@@ -317,6 +345,19 @@ LATTICE_SYSTEM = {
     "P4/mmm": "tetragonal", "R-3m": "hexagonal", "P6/mmm": "hexagonal",
     "P6_3/mmc": "hexagonal", "Fm-3m": "cubic", "Im-3m": "cubic", "Fd-3m": "cubic",
 }
+
+
+def spacegroup_by_name(name) -> Symmetry:
+    """A space group of the table below by its International Tables name
+    (spaces and underscores ignored); "P1" is the identity alone."""
+    key = str(name).replace(" ", "")
+    if key in ("P1", "1"):
+        return Symmetry(np.eye(3, dtype=np.int32)[None], np.zeros((1, 3)))
+    for k in SPACEGROUPS:
+        if k.replace("_", "") == key.replace("_", ""):
+            return spacegroup(k)
+    raise ValueError(f"space group {name!r} is not in this package's table ({', '.join(sorted(SPACEGROUPS))}, P1); "
+                     "give the symmetry operations instead")
 
 
 def spacegroup(name) -> Symmetry:

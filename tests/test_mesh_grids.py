@@ -294,3 +294,23 @@ def test_fill_arguments():
                      (("v",), {}), (("v", "ve"), dict(bogus=1)), (("v", "ve"), dict(vectors_data="c"))):
         with pytest.raises(TypeError):
             fa(args, kw)
+
+
+def test_lattice_reference_forms():
+    """The reference's Python Lattice forms (brille/lattice.py:10-120)."""
+    from brille_gb300.crystal import Basis, Lattice, spacegroup
+
+    a = Lattice(((2.87,) * 3, (90, 90, 90)), symmetry=spacegroup("Im-3m"))
+    b = Lattice(((2.87,) * 3, np.pi / 2 * np.ones(3)), spacegroup="Im-3m")   # radians, by keyword
+    c = Lattice(((2.87,) * 3, (90, 90, 90)), "Im-3m")                       # by position
+    for x in (b, c):
+        assert np.allclose(x.A, a.A) and x.pointgroup.size == a.pointgroup.size
+    r = Lattice(((1, 1, 1), (90, 90, 90)), real_space=False)
+    assert np.allclose(r.B, np.eye(3))
+    h = Lattice(((3.2, 3.2, 5.2), (90, 90, 120)), spacegroup="P 6_3/m m c")
+    assert h.pointgroup.size == 24
+    s = Lattice(np.diag([3.0, 4.0, 5.0]), symmetry=(np.eye(3, dtype=int)[None], np.zeros((1, 3))),
+                basis=([[0, 0, 0]], [0]))
+    assert isinstance(s.basis, Basis) and s.pointgroup.size == 1
+    with pytest.raises(ValueError):
+        Lattice(((3,) * 3, (90,) * 3), spacegroup="Ia-3d")
