@@ -66,3 +66,32 @@ def test_create_rejects_bad_geometry():
     assert st == 1 and not h.value
     st = load().brx_create(None, 0, C.byref(h))
     assert st == 1
+
+
+def test_header_is_strict_c(tmp_path):
+    """include/brx.h compiles as strict C99 and C++17 with every warning an
+    error, and a C program links against libbrx.so and calls it (no GPU
+    work: the ABI version and a rejected geometry)."""
+    from brille_gb300._lib import LIB_PATH
+
+    load()
+    src = tmp_path / "consumer.c"
+    src.write_text(f"""#include "{HEADER}"
+#include <stdio.h>
+int main(void) {{
+  brx_handle* h = 0;
+  brx_status st = brx_create(0, 0, &h);
+  printf("%d %d\\n", (int)brx_abi_version(), (int)st);
+  return st == BRX_ERR_INVALID_ARGUMENT && h == 0 ? 0 : 1;
+}}
+""")
+    exe = tmp_path / "consumer"
+    lib_dir = os.path.dirname(LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", str(src), "-o", str(exe),
+                    "-L" + lib_dir, "-lbrx", "-Wl,-rpath," + lib_dir], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["1", "1"]
+    cpp = tmp_path / "consumer.cpp"
+    cpp.write_text(f'#include "{HEADER}"\nint main() {{ return brx_abi_version() == BRX_ABI_VERSION ? 0 : 1; }}\n')
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", str(cpp)],
+                   check=True)
