@@ -24,8 +24,8 @@ from the knots, then the first listed tetrahedron that contains q).
 
 The mesh: Delaunay tetrahedralisation (Qhull) of the polyhedron's vertices,
 refined by inserting a point into every tetrahedron larger than the maximum
-volume (its circumcentre where that lies well inside, else its centroid)
-until none is (or ``max_points`` is reached).  The polyhedron is convex, so
+volume (its circumcentre where that lies well inside, its projection onto
+the boundary where it lies outside, else its centroid) until none is (or ``max_points`` is reached).  The polyhedron is convex, so
 the Delaunay mesh of points inside it covers it exactly.  It is not the
 reference's TetGen mesh: grids built here are compared with the oracle on
 the same tables.
@@ -54,9 +54,10 @@ def delaunay_mesh(points, max_volume=-1.0, max_points=-1, max_rounds=200):
     tetrahedron positively oriented and, when max_volume > 0, no larger than
     max_volume (unless max_points stops the refinement first).  Refinement
     inserts the circumcentre of each tetrahedron above the limit where it
-    lies well inside the hull and not next to an existing point (Delaunay
-    refinement, which removes the worst-shaped tetrahedra first), else its
-    centroid."""
+    lies well inside the hull (Delaunay refinement, which removes the
+    worst-shaped tetrahedra first), its projection onto the hull face it
+    crosses where that lies on the hull, and its centroid otherwise; never a
+    point next to an existing one."""
     from scipy.spatial import ConvexHull, cKDTree
 
     p = np.unique(np.asarray(points, float), axis=0)
@@ -85,9 +86,16 @@ def delaunay_mesh(points, max_volume=-1.0, max_points=-1, max_rounds=200):
         new = q.mean(axis=1)
         cc, ok = _circumcentres(q)
         edge = np.cbrt(vol[big])
-        ok &= np.all(cc @ eq[:, :3].T + eq[:, 3] < -0.25 * edge[:, None], axis=1)
-        ok &= cKDTree(p).query(cc)[0] > 0.5 * edge
-        new[ok] = cc[ok]
+        d = cc @ eq[:, :3].T + eq[:, 3]  # signed distances to the hull planes, < 0 inside
+        inside = np.all(d < -0.25 * edge[:, None], axis=1)
+        # a circumcentre outside or next to the boundary goes onto the plane
+        # it violates most, when that point lies on the hull
+        f = np.argmax(d, axis=1)
+        proj = cc - d[np.arange(len(cc)), f][:, None] * eq[f, :3]
+        on_face = ~inside & np.all(proj @ eq[:, :3].T + eq[:, 3] < 1e-12 * span, axis=1)
+        cand = np.where(inside[:, None], cc, proj)
+        use = ok & (inside | on_face) & (cKDTree(p).query(cand)[0] > 0.5 * edge)
+        new[use] = cand[use]
         new = new[np.unique(np.round(new / (1e-6 * span)), axis=0, return_index=True)[1]]
         p = np.vstack([p, new])
     return p, s.astype(np.int32), vol
