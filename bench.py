@@ -66,7 +66,7 @@ def build_workload(name):
     lat, masses = getattr(W, builder)()
     bz = BrillouinZone(lat)
     t = time.time()
-    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * fraction)
+    tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * fraction)
     log(f"[setup] trellis {tr.summary()} in {time.time() - t:.1f}s")
     model = W.bvk_for(lat, masses)
     qv = tr.vertices @ np.linalg.inv(lat.B)
@@ -308,12 +308,12 @@ def _batch_item(k, seed, vmin, vmax):
     lat, _ = W.random_crystal(name, int(rng.integers(1, 7)), seed=seed, max_atoms=32)
     bz = BrillouinZone(lat)
     target = float(np.exp(rng.uniform(np.log(vmin), np.log(vmax))))
-    ratio = bz.volume / ConvexHull(bz.ir_vertices).volume
+    ratio = bz.volume / ConvexHull(bz.ir_vertices_invA).volume
     frac = 4.0 / (ratio * target)
-    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac)
+    tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * frac)
     # one correction: vertex count scales about as 1/node volume
     if not 0.67 < len(tr.vertices) / target < 1.5:
-        tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac * len(tr.vertices) / target)
+        tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * frac * len(tr.vertices) / target)
     return name, lat, tr
 
 
@@ -602,7 +602,7 @@ def run_learned(args):
     dev = torch.device("cuda")
 
     def grid_at(frac):
-        tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * frac)
+        tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * frac)
         g = BZTrellisQdd(bz, trellis=tr)
         g.fill(model.frequencies(tr.vertices @ Binv)[:, :, None], [1, 0, 0, 0, 3], storage="f32")
         return g

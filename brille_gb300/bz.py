@@ -140,7 +140,7 @@ class BrillouinZone:
         hs = np.hstack([G, -0.5 * np.sum(G * G, axis=1)[:, None]])
         verts, faces = _polytope(hs, np.zeros(3))
         keep = [i for i, f in enumerate(faces) if len(f) >= 3]
-        self.vertices = verts
+        self.vertices_invA = verts
         self.face_tau = ns[keep].astype(np.int32)
         Gk = G[keep]
         self.face_tau_len = np.linalg.norm(Gk, axis=1)
@@ -194,7 +194,7 @@ class BrillouinZone:
         else:
             interior = np.zeros(3)
         verts, faces = _polytope(hs, interior)
-        self.ir_vertices = verts
+        self.ir_vertices_invA = verts
         self.ir_halfspaces = hs
         self.ir_faces = [f for f in faces if len(f) >= 3]
 
@@ -209,6 +209,50 @@ class BrillouinZone:
             out.append(o.min() > -1e-12)
         return np.array(out)
 
+    # ------------------------------------------------- reference accessors
+    def _rlu(self, xyz):
+        return np.asarray(xyz) @ np.linalg.inv(self.lattice.B)
+
+    @property
+    def vertices(self):
+        """First-zone vertices in r.l.u. (wrap/_bz.cpp:267-271); Å⁻¹ in
+        ``vertices_invA``."""
+        return self._rlu(self.vertices_invA)
+
+    @property
+    def ir_vertices(self):
+        """Irreducible-polyhedron vertices in r.l.u. (wrap/_bz.cpp:334-338);
+        Å⁻¹ in ``ir_vertices_invA``."""
+        return self._rlu(self.ir_vertices_invA)
+
+    @property
+    def wedge_normals(self):
+        """Wedge plane normals in r.l.u. components (wrap/_bz.cpp:361-365);
+        Cartesian in ``wedge_normals_invA``."""
+        return self._rlu(self.wedge_normal)
+
+    @property
+    def wedge_normals_invA(self):
+        return self.wedge_normal.copy()
+
+    @property
+    def normals_invA(self):
+        """Outward unit normals of the first zone's faces (Å⁻¹)."""
+        return self.face_normal.copy()
+
+    @property
+    def normals(self):
+        return self._rlu(self.face_normal)
+
+    @property
+    def points_invA(self):
+        """Centre of each face: half its reciprocal lattice vector (Å⁻¹)."""
+        return 0.5 * self.face_normal * self.face_tau_len[:, None]
+
+    @property
+    def points(self):
+        return self._rlu(self.points_invA)
+
     # ------------------------------------------------- moves, on the GPU
     def _mover(self):
         """A query handle whose trellis is the irreducible polyhedron alone:
@@ -217,7 +261,7 @@ class BrillouinZone:
             from .grid import BZTrellisQdd
             from .trellis import PointTrellis
 
-            self._move_grid = BZTrellisQdd(self, trellis=PointTrellis(self.ir_vertices))
+            self._move_grid = BZTrellisQdd(self, trellis=PointTrellis(self.ir_vertices_invA))
         return self._move_grid
 
     def _move(self, Q, ir, message):
@@ -257,4 +301,4 @@ class BrillouinZone:
     @property
     def ir_volume(self):
         from scipy.spatial import ConvexHull
-        return ConvexHull(self.ir_vertices).volume
+        return ConvexHull(self.ir_vertices_invA).volume

@@ -219,7 +219,7 @@ class _Grid:
             vol = float(node_volume_fraction if max_volume is None else max_volume)
             if not vol > 0:
                 raise ValueError("the maximum node volume must be positive")
-            trellis = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, vol, always_triangulate)
+            trellis = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, vol, always_triangulate)
         self.bz = bz
         self.trellis = trellis
         self.tables = geometry_tables(bz, trellis, gamma=True, float_tolerance=float_tolerance, digit=digit)
@@ -631,7 +631,7 @@ class _MeshGrid(_Grid):
         from .mesh import MeshTrellis
 
         if mesh is None:
-            mesh = MeshTrellis(bz.ir_vertices, float(max_size), int(max_points))
+            mesh = MeshTrellis(bz.ir_vertices_invA, float(max_size), int(max_points))
         self.num_levels = int(num_levels)
         super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
 
@@ -660,7 +660,7 @@ class _NestGrid(_Grid):
         else:
             vol = float(max_volume)
         if mesh is None:
-            mesh = MeshTrellis(bz.ir_vertices, vol)
+            mesh = MeshTrellis(bz.ir_vertices_invA, vol)
         self.max_branchings = int(max_branchings)
         super().__init__(bz, trellis=mesh, device=device, float_tolerance=float_tolerance, digit=digit)
 

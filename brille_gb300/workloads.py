@@ -128,7 +128,7 @@ def grid_for(lat, max_volume_fraction, masses=None, time_reversal=False):
     from .trellis import TrellisBuild
 
     bz = BrillouinZone(lat, time_reversal=time_reversal)
-    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * max_volume_fraction)
+    tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * max_volume_fraction)
     return bz, tr
 
 
@@ -161,11 +161,11 @@ def near_boundary_q(bz, tr, n, delta=1e-6, seed=0):
         x[np.arange(k), axis] = np.where(rng.uniform(size=(k, 1)) < 0.5, lo, hi)[np.arange(k), axis]
         parts.append(x)
     # edges of the irreducible polyhedron (high-symmetry lines)
-    edges = _poly_edges(bz.ir_vertices, bz.ir_halfspaces, 1e-9 * np.abs(bz.ir_vertices).max())
+    edges = _poly_edges(bz.ir_vertices_invA, bz.ir_halfspaces, 1e-9 * np.abs(bz.ir_vertices_invA).max())
     m = n - sum(len(p) for p in parts)
     e = edges[rng.integers(0, len(edges), m)]
     s = rng.uniform(size=(m, 1))
-    parts.append(bz.ir_vertices[e[:, 0]] * (1 - s) + bz.ir_vertices[e[:, 1]] * s)
+    parts.append(bz.ir_vertices_invA[e[:, 0]] * (1 - s) + bz.ir_vertices_invA[e[:, 1]] * s)
     q = np.concatenate(parts) @ Binv
     q += rng.uniform(-delta, delta, size=q.shape)
     W = bz.pointgroup.W[rng.integers(0, bz.pointgroup.size, len(q))]

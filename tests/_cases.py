@@ -40,7 +40,7 @@ CRYSTALS = {
 def crystal_case(name, fraction=1 / 2000, always_triangulate=False):
     lat, masses = CRYSTALS[name]() if name in CRYSTALS else W.random_crystal(name, 2, seed=3)
     bz = BrillouinZone(lat)
-    tr = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume * fraction, always_triangulate)
+    tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * fraction, always_triangulate)
     t = geometry_tables(bz, tr)
     model = W.bvk_for(lat, masses)
     qv = tr.vertices @ np.linalg.inv(lat.B)

@@ -97,7 +97,7 @@ def test_nb_vector_field_nest_known_answer_gpu():
     g = BZNestQdd(bz, 0.01, 5)
     xyz = g.trellis.vertices
     rng = np.random.default_rng(11)
-    lo, hi = bz.ir_vertices.min(axis=0), bz.ir_vertices.max(axis=0)
+    lo, hi = bz.ir_vertices_invA.min(axis=0), bz.ir_vertices_invA.max(axis=0)
     x = rng.uniform(lo, hi, (20000, 3))
     hs = bz.ir_halfspaces
     x = x[np.all(x @ hs[:, :3].T + hs[:, 3] < -1e-6, axis=1)][:200]
@@ -119,7 +119,7 @@ def test_nb_vector_field_along_face_gpu():
     bz = BrillouinZone(lat)
     g = BZNestQdd(bz, 0.01)
     xyz = g.trellis.vertices
-    rlu = bz.ir_vertices @ np.linalg.inv(lat.B)
+    rlu = bz.ir_vertices_invA @ np.linalg.inv(lat.B)
     v_min, v_del = rlu.min(axis=0), rlu.max(axis=0) - rlu.min(axis=0)
     Q = np.array([v_min + v_del * (i + 1) * (0.64 / 99) for i in range(99)])
     g.fill(np.ones(len(xyz)), [1, 0, 0, 0, 3], np.ascontiguousarray(xyz[:, None, :]), [0, 3, 0, 0, 4])

@@ -30,7 +30,7 @@ def _bz(name):
 def test_mesh_covers_polyhedron(name):
     bz = _bz(name)
     vmax = bz.ir_volume / 400
-    m = MeshTrellis(bz.ir_vertices, vmax)
+    m = MeshTrellis(bz.ir_vertices_invA, vmax)
     T, v = m.mesh_tetrahedra, m.vertices
     q = v[T]
     o = np.einsum("ij,ij->i", q[:, 0] - q[:, 3], np.cross(q[:, 1] - q[:, 3], q[:, 2] - q[:, 3]))
@@ -45,16 +45,16 @@ def test_mesh_covers_polyhedron(name):
 
 def test_max_points_stops_refinement():
     bz = _bz("diamond2")
-    v, t, vol = delaunay_mesh(bz.ir_vertices, bz.ir_volume / 5000, max_points=200)
+    v, t, vol = delaunay_mesh(bz.ir_vertices_invA, bz.ir_volume / 5000, max_points=200)
     assert len(v) <= 200 + len(t)  # the last round may add up to one point per tetrahedron it split
-    v2, _, _ = delaunay_mesh(bz.ir_vertices, -1)
-    assert len(v2) == len(np.unique(bz.ir_vertices, axis=0))
+    v2, _, _ = delaunay_mesh(bz.ir_vertices_invA, -1)
+    assert len(v2) == len(np.unique(bz.ir_vertices_invA, axis=0))
 
 
 @pytest.mark.parametrize("name", ["diamond2", "hex16"])
 def test_oracle_locates_every_point(name):
     bz = _bz(name)
-    m = MeshTrellis(bz.ir_vertices, bz.ir_volume / 300)
+    m = MeshTrellis(bz.ir_vertices_invA, bz.ir_volume / 300)
     t = geometry_tables(bz, m)
     rng = np.random.default_rng(3)
     Q = rng.uniform(-1.5, 1.5, (3000, 3))
@@ -108,7 +108,7 @@ def test_nest_density_and_volume():
 
 def test_mesh_permutation_keys():
     bz = _bz("diamond2")
-    m = MeshTrellis(bz.ir_vertices, bz.ir_volume / 100)
+    m = MeshTrellis(bz.ir_vertices_invA, bz.ir_volume / 100)
     n = len(m.vertices)
     want = set()
     for tet in m.mesh_tetrahedra:
@@ -138,7 +138,7 @@ def test_nb_vector_field_nest_known_answer(cls):
     rng = np.random.default_rng(11)
     # random points of the irreducible polyhedron (rejection from its box),
     # kept off its surface so that rounding cannot move them out
-    lo, hi = bz.ir_vertices.min(axis=0), bz.ir_vertices.max(axis=0)
+    lo, hi = bz.ir_vertices_invA.min(axis=0), bz.ir_vertices_invA.max(axis=0)
     x = rng.uniform(lo, hi, (20000, 3))
     hs = bz.ir_halfspaces
     inside = np.all(x @ hs[:, :3].T + hs[:, 3] < -1e-6, axis=1)
@@ -166,7 +166,7 @@ def test_nb_vector_field_along_face(cls):
     bz = BrillouinZone(lat)
     g = BZNestQdd(bz, 0.01) if cls == "nest" else BZMeshQdd(bz, 0.01)
     xyz = g.trellis.vertices
-    rlu = bz.ir_vertices @ np.linalg.inv(lat.B)
+    rlu = bz.ir_vertices_invA @ np.linalg.inv(lat.B)
     v_min, v_del = rlu.min(axis=0), rlu.max(axis=0) - rlu.min(axis=0)
     step = 0.64 / 99
     Q = np.array([v_min + v_del * (i + 1) * step for i in range(99)])
@@ -226,7 +226,7 @@ def test_brillouin_zone_arguments():
     lat, _ = W.hexagonal16()
     a = BrillouinZone(lat)
     b = BrillouinZone(lat, True, 1, False, True, True)
-    assert np.array_equal(a.ir_vertices, b.ir_vertices)
+    assert np.array_equal(a.ir_vertices_invA, b.ir_vertices_invA)
     c = BrillouinZone(lat, time_reversal_symmetry=True)
     d = BrillouinZone(lat, time_reversal=True)
     assert c.time_reversal and d.time_reversal
@@ -259,7 +259,7 @@ def test_mesh_boundary_points_locate(kind, name):
     bz = _bz(name)
     g = BZMeshQdd(bz, bz.ir_volume / 300) if kind == "mesh" else BZNestQdd(bz, 300)
     rng = np.random.default_rng(8)
-    v = bz.ir_vertices
+    v = bz.ir_vertices_invA
     pts = [v]
     for f in bz.ir_faces:
         ring = v[list(f)]
@@ -314,3 +314,16 @@ def test_lattice_reference_forms():
     assert isinstance(s.basis, Basis) and s.pointgroup.size == 1
     with pytest.raises(ValueError):
         Lattice(((3,) * 3, (90,) * 3), spacegroup="Ia-3d")
+
+
+def test_brillouin_zone_accessors():
+    """Reference units: vertices in r.l.u., *_invA in Å⁻¹ (wrap/_bz.cpp:237-372)."""
+    bz = _bz("hex16")
+    B = bz.lattice.B
+    assert np.allclose(bz.ir_vertices @ B, bz.ir_vertices_invA)
+    assert np.allclose(bz.vertices @ B, bz.vertices_invA)
+    assert np.allclose(bz.points @ B, bz.points_invA)
+    assert np.allclose(np.linalg.norm(bz.normals_invA, axis=1), 1)
+    assert np.allclose(bz.wedge_normals @ B, bz.wedge_normals_invA)
+    # the face centres are on the faces: n·p = |τ|/2
+    assert np.allclose(np.einsum("ij,ij->i", bz.normals_invA, bz.points_invA), bz.face_tau_len / 2)

@@ -15,7 +15,7 @@ def _bz():
 
 def test_save_load_roundtrip(tmp_path):
     bz = _bz()
-    t = TrellisBuild(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 500)
+    t = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 500)
     p = tmp_path / "t.npz"
     t.save(p)
     u = TrellisBuild.load(p)
@@ -29,16 +29,16 @@ def test_save_load_roundtrip(tmp_path):
 def test_cache_builds_once_and_checks_inputs(tmp_path):
     bz = _bz()
     p = tmp_path / "c.npz"
-    a = TrellisBuild.cached(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 300, p)
+    a = TrellisBuild.cached(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 300, p)
     mtime = p.stat().st_mtime_ns
-    b = TrellisBuild.cached(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 300, p)
+    b = TrellisBuild.cached(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 300, p)
     assert p.stat().st_mtime_ns == mtime  # loaded, not rebuilt
     assert np.array_equal(a.tet_vertices, b.tet_vertices)
     with pytest.raises(ValueError):
-        TrellisBuild.load(p, fingerprint=TrellisBuild.fingerprint(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 301))
-    TrellisBuild.cached(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 301, p)  # other inputs: rebuilt
-    fp_new = TrellisBuild.fingerprint(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 301)
-    fp_old = TrellisBuild.fingerprint(bz.ir_vertices, bz.ir_halfspaces, bz.volume / 300)
+        TrellisBuild.load(p, fingerprint=TrellisBuild.fingerprint(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 301))
+    TrellisBuild.cached(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 301, p)  # other inputs: rebuilt
+    fp_new = TrellisBuild.fingerprint(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 301)
+    fp_old = TrellisBuild.fingerprint(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 300)
     TrellisBuild.load(p, fingerprint=fp_new)
     with pytest.raises(ValueError):
         TrellisBuild.load(p, fingerprint=fp_old)
