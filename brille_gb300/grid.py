@@ -129,10 +129,38 @@ def _cost_fns(el):
 
 
 class NodeType(IntEnum):
-    """Trellis node types (src/enums.hpp:73; include/brx.h BRX_NODE_*)."""
-    null = 0
-    cube = 1
-    poly = 2
+    """Trellis node types with the reference's names and values
+    (src/enums.hpp:43, wrap/_enums.cpp:41-48); the tables store them as
+    BRX_NODE_NULL / CUBE / POLY (include/brx.h), see ``node_type``."""
+    assumed_null = 0
+    found_null = 1
+    null = 2
+    cube = 3
+    polygon = 4
+    poly = 4
+
+
+class RotatesLike(IntEnum):
+    """How vector data transform (src/rotates.hpp:27); the codes of fill's
+    elements[3]."""
+    vector = 0
+    pseudovector = 1
+    Gamma = 2
+
+
+class LengthUnit(IntEnum):
+    """Units of vector data (src/enums.hpp:37); the codes of fill's
+    elements[4]."""
+    none = 0
+    angstrom = 1
+    inverse_angstrom = 2
+    real_lattice = 3
+    reciprocal_lattice = 4
+
+
+def node_type(table_code):
+    """NodeType of a node-table code (BRX_NODE_NULL, _CUBE, _POLY)."""
+    return (NodeType.null, NodeType.cube, NodeType.polygon)[int(table_code)]
 
 
 def table_from_moved(keys, moved, perms, n_branches):
@@ -275,7 +303,7 @@ class _Grid:
     def all_node_types(self):
         """Type of every node in linear order i + nx(j + ny k)
         (wrap/_trellis.hpp:96-98)."""
-        return [NodeType(int(t)) for t in self.trellis.node_type]
+        return [node_type(t) for t in self.trellis.node_type]
 
     def node_at_type(self, subscript):
         """Type of the node at subscript (i, j, k) (wrap/_trellis.hpp:84-86)."""
@@ -283,7 +311,7 @@ class _Grid:
         i, j, k = (int(x) for x in subscript)
         if not (0 <= i < nx and 0 <= j < ny and 0 <= k < nz):
             raise IndexError(f"node subscript {subscript} outside {self.trellis.shape}")
-        return NodeType(int(self.trellis.node_type[i + nx * (j + ny * k)]))
+        return node_type(self.trellis.node_type[i + nx * (j + ny * k)])
 
     def node_containing_type(self, Q):
         """Type of the node whose cell holds each Q (r.l.u., not moved), as
@@ -293,7 +321,7 @@ class _Grid:
         node = rec["node"][:, 0]
         out = []
         for n in node:
-            out.append(NodeType(int(self.trellis.node_type[n])) if n >= 0 else NodeType.null)
+            out.append(node_type(self.trellis.node_type[n]) if n >= 0 else NodeType.null)
         return out
 
     @property

@@ -130,7 +130,7 @@ def test_nb_vector_field_along_face_gpu():
 def test_node_containing_type():
     """node_containing_type (wrap/_trellis.hpp:88-94) on a trellis and a mesh
     grid: the type of the node the oracle's locate finds for each point."""
-    from brille_gb300.grid import BZTrellisQdc, NodeType
+    from brille_gb300.grid import BZTrellisQdc, NodeType, node_type
 
     lat, _ = W.diamond_primitive()
     bz = BrillouinZone(lat)
@@ -138,6 +138,6 @@ def test_node_containing_type():
         Q = Oracle(g.tables).move(np.random.default_rng(3).uniform(-1, 1, (500, 3)), ir=True)[0]
         got = g.node_containing_type(Q)
         node = Oracle(g.tables).move_locate(Q, ir=False, no_move=True)["node"][:, 0]
-        want = [NodeType(int(g.trellis.node_type[n])) if n >= 0 else NodeType.null for n in node]
+        want = [node_type(g.trellis.node_type[n]) if n >= 0 else NodeType.null for n in node]
         assert got == want
         assert all(t != NodeType.null for t in got)

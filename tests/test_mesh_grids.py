@@ -181,7 +181,7 @@ def test_trellis_accessors():
     """The reference's BZTrellisQ accessors (wrap/_trellis.hpp:36-98):
     node_volume_fraction (the maximum node volume in Å⁻³), inner/outer
     vertices, node types."""
-    from brille_gb300.grid import BZTrellisQdc, NodeType
+    from brille_gb300.grid import BZTrellisQdc, node_type
 
     bz = _bz("diamond2")
     g = BZTrellisQdc(bz, node_volume_fraction=bz.ir_volume / 100)
@@ -190,7 +190,7 @@ def test_trellis_accessors():
     nx, ny, _ = t.shape
     for lin in (0, t.node_type.size // 2, t.node_type.size - 1):
         sub = (lin % nx, (lin // nx) % ny, lin // (nx * ny))
-        assert g.node_at_type(sub) == NodeType(int(t.node_type[lin]))
+        assert g.node_at_type(sub) == node_type(t.node_type[lin])
     with pytest.raises(IndexError):
         g.node_at_type(t.shape)
     assert set(map(tuple, g.inner_invA)) == set(map(tuple, t.vertices[np.unique(t.cube_vertices)]))
