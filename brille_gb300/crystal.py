@@ -20,7 +20,7 @@ Conventions follow the reference's public Python surface:
 from __future__ import annotations
 
 import itertools
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 

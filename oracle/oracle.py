@@ -11,7 +11,7 @@ import subprocess
 
 import numpy as np
 
-from brille_gb300._abi import BRX_C128, Data, GeometryHolder, make_data
+from brille_gb300._abi import GeometryHolder, make_data
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
