@@ -327,3 +327,27 @@ def test_brillouin_zone_accessors():
     assert np.allclose(bz.wedge_normals @ B, bz.wedge_normals_invA)
     # the face centres are on the faces: n·p = |τ|/2
     assert np.allclose(np.einsum("ij,ij->i", bz.normals_invA, bz.points_invA), bz.face_tau_len / 2)
+
+
+def test_create_bz_and_grid():
+    """create_bz / create_grid (brille/utils.py:63-356) argument forms."""
+    from brille_gb300 import grid as G
+    from brille_gb300.utils import create_bz, create_grid
+
+    a = create_bz(2.87, 2.87, 2.87, 90, 90, 90, "Im-3m")
+    b = create_bz([2.87] * 3, [90] * 3, "Im-3m")
+    c = create_bz(np.eye(3) * 2.87, "Im-3m")
+    d = create_bz(lens=[2.87] * 3, angs=[np.pi / 2] * 3, spacegroup="Im-3m")
+    for z in (b, c, d):
+        assert np.allclose(z.ir_vertices_invA, a.ir_vertices_invA)
+    r = create_bz([1, 1, 1], [90, 90, 90], "P1", is_reciprocal=True)
+    assert np.allclose(r.lattice.B, np.eye(3))
+    with pytest.raises(ValueError):
+        create_bz([2.87] * 3, [90] * 3)
+    g = create_grid(a, node_volume_fraction=a.ir_volume / 50)
+    assert type(g) is G.BZTrellisQdd
+    assert type(create_grid(a, complex_vectors=True, mesh=True, max_size=a.ir_volume / 20)) is G.BZMeshQdc
+    assert type(create_grid(a, True, True, nest=True, number_density=20)) is G.BZNestQcc
+    for kw in (dict(mesh=True, nest=True), dict(nest=True), dict(max_size=1.0), dict(nest=True, num_levels=2)):
+        with pytest.raises(ValueError):
+            create_grid(a, **kw)
