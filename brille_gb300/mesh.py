@@ -25,8 +25,9 @@ from the knots, then the first listed tetrahedron that contains q).
 The mesh: Delaunay tetrahedralisation (Qhull) of the polyhedron's vertices,
 refined by inserting a point into every tetrahedron larger than the maximum
 volume (its circumcentre where that lies well inside, its projection onto
-the boundary where it lies outside, else its centroid) until none is (or ``max_points`` is reached).  The polyhedron is convex, so
-the Delaunay mesh of points inside it covers it exactly.  It is not the
+the boundary where it lies outside, else its centroid) until none is (or
+``max_points`` is reached).  The polyhedron is convex, so the Delaunay mesh
+of points inside it covers it exactly.  It is not the
 reference's TetGen mesh: grids built here are compared with the oracle on
 the same tables.
 """
