@@ -212,7 +212,8 @@ __device__ __forceinline__ void store_group(Out* dst, const Acc* vr, const Acc* 
 // R⁻¹·M·R (axial).
 template <typename Acc, typename St, bool CPLX, typename Out>
 __device__ void matrix_item(const GatherParams& p, const St* s_Y, int rs, const Acc* s_e, const Acc* wj, const Acc* R,
-                            int ident, bool gamma, int pivot, int nslot, int MB, int b, int e0, Out* dst) {
+                            int ident, bool gamma, int pivot, int nslot, int MB, int b, int e0, Out* dst,
+                            bool pre = false) {
   using A = Ar<Acc>;
   constexpr int comps = CPLX ? 2 : 1;
   Acc vr[9], vi[9];
@@ -220,7 +221,8 @@ __device__ void matrix_item(const GatherParams& p, const St* s_Y, int rs, const 
   for (int x = pivot; x < nslot; ++x) {
     const Acc wx = wj[x];
     if (wx == (Acc)0) continue;
-    const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
+    // pre: the staged rows already carry their antiphase
+    const Acc er = pre ? (Acc)1 : s_e[2 * (x * MB + b)], ei = pre ? (Acc)0 : s_e[2 * (x * MB + b) + 1];
     const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
     const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
     for (int k = 0; k < 9; ++k) {
@@ -273,24 +275,35 @@ __device__ void matrix_item(const GatherParams& p, const St* s_Y, int rs, const 
   }
 }
 
-// Rotate (and for Γ permute and phase) one 3-vector of one q in place;
-// returns the destination element offset.
+// FP64 rotation (and Γ permutation and phase) of one interpolated 3-vector
+// with the q's matrix M (already transposed, inverted or scaled as the
+// rotation mode needs) and its code (bits 1-9: non-zero entries; 4 bits per
+// row from bit 10: a row that is a single ±1 entry).  GB300 issues FP64 at
+// 1/64 of the FP32 rate, so every skipped multiply counts: a signed
+// permutation (cubic operations, and the z row of hexagonal ones) costs no
+// arithmetic at all.  Returns the destination element offset.
 template <typename Acc, bool CPLX>
-__device__ __forceinline__ int rotate_vector(const GatherParams& p, bool gamma, const Acc* R, const Acc* ph, int k,
-                                             int r_inv, int e0, Acc* vr, Acc* vi) {
-  using A = Ar<Acc>;
-  const Acc* Ri = R + 9;
-  const Acc* M = (gamma || p.rot_mode == ROT_AXIAL) ? Ri : R;
-  const bool tr_ = p.rot_mode == ROT_RECIP;
+__device__ __forceinline__ int rotate_vector_f64(const GatherParams& p, bool gamma, const Acc* M, int code,
+                                                 const Acc* ph, int k, int r_inv, int e0, Acc* vr, Acc* vi) {
   Acc tr[3], ti[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
+    const int single = (code >> (10 + 4 * a)) & 15;
+    if (single) {
+      const int c = (single - 1) % 3;
+      const Acc sr = c == 0 ? vr[0] : (c == 1 ? vr[1] : vr[2]);
+      const Acc si = c == 0 ? vi[0] : (c == 1 ? vi[1] : vi[2]);
+      tr[a] = single > 3 ? -sr : sr;
+      ti[a] = single > 3 ? -si : si;
+      continue;
+    }
     Acc sr = 0, si = 0;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const Acc m = tr_ ? M[3 * c + a] : M[3 * a + c];
-      sr = A::add(sr, A::mul(m, vr[c]));
-      if (CPLX) si = A::add(si, A::mul(m, vi[c]));
+      if (!((code >> (1 + 3 * a + c)) & 1)) continue;
+      const Acc m = M[3 * a + c];
+      sr = fma(m, vr[c], sr);
+      if (CPLX) si = fma(m, vi[c], si);
     }
     tr[a] = sr;
     ti[a] = si;
@@ -301,14 +314,9 @@ __device__ __forceinline__ int rotate_vector(const GatherParams& p, bool gamma, 
     const Acc pr = ph[0], pi = ph[1];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-      vr[a] = A::sub(A::mul(pr, tr[a]), A::mul(pi, ti[a]));
-      vi[a] = A::add(A::mul(pr, ti[a]), A::mul(pi, tr[a]));
+      vr[a] = fma(pr, tr[a], -(pi * ti[a]));
+      vi[a] = fma(pr, ti[a], pi * tr[a]);
     }
-  } else if (p.rot_mode == ROT_AXIAL) {
-    const Acc dt = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
-                   R[2] * (R[3] * R[7] - R[4] * R[6]);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) { vr[a] = A::mul(dt, tr[a]); vi[a] = A::mul(dt, ti[a]); }
   } else {
 #pragma unroll
     for (int a = 0; a < 3; ++a) { vr[a] = tr[a]; vi[a] = ti[a]; }
@@ -682,23 +690,36 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       s_rot[2 * j] = r0;
       s_rot[2 * j + 1] = r1;
       s_id[j] = ident;
-      // the matrix applied to 3-vectors (FP32 path), and whether to apply it
-      if constexpr (kRegTile) {
+      // the matrix applied to 3-vectors, and whether to apply it: bit 0 set
+      // when it applies; for the FP64 path bits 1-9 mark its non-zero entries
+      // and 4 bits per row from bit 10 name a row that is a single ±1 entry
+      // (1 + column, + 3 when negative), which then costs no arithmetic
+      {
         const Acc* R = s_R + 18 * j;
         const Acc* Ri = R + 9;
         Acc scale = 1;
         if (p.rot_mode == ROT_AXIAL)
           scale = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) +
                   R[2] * (R[3] * R[7] - R[4] * R[6]);
-        for (int a = 0; a < 3; ++a)
+        const bool apply = p.rot_mode != ROT_NONE && (gamma || !ident);
+        int code = apply ? 1 : 0;
+        for (int a = 0; a < 3; ++a) {
+          int nz = 0, single = 0;
           for (int c = 0; c < 3; ++c) {
             Acc m;
             if (p.rot_mode == ROT_RECIP) m = R[3 * c + a];
             else if (gamma || p.rot_mode == ROT_AXIAL) m = scale * Ri[3 * a + c];
             else m = R[3 * a + c];
             s_M[12 * j + 3 * a + c] = m;
+            if (apply && m != (Acc)0) {
+              code |= 1 << (1 + 3 * a + c);
+              ++nz;
+              single = (m == (Acc)1) ? 1 + c : (m == (Acc)-1 ? 4 + c : 0);
+            }
           }
-        s_rotf[j] = (p.rot_mode != ROT_NONE && (gamma || !ident)) ? 1 : 0;
+          if (nz == 1) code |= single << (10 + 4 * a);
+        }
+        s_rotf[j] = code;
       }
     }
     __syncthreads();
@@ -773,6 +794,26 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
         s_e[2 * (x * MB + b) + 1] = ei;
       }
       __syncthreads();
+      // FP64: every staged row of a slot past the pivot is multiplied by its
+      // antiphase once here, so that the per-q sums below take one FMA per
+      // weight and component (the pivot's own factor is 1)
+      const bool pre = !kRegTile && CPLX && p.phase_allowed;
+      if constexpr (!kRegTile && CPLX) {
+        if (pre) {
+          St* Yw = s_Y0 + buf * ybuf;
+          const int rows = (ns - 1) * mb;
+          for (int it = tid; it < rows * s; it += nth) {
+            const int e = it % s, r = it / s;
+            const int b = r % mb, x = pivot + 1 + r / mb;
+            const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
+            St* y = Yw + (size_t)(x * MB + b) * rs + 2 * e;
+            const Acc dr = y[0], di = y[1];
+            y[0] = fma(er, dr, -(ei * di));
+            y[1] = fma(er, di, ei * dr);
+          }
+          __syncthreads();
+        }
+      }
       const int nitem = mb * G;
       if constexpr (kRegTile) {
         if (nslot == 4)
@@ -796,33 +837,29 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
           else { e0 = p.nsc + 3 * p.nvec + 9 * (gi - p.nsc - p.nvec); ne = 9; }
           if (ne == 9) {
             matrix_item<Acc, St, CPLX, Out>(p, s_Y, rs, s_e, wj, s_R + 18 * j, s_id[j], gamma, pivot, nslot, MB, b,
-                                            e0, dst);
+                                            e0, dst, pre);
             continue;
           }
+          // Σ_x w_x·(e_x·d_x) over the weighted vertices, one FMA per weight
+          // and component on the antiphased rows (without a phase, e_x = 1)
           Acc vr[3] = {0, 0, 0}, vi[3] = {0, 0, 0};
-          // the reference's order: out += (w·e^{-iθ})·d over the weighted vertices
           for (int x = pivot; x < nslot; ++x) {
             const Acc wx = wj[x];
             if (wx == (Acc)0) continue;
-            const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
-            const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
             const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
             for (int k = 0; k < ne; ++k) {
               Acc dr, di;
               ldY<Acc, St, CPLX>(y + k * comps, dr, di);
-              if (CPLX) {
-                vr[k] = A::add(vr[k], A::sub(A::mul(wr, dr), A::mul(wi, di)));
-                vi[k] = A::add(vi[k], A::add(A::mul(wr, di), A::mul(wi, dr)));
-              } else {
-                vr[k] = A::add(vr[k], A::mul(wx, dr));
-              }
+              vr[k] = fma(wx, dr, vr[k]);
+              if (CPLX) vi[k] = fma(wx, di, vi[k]);
             }
           }
           int de = e0;
-          if (ne == 3 && p.rot_mode != ROT_NONE && (gamma || !s_id[j])) {
+          const int rotf = s_rotf[j];
+          if (ne == 3 && rotf) {
             const int k = gi - p.nsc;
-            de = rotate_vector<Acc, CPLX>(p, gamma, s_R + 18 * j, s_ph + 2 * (j * na + k), k, s_rot[2 * j + 1], e0,
-                                          vr, vi);
+            de = rotate_vector_f64<Acc, CPLX>(p, gamma, s_M + 12 * j, rotf, s_ph + 2 * (j * na + k), k,
+                                              s_rot[2 * j + 1], e0, vr, vi);
           }
           store_group<Out, CPLX>(dst + (size_t)de * comps, vr, vi, ne);
         }
@@ -1785,12 +1822,10 @@ static void launch_t(const GatherParams& p, int num_sms, size_t budget, cudaStre
   if constexpr (sizeof(Acc) == 4)
     if (launch_warp<St, CPLX, Out>(p, num_sms, budget, s)) return;
   const size_t smem = layout_bytes<Acc, St, CPLX>(p, p.MB);
-  static bool configured = false;
-  if (!configured) {
-    cudaFuncSetAttribute(group_gather_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         200 * 1024);
-    configured = true;
-  }
+  // the limit belongs to the current device: set on every launch (a host
+  // call, no stream work)
+  cudaFuncSetAttribute(group_gather_kernel<Acc, St, CPLX, Out>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       200 * 1024);
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, group_gather_kernel<Acc, St, CPLX, Out>, kGatherThreads,
                                                 smem);
