@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -201,6 +202,12 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.n_perms = h->n_perms;
   p.perms = static_cast<const int32_t*>(h->perms.p);
   p.n_vertices = h->host_geom.n_vertices;
+  // the antiphase table holds the eigenvectors' factors (FP64 complex data)
+  if (phase && which == 1 && h->ph_valid && d.store == ST_F64 && d.cplx) {
+    p.n_ph_keys = h->n_ph_keys;
+    p.ph_keys = static_cast<const long long*>(h->ph_keys.p);
+    p.ph_table = static_cast<const double2*>(h->ph_table.p);
+  }
   p.ops = h->g.ops;
   p.rot_cart = h->g.rot_cart;
   p.n_ops = h->g.n_ops;
@@ -211,6 +218,7 @@ GatherParams gather_params(brx_handle* h, const Interp& d, const Scratch& s, lon
   p.qsplit = h->qsplit;
   p.err = h->err;
   p.variant = h->gather_variant;
+  p.stall = h->test_stall ? 1 : 0;
   return p;
 }
 
@@ -252,7 +260,7 @@ brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, b
     return fail(h, BRX_ERR_NULL_NODE, buf);
   }
   if (has(BRX_ERR_TIMEOUT))
-    return fail(h, BRX_ERR_TIMEOUT, "a bounded device-side wait ran out (learned residual); results are incomplete");
+    return fail(h, BRX_ERR_TIMEOUT, "a bounded device-side wait ran out; results are incomplete");
   if (has(BRX_ERR_NOT_FOUND)) {
     std::snprintf(buf, sizeof buf, "interpolate_at failed to find %d point%s", ew.count, ew.count > 1 ? "s." : ".");
     return fail(h, BRX_ERR_NOT_FOUND, buf);
@@ -292,10 +300,14 @@ void harvest_events(brx_handle* h) {
   h->ev_used = 0;
 }
 
+// The device error word is cleared on the device, in stream order: flags and
+// count to zero, first_bad to 0x7f7f7f7f7f7f7f7f (above any q index, so the
+// locate kernel's atomicMin keeps the smallest failing one).  No host memory
+// is written at call time.
 brx_status reset_errors(brx_handle* h, cudaStream_t s) {
-  ErrorWord z{0, 0, (long long)0x7fffffffffffffffLL};
-  *h->err_host = z;
-  BRX_CUDA(h, cudaMemcpyAsync(h->err, h->err_host, sizeof(ErrorWord), cudaMemcpyHostToDevice, s));
+  static_assert(sizeof(ErrorWord) == 16 && offsetof(ErrorWord, first_bad) == 8, "ErrorWord layout");
+  BRX_CUDA(h, cudaMemsetAsync(h->err, 0, 8, s));
+  BRX_CUDA(h, cudaMemsetAsync(reinterpret_cast<char*>(h->err) + 8, 0x7f, 8, s));
   return BRX_OK;
 }
 
@@ -315,6 +327,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   }
   const bool no_move = flags & BRX_FLAG_NO_MOVE;
   const bool f32 = flags & BRX_FLAG_OUT_F32;
+  h->test_stall = (flags & BRX_FLAG_TEST_TIMEOUT) != 0;
   int vmode = ROT_NONE, cmode = ROT_NONE;
   if (ir && !locate_only) {
     std::string msg;
@@ -821,6 +834,8 @@ void brx_destroy(brx_handle* h) {
   for (auto p : h->group_counts) cudaFreeHost(p);
   h->vals.data.release();
   h->vecs.data.release();
+  h->ph_keys.release();
+  h->ph_table.release();
   h->perm_keys.release();
   h->perm_ids.release();
   h->perms.release();
@@ -935,6 +950,7 @@ brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vecto
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "The values and vectors must have matching number of points and branches");
   BRX_CUDA(h, cudaSetDevice(h->device));
   h->filled = false;
+  h->ph_valid = false;
   h->mlp_on = false;  // a residual model belongs to the data it was trained on
   // bfloat16 storage applies to the eigenvectors; eigenvalues keep float32
   brx_status st = fill_one(h, values, h->vals, storage == BRX_STORE_BF16 ? BRX_STORE_F32 : storage);
@@ -946,7 +962,7 @@ brx_status brx_fill(brx_handle* h, const brx_data* values, const brx_data* vecto
   // new data invalidates any permutation table (DualInterpolator::replace_data)
   h->n_keys = 0;
   h->n_perms = 0;
-  return BRX_OK;
+  return build_phase_table(h);
 }
 
 brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* keys, const int32_t* perm_ids,
@@ -965,7 +981,8 @@ brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* ke
   BRX_CUDA(h, cudaSetDevice(h->device));
   h->n_keys = 0;
   h->n_perms = 0;
-  if (n_keys == 0) return BRX_OK;
+  h->ph_valid = false;
+  if (n_keys == 0) return build_phase_table(h);
   BRX_CUDA(h, h->perm_keys.ensure(sizeof(int64_t) * n_keys));
   BRX_CUDA(h, h->perm_ids.ensure(sizeof(int32_t) * n_keys));
   BRX_CUDA(h, h->perms.ensure(sizeof(int32_t) * (size_t)n_perms * B));
@@ -974,7 +991,7 @@ brx_status brx_set_permutations(brx_handle* h, int64_t n_keys, const int64_t* ke
   BRX_CUDA(h, cudaMemcpy(h->perms.p, perms, sizeof(int32_t) * (size_t)n_perms * B, cudaMemcpyHostToDevice));
   h->n_keys = n_keys;
   h->n_perms = n_perms;
-  return BRX_OK;
+  return build_phase_table(h);
 }
 
 brx_status brx_ir_interpolate_at(brx_handle* h, const double* Q, int64_t n, void* values_out, void* vectors_out,

@@ -349,7 +349,19 @@ struct GroupInfo {
   int nslot, pivot;
   int vid[8];
   int pid[8];
+  int kid[8];  // antiphase-table key of (pivot, slot) or -1 (FP64 complex data)
 };
+
+// index of key i·N + j in the antiphase table's sorted keys, or -1
+__device__ __forceinline__ int phase_key(const GatherParams& p, long long i, long long j) {
+  if (!p.ph_table || i == j) return -1;
+  long long key = i * p.n_vertices + j, lo = 0, hi = p.n_ph_keys;
+  while (lo < hi) {
+    long long mid = (lo + hi) >> 1;
+    if (__ldg(p.ph_keys + mid) < key) lo = mid + 1; else hi = mid;
+  }
+  return (lo < p.n_ph_keys && __ldg(p.ph_keys + lo) == key) ? (int)lo : -1;
+}
 
 // Warp 0 takes the next work descriptor and decodes its vertex slots.  In a
 // batch (gb.items set) it also finds the descriptor's interpolator and
@@ -399,6 +411,7 @@ __device__ __forceinline__ void fetch_group(const GatherBatch& gb, int n_groups,
   if (lane < 8) {
     gi->vid[lane] = vid;
     gi->pid[lane] = lane < nslot ? perm_lookup(p, pv, vid) : -1;
+    gi->kid[lane] = lane < nslot ? phase_key(p, pv, vid) : -1;
   }
   if (lane == 0) {
     gi->key = key;
@@ -773,7 +786,13 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       for (int it = tid; it < ns * mb; it += nth) {
         const int b = it % mb, x = pivot + it / mb;
         Acc er = 1, ei = 0;
-        if (CPLX && p.phase_allowed && x != pivot) {
+        const int kid = gc.kid[x];
+        if (CPLX && p.phase_allowed && x != pivot && kid >= 0) {
+          // formed once per vertex pair when the data were set
+          const double2 t = __ldg(p.ph_table + (long long)kid * B + b0 + b);
+          er = (Acc)t.x;
+          ei = (Acc)t.y;
+        } else if (CPLX && p.phase_allowed && x != pivot) {
           const St* a = s_Y + (size_t)(pivot * MB + b) * rs;
           const St* c = s_Y + (size_t)(x * MB + b) * rs;
           Acc rd = 0, id = 0;
@@ -988,7 +1007,7 @@ __device__ __forceinline__ void g_bulk(uint32_t dst, const void* src, uint32_t b
                "l"(src), "r"(bytes), "r"(m)
                : "memory");
 }
-__device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase) {
+__device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase, long long limit = kGatherSpin) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t done;
@@ -998,9 +1017,11 @@ __device__ __forceinline__ bool g_wait(uint32_t m, uint32_t phase) {
         : "r"(m), "r"(phase)
         : "memory");
     if (done) return true;
-    if (clock64() - t0 > kGatherSpin) return false;
+    if (clock64() - t0 > limit) return false;
   }
 }
+// BRX_FLAG_TEST_TIMEOUT: about a millisecond on a barrier nothing completes
+constexpr long long kStallCycles = 2000000LL;
 
 // One lane's (mode, element group) unit of the warp gather over its q.
 // Values travel as (re, im) pairs on the packed FP32 pipe: the NS corner
@@ -1233,8 +1254,10 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
   __shared__ GatherParams s_par[2];
   __shared__ GroupInfo s_g[2];
   __shared__ int s_abort;
+  __shared__ __align__(8) unsigned long long s_stall_bar;  // BRX_FLAG_TEST_TIMEOUT: never completed
   const int tid = threadIdx.x, nth = blockDim.x, warp = tid >> 5, lane = tid & 31, nwarps = nth >> 5;
   const bool batch = gb.items != nullptr;
+  bool stall = !batch && p.stall;
   if (!batch)
     for (int w = tid; w < (int)(sizeof(GatherParams) / sizeof(int)); w += nth) {
       reinterpret_cast<int*>(&s_par[0])[w] = reinterpret_cast<const int*>(&p)[w];
@@ -1259,7 +1282,10 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
     g_mbar_init(mbar);
     g_mbar_init(mbar + 8);
   }
-  if (tid == 0) s_abort = 0;
+  if (tid == 0) {
+    s_abort = 0;
+    g_mbar_init(smem_addr(&s_stall_bar));
+  }
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   __syncthreads();
   const int n_groups = *gb.n_groups;
@@ -1421,7 +1447,15 @@ __global__ void __launch_bounds__(kWarpGatherMaxWarps * 32, 2) warp_gather_kerne
     const int bstep = wq > 1 ? nblk : nwarps;
     for (int blk = bfirst; blk < nblk && ok; blk += bstep) {
       if (blk + bstep < nblk) issue(p, itm, gc, blk + bstep, buf ^ 1);
-      bool got = g_wait(mbar + 8 * buf, phase[buf]);
+      bool got;
+      if (stall) {
+        // test of the error path: the copies of this block stay pending and
+        // are drained at exit
+        got = g_wait(smem_addr(&s_stall_bar), 0, kStallCycles);
+        stall = false;
+      } else {
+        got = g_wait(mbar + 8 * buf, phase[buf]);
+      }
       got = __all_sync(0xffffffffu, got);
       if (!got) {
         ok = false;
@@ -1891,6 +1925,48 @@ cudaError_t preload_query_kernels() {
   if ((e = preload_store<float, __nv_bfloat16>()) != cudaSuccess) return e;
   if ((e = preload_grouping_kernels()) != cudaSuccess) return e;
   return preload_locate_kernel();
+}
+
+// Antiphase of every (key, mode) of FP64 complex data: key k = i·N + j
+// names the pivot vertex i and the vertex j; row b of i against row
+// perm_ij(b) of j, with the arithmetic and the order of the group gather's
+// own antiphase loop (so a factor read from the table equals the one the
+// loop forms), e = conj(z)/|z| with z = Σ_e conj(a_e)·c_e.
+__global__ void phase_table_kernel(GatherParams p, const long long* keys, long long n_keys, double2* out) {
+  using A = Ar<double>;
+  const double* data = static_cast<const double*>(p.data);
+  const int B = p.B, s = p.s;
+  const long long total = n_keys * (long long)B;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long k = t / B;
+    const int b = (int)(t - k * B);
+    const long long key = __ldg(keys + k);
+    const long long i = key / p.n_vertices, j = key - i * p.n_vertices;
+    const int pid = perm_lookup(p, i, j);
+    const int row = pid >= 0 ? __ldg(p.perms + (long long)pid * B + b) : b;
+    const double2* a = reinterpret_cast<const double2*>(data + (i * B + b) * (long long)s * 2);
+    const double2* c = reinterpret_cast<const double2*>(data + (j * B + row) * (long long)s * 2);
+    double rd = 0, id = 0;
+    for (int e = 0; e < s; ++e) {
+      const double2 x = __ldg(a + e), y = __ldg(c + e);
+      rd = A::add(rd, A::add(A::mul(x.x, y.x), A::mul(x.y, y.y)));
+      id = A::add(id, A::sub(A::mul(x.x, y.y), A::mul(x.y, y.x)));
+    }
+    const double mag = sqrt(A::add(A::mul(rd, rd), A::mul(id, id)));
+    double2 r = make_double2(1.0, 0.0);
+    if (mag > 0.0) r = make_double2(rd / mag, -(id / mag));
+    out[t] = r;
+  }
+}
+
+void launch_phase_table(const GatherParams& p, const long long* keys, long long n_keys, double2* out,
+                        cudaStream_t s) {
+  const long long total = n_keys * (long long)p.B;
+  if (total <= 0) return;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 152LL * 64) blocks = 152LL * 64;
+  phase_table_kernel<<<(unsigned)blocks, 256, 0, s>>>(p, keys, n_keys, out);
 }
 
 int launch_structure_factor(const GatherParams& p, int store_kind, int num_sms, size_t budget, cudaStream_t s) {

@@ -82,6 +82,11 @@ struct brx_handle {
   DevBuf perm_keys, perm_ids, perms;
   long long n_keys = 0;
   int n_perms = 0;
+  // antiphase table of FP64 complex eigenvectors (brx_phase.cu): keys of
+  // the vertex pairs that share a node, one factor per key and mode
+  DevBuf ph_keys, ph_table;
+  long long n_ph_keys = 0;
+  bool ph_valid = false;
   Scratch sc[2];
   long long scratch_q = 0;
   ErrorWord* err = nullptr;       // device
@@ -115,6 +120,7 @@ struct brx_handle {
   // the reciprocal basis rows, on the device
   int sf_n = 0;
   DevBuf sf_atoms, sf_B;
+  bool test_stall = false;  // this call carries BRX_FLAG_TEST_TIMEOUT
   bool async_pending = false;
   cudaStream_t async_stream = nullptr;
   int async_ir = 0;
@@ -134,6 +140,9 @@ size_t smem_budget(brx_handle* h, int which);
 size_t out_elem_bytes(const Interp& d, bool f32);
 brx_status collect_errors(brx_handle* h, int ir, const double* Q, long long n, bool q_host);
 brx_status reset_errors(brx_handle* h, cudaStream_t s);
+// (Re)builds the antiphase table after the vertex data or the permutation
+// table changed (no-op unless the eigenvectors are complex FP64 data).
+brx_status build_phase_table(brx_handle* h);
 // Adds the learned residual to the eigenvalues just gathered for a chunk;
 // returns the number of kernels launched (0 without a model).
 int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_out, bool out_f32, cudaStream_t cs);

@@ -55,6 +55,12 @@ struct GatherParams {
   int n_perms;
   const int32_t* perms;
   long long n_vertices;
+  // antiphase table of FP64 complex data (null: formed per group): one
+  // factor per mode for every sorted key i*n_vertices+j of an ordered pair
+  // of vertices sharing a node, against the pivot i
+  long long n_ph_keys;
+  const long long* ph_keys;
+  const double2* ph_table;
   // rotation tables
   const int32_t* ops;
   const double* rot_cart;
@@ -69,6 +75,7 @@ struct GatherParams {
   int qsplit;                // FP32 gather: about qsplit work units per thread and block (0: 2)
   ErrorWord* err;            // bounded waits that run out report here
   int variant;               // FP32 gather: 0 warp-independent kernel where it applies, 1 classic
+  int stall;                 // BRX_FLAG_TEST_TIMEOUT: the first bounded wait of each warp never completes
   // batches: records are indexed by batch-wide q, the output by q − q_base;
   // group keys are batch-wide, the trellis's own by key − key_base
   long long q_base;
@@ -161,6 +168,11 @@ int gather_max_ctas(int store_kind, bool cplx, bool out_f32, size_t smem);
 // it (FP64 data, matrices, unaligned data).
 bool gather_warp_plan(int store_kind, bool cplx, bool out_f32, const GatherParams* items, int n, int qmax,
                       size_t budget, GatherBatch* gb, size_t* smem, int* ctas_per_sm);
+
+// Antiphase table of FP64 complex data p.data (p.B, p.s, permutation table
+// and n_vertices as the gather reads them): out[k·B + b] for every key k.
+void launch_phase_table(const GatherParams& p, const long long* keys, long long n_keys, double2* out,
+                        cudaStream_t s);
 
 // Load every query kernel of this library on the current device (module
 // loading is otherwise deferred to the first launch).

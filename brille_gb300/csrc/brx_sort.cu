@@ -520,7 +520,10 @@ extern "C" brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* key
   cudaStream_t cs = stream ? static_cast<cudaStream_t>(stream) : h->sc[0].stream;
   h->n_keys = 0;
   h->n_perms = 0;
-  if (n_keys == 0) return BRX_OK;
+  // the antiphase table follows the permutations: until it is rebuilt the
+  // gather forms its factors per group
+  h->ph_valid = false;
+  if (n_keys == 0) return build_phase_table(h);
   // transient buffers of this call, released on every return
   struct Transient {
     DevBuf out, flag, status;
@@ -590,7 +593,7 @@ extern "C" brx_status brx_sort(brx_handle* h, int64_t n_keys, const int64_t* key
   BRX_CUDA(h, cudaStreamSynchronize(cs));
   h->n_keys = n_keys;
   h->n_perms = n_perm;
-  return BRX_OK;
+  return build_phase_table(h);
 }
 
 extern "C" brx_status brx_get_permutations(brx_handle* h, int64_t n_keys, int64_t* keys_out, int32_t* perms_out) {
