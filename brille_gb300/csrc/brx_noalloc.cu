@@ -1,32 +1,34 @@
 // brx_ir_interpolate_at_noalloc: ir_interpolate_at without any allocation.
 //
-// Who needs it: callers that may not allocate device memory while they run.
-// A query issued during CUDA stream capture cannot call cudaMalloc (it is not
-// a capturable operation and breaks the capture); a serving loop with a
-// latency budget cannot afford cudaMalloc's implicit device synchronisation;
-// and a host framework that hands all device memory to its own pool (the
-// caching allocators of PyTorch or JAX) may have nothing left for an outside
-// cudaMalloc.  The regular entry point grows its scratch on demand, so it can
-// allocate on any call; this one never does.
+// Who needs it: callers that must not allocate device memory while they run.
+// A serving loop with a per-request latency budget cannot take the implicit
+// device-wide synchronisation that cudaMalloc and cudaFree bring; a host
+// framework that hands all device memory to its own caching pool (PyTorch's
+// or JAX's allocator, say) may have nothing left for an outside cudaMalloc,
+// and a plugin inside such a host is often not allowed to allocate at all.
+// The regular entry point grows its scratch on demand, so any call may
+// allocate; this one never does.
 //
 // How: the per-q scratch of the pipeline (locate records, gather work
 // descriptors, work-queue counters) lives in one file-scope __device__ array
 // of fixed size, enough for BRX_NOALLOC_MAX_Q q per call (about 14 MB, held by
 // every GPU that loads this library until the process exits).  Host code
 // cannot use the array's name as a device address, so the first call on each
-// device looks the address up with cudaGetSymbolAddress (with that device
-// current) and also loads the kernels the call launches; that first call must
-// therefore come before any stream capture.  Later calls allocate nothing:
-// no cudaMalloc, cudaFree, pinned-host or library allocation.
+// device, with that device current, looks the address up with
+// cudaGetSymbolAddress and also loads every kernel the call launches; that
+// first call should come before any stream capture.  Later calls allocate
+// nothing: no cudaMalloc, cudaFree, pinned-host or library allocation.
 //
 // Every call shares the array and it keeps the last call's contents; the
-// counters that must start at zero are cleared at the start of each call.
-// Calls that overlap on the GPU (two streams, two handles on one device, or
-// two threads) race on the array: serialise them.
+// counters that must start at zero, and the handle's error word, are cleared
+// on the device at the start of each call.  Calls that overlap on the GPU
+// (two streams, two handles on one device, or two threads) race on the
+// array: serialise them.
 //
 // Semantics differ from brx_ir_interpolate_at in three ways: Q and the
-// outputs must be device memory, n is at most BRX_NOALLOC_MAX_Q, and q are
-// gathered one per work group instead of grouped by shared vertices.
+// outputs must be device memory on the handle's device, n is at most
+// BRX_NOALLOC_MAX_Q, and q are gathered one per work group instead of grouped
+// by shared vertices.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -50,25 +52,6 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 void* g_scratch[kMaxDevices] = {};
 
-// the array's device address on `device`, looked up once with that device
-// current; the kernels are loaded at the same time
-brx_status scratch_address(brx_handle* h, void** out) {
-  int device = 0;
-  BRX_CUDA(h, cudaGetDevice(&device));
-  if (device < 0 || device >= kMaxDevices) return fail(h, BRX_ERR_INVALID_ARGUMENT, "device index out of range");
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch[device]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, brx_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(brx_noalloc_scratch)");
-    e = brx::preload_query_kernels();
-    if (e != cudaSuccess) return cuda_fail(h, e, "loading the query kernels");
-    g_scratch[device] = p;
-  }
-  *out = g_scratch[device];
-  return BRX_OK;
-}
-
 __global__ void one_q_per_group_kernel(const int32_t* status, const int32_t* key, long long n, int32_t* order,
                                        brx::GroupDesc* groups, int32_t* n_groups) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
@@ -83,14 +66,39 @@ __global__ void one_q_per_group_kernel(const int32_t* status, const int32_t* key
   }
 }
 
-bool is_device_ptr(const void* p) {
+// the array's device address on `device`, looked up once with that device
+// current; the kernels are loaded at the same time
+brx_status scratch_address(brx_handle* h, void** out) {
+  int device = 0;
+  BRX_CUDA(h, cudaGetDevice(&device));
+  if (device < 0 || device >= kMaxDevices) return fail(h, BRX_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch[device]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, brx_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaGetSymbolAddress(brx_noalloc_scratch)");
+    e = brx::preload_query_kernels();
+    if (e != cudaSuccess) return cuda_fail(h, e, "loading the query kernels");
+    cudaFuncAttributes a;
+    e = cudaFuncGetAttributes(&a, one_q_per_group_kernel);
+    if (e != cudaSuccess) return cuda_fail(h, e, "loading one_q_per_group_kernel");
+    g_scratch[device] = p;
+  }
+  *out = g_scratch[device];
+  return BRX_OK;
+}
+
+// device (or managed) memory that the handle's device reaches directly;
+// device memory of another GPU is refused rather than read as peer memory
+bool is_device_ptr(const void* p, int device) {
   if (!p) return false;
   cudaPointerAttributes a{};
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == device;
 }
 
 }  // namespace
@@ -109,8 +117,10 @@ extern "C" brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double*
   brx_status st = scratch_address(h, &base);
   if (st) return st;
   if (n == 0) return BRX_OK;
-  if (!is_device_ptr(Q) || !is_device_ptr(values_out) || (h->vecs.present && !is_device_ptr(vectors_out)))
-    return fail(h, BRX_ERR_INVALID_ARGUMENT, "brx_ir_interpolate_at_noalloc needs device pointers for Q and outputs");
+  if (!is_device_ptr(Q, h->device) || !is_device_ptr(values_out, h->device) ||
+      (h->vecs.present && !is_device_ptr(vectors_out, h->device)))
+    return fail(h, BRX_ERR_INVALID_ARGUMENT,
+                "brx_ir_interpolate_at_noalloc needs Q and outputs in device memory of the handle's device");
   std::string msg;
   int vmode = brx::ROT_NONE, cmode = brx::ROT_NONE;
   st = rotation_mode(h->vals, &vmode, &msg);

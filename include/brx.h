@@ -65,6 +65,14 @@ enum { BRX_STORE_F64 = 0,  /* as given: float64 / complex128, FP64 arithmetic */
 #define BRX_FLAG_OUT_F32   0x2u  /* write float32 / complex64 outputs instead of the input dtype  */
 #define BRX_FLAG_ASYNC     0x4u  /* device I/O only: return without synchronising; errors are read
                                     later with brx_sync */
+/* Diagnostic, no counterpart in the reference: the first bounded device
+ * wait of every warp of the FP32/BF16 vectors gather, and of every slot of
+ * the tensor-core residual network, waits on a barrier that nothing
+ * completes, so it gives up after about a millisecond.  The kernels then
+ * take their error path (error flag, copies in flight drained, tensor
+ * memory released) and the call returns BRX_ERR_TIMEOUT.  For tests of that
+ * path only: the outputs of such a call are incomplete. */
+#define BRX_FLAG_TEST_TIMEOUT 0x100u
 
 /*
  * Everything the query path reads, flattened.  All arrays are row-major and
@@ -244,17 +252,18 @@ brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n,
 brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir,
                       uint32_t flags, const brx_locate_out* out, void* stream);
 
-/* ir_interpolate_at for callers that may not allocate device memory while
- * they run: work queued during CUDA stream capture (cudaMalloc cannot be
- * captured), serving loops that cannot take cudaMalloc's device-wide
- * synchronisation, and host frameworks whose own pool owns the device memory.
- * No counterpart in the reference.  All per-q scratch lives in one fixed
- * __device__ array of this library (about 14 MB on every device that loads
- * it, kept until exit), so a call allocates nothing.  Limits: Q and outputs
- * must be device pointers; n ≤ BRX_NOALLOC_MAX_Q (larger n is rejected with
- * BRX_ERR_INVALID_ARGUMENT).  The first call on a device looks up the array
- * and loads the kernels; make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race and must be serialised. */
+/* ir_interpolate_at for callers that must not allocate device memory while
+ * they run: serving loops that cannot take the device-wide synchronisation
+ * of cudaMalloc/cudaFree inside a request, and plugins of host frameworks
+ * whose own caching pool owns the device memory.  No counterpart in the
+ * reference.  All per-q scratch lives in one fixed __device__ array of this
+ * library (about 14 MB on every device that loads it, kept until exit), so a
+ * call allocates nothing.  Limits: Q and outputs must be device memory of the
+ * handle's device; n ≤ BRX_NOALLOC_MAX_Q (larger n is rejected with
+ * BRX_ERR_INVALID_ARGUMENT).  The first call on a device looks up the
+ * array's address and loads the kernels; make it before any stream capture.
+ * Calls share the array, which keeps the last call's contents: calls that
+ * overlap on the GPU race and must be serialised. */
 #define BRX_NOALLOC_MAX_Q 65536
 brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double* Q, int64_t n,
                                          void* values_out, void* vectors_out,
@@ -269,8 +278,9 @@ brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double* Q, int64_t
  *   0-2 position of q in its node cell; 3-10 the weights of the vertex
  *   slots; 11 tetrahedron flag; 12 + slot·B + mode the vertex eigenvalues;
  *   12 + 8B + mode the interpolated eigenvalues; 12 + 9B + 0..2 the
- *   position of q in the trellis's bounding box; zeros up to d_in;
- * eigenvalues divided by omega_scale.  d_in ≥ 15 + 9B, a multiple of 16,
+ *   position of q in the trellis's bounding box; 15 + 9B the distance of q
+ *   to Γ over the box's longest side; zeros up to d_in;
+ * eigenvalues divided by omega_scale.  d_in ≥ 16 + 9B, a multiple of 16,
  * ≤ 512; n_out a multiple of 8, ≤ 64, ≥ n_modes = B.  Parameters are one
  * FP32 vector: W0 (128×d_in, row-major [out][in]), b0, W1, b1, W2, b2,
  * W3 (n_out×128), b3.  Every pointer below except the host params of
