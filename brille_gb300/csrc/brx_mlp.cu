@@ -117,7 +117,9 @@ struct FeatureArgs {
 // (12 + slot·B + mode), interpolated eigenvalues Σ w·v in slot order
 // (12 + 8B + mode, also returned through base unscaled; the FP32 gather
 // forms the same sum, possibly with fused multiply-adds), position in the
-// trellis box (12 + 9B + 0..2).
+// trellis box (12 + 9B + 0..2), and the distance |q_ir| to Γ over the
+// longest side of that box (15 + 9B): acoustic branches rise as a cone
+// from Γ, where linear interpolation errs most.
 // The record's vertex ids and weights are read once, as vectors.
 template <typename VT, class Put>
 __device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs& a, long long i, Put put,
@@ -133,6 +135,7 @@ __device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs&
     x[d] = __fadd_rn(__fadd_rn(__fmul_rn((float)g.outer_B[d], q0), __fmul_rn((float)g.outer_B[3 + d], q1)),
                      __fmul_rn((float)g.outer_B[6 + d], q2));
   const int B = a.B;
+  float span = 0.f;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     const double* kn = g.knots[d];
@@ -140,7 +143,10 @@ __device__ __forceinline__ void feature_all(const DevGeom& g, const FeatureArgs&
     put(d, __fdiv_rn(__fsub_rn(x[d], lo), __fsub_rn(hi, lo)));
     const float lo0 = (float)kn[0], hi0 = (float)kn[g.n_knots[d] - 1];
     put(12 + 9 * B + d, __fdiv_rn(__fsub_rn(x[d], lo0), __fsub_rn(hi0, lo0)));
+    span = fmaxf(span, __fsub_rn(hi0, lo0));
   }
+  const float r2 = __fadd_rn(__fadd_rn(__fmul_rn(x[0], x[0]), __fmul_rn(x[1], x[1])), __fmul_rn(x[2], x[2]));
+  put(15 + 9 * B, __fdiv_rn(__fsqrt_rn(r2), span));
   const int nw = min(a.nw[i], 8);
   const int4 v0 = reinterpret_cast<const int4*>(a.vidx + 8 * i)[0];
   const int4 v1 = reinterpret_cast<const int4*>(a.vidx + 8 * i)[1];
@@ -759,12 +765,17 @@ __device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t phase) {
   return done != 0;
 }
 // bounded wait for the completion of phase `phase`
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, long long limit = kSpinCycles) {
   const long long t0 = clock64();
   while (!mbar_try(mbar, phase))
-    if (clock64() - t0 > kSpinCycles) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(mbar) : "memory");
+}
+// BRX_FLAG_TEST_TIMEOUT: about a millisecond on a barrier nothing completes
+constexpr long long kTcStallCycles = 2000000LL;
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
                "l"(src), "r"(bytes), "r"(mbar)
@@ -821,6 +832,7 @@ struct TcArgs {
   void* values_out;
   int out_f64;
   ErrorWord* err;
+  int stall;  // BRX_FLAG_TEST_TIMEOUT: each slot's first wait for its rows never completes
 };
 
 __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
@@ -833,11 +845,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
   for (int i = tid; i < 3 * kWidth + tc_out_pad(a.n_out); i += kTcThreads) sb[i] = a.bias[i];
   const uint32_t mbar_mma = smem_u32(sm + S.mbar_off) + 16 * slot;
   const uint32_t mbar_x = mbar_mma + 8;
+  // s_fail[slot]: the slot's issuer gave up waiting for its rows and
+  // released the slot's MMA barrier without issuing; s_stall: a barrier
+  // nothing completes (BRX_FLAG_TEST_TIMEOUT)
+  __shared__ int s_fail[kTcSlots];
+  __shared__ __align__(8) unsigned long long s_stall;
   if (tid == 0) {
     for (int s = 0; s < kTcSlots; ++s) {
       mbar_init(smem_u32(sm + S.mbar_off) + 16 * s, 1);
       mbar_init(smem_u32(sm + S.mbar_off) + 16 * s + 8, 1);
+      s_fail[s] = 0;
     }
+    mbar_init(smem_u32(&s_stall), 1);
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 0) {
@@ -859,7 +878,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
   const uint32_t tile_bytes = (uint32_t)kInferRows * a.d_in * 2;
   const bool issuer = st == 0;
   uint32_t ph_mma = 0, ph_x = 0;
-  bool x_pending = false;
+  bool x_pending = false, mma_pending = false, stall = a.stall != 0;
   long long tile = (long long)blockIdx.x * kTcSlots + slot;
   if (issuer && tile < n_tiles) {
     mbar_expect_tx(mbar_x, tile_bytes);
@@ -875,9 +894,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
       bool good = true;
       if (issuer) {
         if (l == 0) {
-          good = mbar_wait(mbar_x, ph_x);
-          ph_x ^= 1;
-          x_pending = !good;
+          if (stall) {
+            // test of the error path: the tile's rows stay in flight and
+            // are drained at exit
+            good = mbar_wait(smem_u32(&s_stall), 0, kTcStallCycles);
+            stall = false;
+          } else {
+            good = mbar_wait(mbar_x, ph_x);
+          }
+          if (good) {
+            ph_x ^= 1;
+            x_pending = false;
+          }
         }
         tc_fence_after();
         if (good) {
@@ -886,10 +914,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
           for (int k = 0; k < K / 16; ++k)
             tc_mma(tmem_d, tc_desc(a0 + 256 * k, 128, 16 * K), tc_desc(b0 + 256 * k, 128, 16 * K), idesc, k > 0);
           tc_commit(mbar_mma);
+        } else {
+          // nothing to compute: release the slot's threads waiting below
+          s_fail[slot] = 1;
+          mbar_arrive(mbar_mma);
         }
       }
-      good = mbar_wait(mbar_mma, ph_mma) && good;
-      ph_mma ^= 1;
+      const bool done = mbar_wait(mbar_mma, ph_mma);
+      if (done) ph_mma ^= 1;
+      else mma_pending = true;  // an MMA may still write tensor memory
+      good = done && !*reinterpret_cast<volatile int*>(&s_fail[slot]);
       tc_fence_after();
       if (l == 3 && issuer && good && tile + step < n_tiles) {
         // layer 3 has read the buffer: the next tile's rows go there now
@@ -939,7 +973,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_infer_tc_kernel(TcArgs a) {
     atomicOr(&a.err->flags, 1 << BRX_ERR_TIMEOUT);
     atomicAdd(&a.err->count, 1);
   }
-  if (issuer && x_pending) mbar_wait(mbar_x, ph_x);  // no copy may land after exit
+  // no copy may land and no MMA may write tensor memory after exit
+  if (issuer && x_pending) mbar_wait(mbar_x, ph_x);
+  if (issuer && mma_pending) mbar_wait(mbar_mma, ph_mma);
   __syncthreads();
   if (warp == 0) {
     tc_fence_after();
@@ -965,7 +1001,7 @@ bool mlp_dims_ok(const brx_mlp_dims* d) {
          d->n_out <= 64 && d->n_modes >= 1 && d->n_modes <= d->n_out && (d->flags & ~BRX_MLP_FP32) == 0;
 }
 
-int feature_cols(int B) { return 15 + 9 * B; }
+int feature_cols(int B) { return 16 + 9 * B; }
 
 brx::FeatureArgs feature_args(const brx_handle* h, const double* q_ir, const int32_t* node, const int32_t* nw,
                               const int32_t* vidx, const double* w, const int32_t* status, long long n, int d_in,
@@ -1185,6 +1221,7 @@ int launch_residual(brx_handle* h, const Scratch& s, long long n, void* values_o
       t.values_out = a.values_out;
       t.out_f64 = a.out_f64;
       t.err = h->err;
+      t.stall = h->test_stall ? 1 : 0;
       const long long grid = std::min<long long>((tiles + brx::kTcSlots - 1) / brx::kTcSlots, (long long)h->num_sms);
       brx::mlp_infer_tc_kernel<<<(unsigned)grid, brx::kTcThreads, brx::tc_smem(d_in, a.n_out).total, cs>>>(t);
     } else {
