@@ -44,7 +44,9 @@ def crystal_case(name, fraction=1 / 2000, always_triangulate=False):
     t = geometry_tables(bz, tr)
     model = W.bvk_for(lat, masses)
     qv = tr.vertices @ np.linalg.inv(lat.B)
-    w, v = model.modes(qv)
+    # large trellises: eigensolves over spawn-started worker processes
+    procs = min(16, os.cpu_count() or 1) if len(qv) > 20000 else 0
+    w, v = model.modes(qv, processes=procs)
     return dict(lat=lat, bz=bz, tr=tr, tables=t, model=model, w=w, v=v)
 
 
