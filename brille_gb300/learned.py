@@ -28,7 +28,7 @@ WIDTH = 128
 
 def feature_width(n_modes):
     """Smallest legal input width (a multiple of 16) for n_modes eigenvalues."""
-    return (15 + 9 * n_modes + 15) // 16 * 16
+    return (16 + 9 * n_modes + 15) // 16 * 16
 
 
 def _torch():

@@ -32,7 +32,7 @@ def bf16(x):
 
 def feature_width(n_modes):
     """Smallest legal d_in (a multiple of 16) for n_modes eigenvalues."""
-    need = 15 + 9 * n_modes
+    need = 16 + 9 * n_modes
     return (need + 15) // 16 * 16
 
 
@@ -166,11 +166,15 @@ def features(records, values, knots, outer_B, n_modes, d_in, omega_scale):
     vid = np.asarray(records["vertex"]).reshape(n, 8)
     w = np.asarray(records["weight"]).reshape(n, 8).astype(f32)
     kn = [np.asarray(k, np.float64).astype(f32) for k in knots]
+    span = max(kn[d][-1] - kn[d][0] for d in range(3))
     for i in np.nonzero(ok)[0]:
         for d in range(3):
             lo, hi = kn[d][sub[i, d]], kn[d][sub[i, d] + 1]
             X[i, d] = (x[i, d] - lo) / (hi - lo)
             X[i, 12 + 9 * B + d] = (x[i, d] - kn[d][0]) / (kn[d][-1] - kn[d][0])
+        # distance to Γ over the longest side of the trellis box
+        r2 = (x[i, 0] * x[i, 0] + x[i, 1] * x[i, 1]) + x[i, 2] * x[i, 2]
+        X[i, 15 + 9 * B] = np.sqrt(r2) / span
         X[i, 3:3 + nw[i]] = w[i, :nw[i]]
         X[i, 11] = 1.0 if node[i, 1] >= 0 else 0.0
         for b in range(B):

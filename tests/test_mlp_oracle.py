@@ -79,3 +79,8 @@ def test_feature_base_equals_oracle_interpolation():
     assert np.allclose(X[:, 12 + 8 * B:12 + 9 * B] * 50.0, base, rtol=1e-6)
     box = X[:, 12 + 9 * B:15 + 9 * B]
     assert np.all((box >= -1e-6) & (box <= 1 + 1e-6))
+    # distance to Γ: |q_ir| in Å⁻¹ over the longest side of the trellis box
+    kn = c["tables"]["knots"]
+    span = max(k[-1] - k[0] for k in kn)
+    r = np.linalg.norm(rec["q_ir"] @ np.asarray(c["tables"]["outer_B"]).reshape(3, 3), axis=1)
+    assert np.allclose(X[:, 15 + 9 * B], r / span, rtol=1e-5, atol=1e-7)
