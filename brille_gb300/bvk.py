@@ -150,6 +150,36 @@ class BvKModel:
         return np.sign(lam) * np.sqrt(np.abs(lam)) * HBAR_OMEGA_MEV
 
 
+def modes_each(items, on_item, processes=0, chunk=4096):
+    """modes() of many (model, q_rlu) items through one process pool, one
+    item at a time: on_item(i, w, v) receives each item's results before the
+    next item starts, so only one item's eigenvectors are held at once."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    from multiprocessing import shared_memory
+
+    if processes <= 1:
+        for i, (model, q) in enumerate(items):
+            on_item(i, *model.modes(q, chunk=chunk))
+        return
+    with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
+        for i, (model, q) in enumerate(items):
+            q = np.atleast_2d(np.asarray(q, float))
+            N, n = q.shape[0], model.n_atoms
+            shm_w = shared_memory.SharedMemory(create=True, size=max(1, N * 3 * n * 8))
+            shm_v = shared_memory.SharedMemory(create=True, size=max(1, N * 3 * n * n * 3 * 16))
+            try:
+                parts = [(a, min(N, a + chunk)) for a in range(0, N, chunk)]
+                for f in [ex.submit(_modes_worker, model, q[a:b], a, N, shm_w.name, shm_v.name) for a, b in parts]:
+                    f.result()
+                on_item(i, np.ndarray((N, 3 * n), float, buffer=shm_w.buf),
+                        np.ndarray((N, 3 * n, n, 3), complex, buffer=shm_v.buf))
+            finally:
+                for s_ in (shm_w, shm_v):
+                    s_.close()
+                    s_.unlink()
+
+
 def _run_pool(processes, fn, jobs):
     """Run fn(*job) for every job on a spawn-started process pool.  A worker
     that cannot start (e.g. a __main__ that spawn cannot re-import) raises

@@ -368,7 +368,13 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     }
   }
   const bool any_host = q_host || o_host;
-  const bool async = (flags & BRX_FLAG_ASYNC) && !any_host;
+  // BRX_FLAG_ASYNC with host I/O needs page-locked Q and outputs: their
+  // copies then run in stream order like everything else, and the caller
+  // reads the outputs after brx_sync (or an event behind the call)
+  const bool pinned_io =
+      (!q_host || mapped_ptr(const_cast<double*>(Q))) &&
+      (!o_host || locate_only || (mapped_ptr(vals_out) && (!h->vecs.present || mapped_ptr(vecs_out))));
+  const bool async = (flags & BRX_FLAG_ASYNC) && !locate_only && (!any_host || pinned_io);
 
   size_t out_q = 0;  // output bytes per q
   if (!locate_only) {
@@ -380,16 +386,34 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   // outputs, alternating between two streams and staging buffers
   const char* chunk_env = std::getenv("BRX_HOST_CHUNK_MB");
   const long long chunk_mb = chunk_env ? std::atoll(chunk_env) : 0;
-  const long long host_chunk = (chunk_mb > 0 && chunk_mb <= 16384 ? chunk_mb : 512) << 20;
+  const long long host_chunk = (chunk_mb > 0 && chunk_mb <= 65536 ? chunk_mb : 512) << 20;
   if (o_host && out_q) chunk = std::max<long long>(1024, std::min<long long>(chunk, host_chunk / (long long)out_q));
   if (chunk > n) chunk = n;
+  const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
+  const size_t crow = !h->vecs.present ? 0
+                      : sf ? (size_t)h->vecs.B * 4 : (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
+  // buffers that must grow are freed and allocated anew: queued work that
+  // may still use them finishes first
+  if (h->async_pending) {
+    bool grow = chunk > h->scratch_q;
+    for (int k = 0; k < 2; ++k) {
+      if (!locate_only && o_host && (h->sc[k].vbuf.bytes < vrow * (size_t)chunk + 16 ||
+                                     (crow && h->sc[k].cbuf.bytes < crow * (size_t)chunk + 16)))
+        grow = true;
+      if (q_host && h->sc[k].qbuf.bytes < 24 * (size_t)chunk + 16) grow = true;
+    }
+    if (grow) BRX_CUDA(h, cudaStreamSynchronize(h->async_stream));
+  }
   brx_status st = ensure_scratch(h, chunk);
   if (st) return st;
 
   cudaStream_t us = static_cast<cudaStream_t>(user_stream);
-  const int nstreams = (any_host && !us) ? 2 : 1;
+  // host I/O: chunks alternate between the handle's two streams (copies of
+  // one chunk overlap the kernels of the next), joined to the caller's
+  // stream at both ends
+  const int nstreams = any_host ? 2 : 1;
   cudaStream_t main_s = us ? us : h->sc[0].stream;
-  if (h->async_pending && (any_host || !(flags & BRX_FLAG_ASYNC) || main_s != h->async_stream))
+  if (h->async_pending && !async)
     return fail(h, BRX_ERR_INVALID_ARGUMENT, "asynchronous queries must be synchronised with brx_sync first");
   if (!h->async_pending) {
     // queued asynchronous queries on one stream share one error word until brx_sync
@@ -398,11 +422,9 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   }
   if (nstreams == 2) {
     BRX_CUDA(h, cudaEventRecord(h->sc[0].done, main_s));
-    BRX_CUDA(h, cudaStreamWaitEvent(h->sc[1].stream, h->sc[0].done, 0));
+    for (int k = 0; k < 2; ++k)
+      if (h->sc[k].stream != main_s) BRX_CUDA(h, cudaStreamWaitEvent(h->sc[k].stream, h->sc[0].done, 0));
   }
-  const size_t vrow = (size_t)h->vals.B * span(h->vals) * out_elem_bytes(h->vals, f32);
-  const size_t crow = !h->vecs.present ? 0
-                      : sf ? (size_t)h->vecs.B * 4 : (size_t)h->vecs.B * span(h->vecs) * out_elem_bytes(h->vecs, f32);
   if (!locate_only && o_host) {
     for (int k = 0; k < nstreams; ++k) {
       BRX_CUDA(h, h->sc[k].vbuf.ensure(vrow * (size_t)chunk + 16));
@@ -415,7 +437,9 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   long long ci = 0;
   for (long long base = 0; base < n; base += chunk, ++ci) {
     const long long m = std::min(chunk, n - base);
-    Scratch& s = h->sc[nstreams == 2 ? (ci & 1) : 0];
+    // host I/O: consecutive chunks, of this call and of the next, take turns
+    // on the two streams, so a queued call computes while this one copies
+    Scratch& s = h->sc[nstreams == 2 ? ((h->chunk_seq + ci) & 1) : 0];
     cudaStream_t cs = nstreams == 2 ? s.stream : main_s;
     const double* Qd = Q + 3 * base;
     if (q_host) {
@@ -495,21 +519,27 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     }
   }
   BRX_CUDA(h, cudaGetLastError());
+  if (nstreams == 2) h->chunk_seq += ci;
   if (nstreams == 2) {
-    BRX_CUDA(h, cudaEventRecord(h->sc[1].done, h->sc[1].stream));
-    BRX_CUDA(h, cudaStreamWaitEvent(main_s, h->sc[1].done, 0));
+    for (int k = 0; k < 2; ++k) {
+      if (h->sc[k].stream == main_s) continue;
+      BRX_CUDA(h, cudaEventRecord(h->sc[k].done, h->sc[k].stream));
+      BRX_CUDA(h, cudaStreamWaitEvent(main_s, h->sc[k].done, 0));
+    }
   }
   BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(ErrorWord), cudaMemcpyDeviceToHost, main_s));
   if (async) {
     h->async_pending = true;
     h->async_stream = main_s;
+    if (std::find(h->async_streams.begin(), h->async_streams.end(), main_s) == h->async_streams.end())
+      h->async_streams.push_back(main_s);
     h->async_ir = ir;
     h->async_Q = Q;
     h->async_n = n;
+    h->async_q_host = q_host;
     return BRX_OK;
   }
   BRX_CUDA(h, cudaStreamSynchronize(main_s));
-  if (nstreams == 2) BRX_CUDA(h, cudaStreamSynchronize(h->sc[1].stream));
   if (h->profile) harvest_events(h);
   return collect_errors(h, ir, Q, n, q_host);
 }
@@ -556,6 +586,17 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
     for (long long i = 0; i < (long long)G.n_atoms * G.n_ops; ++i)
       if (G.gamma_F0[i] < 0 || G.gamma_F0[i] >= G.n_atoms || G.gamma_vidx[i] < 0 || G.gamma_vidx[i] >= G.n_gamma_vectors)
         return BRX_ERR_INVALID_ARGUMENT;
+    // every operation permutes the atoms (GammaTable::F0 of the reference);
+    // the gathers rely on it
+    std::vector<char> seen((size_t)G.n_atoms);
+    for (int r = 0; r < G.n_ops; ++r) {
+      std::fill(seen.begin(), seen.end(), 0);
+      for (int k = 0; k < G.n_atoms; ++k) {
+        const int f = G.gamma_F0[(long long)k * G.n_ops + r];
+        if (seen[(size_t)f]) return BRX_ERR_INVALID_ARGUMENT;
+        seen[(size_t)f] = 1;
+      }
+    }
   }
 
   brx_handle* h = new (std::nothrow) brx_handle();
@@ -1044,11 +1085,13 @@ brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir, uin
 brx_status brx_sync(brx_handle* h, void* stream) {
   if (!h) return BRX_ERR_INVALID_ARGUMENT;
   if (!h->async_pending) return BRX_OK;
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : h->async_stream;
-  BRX_CUDA(h, cudaStreamSynchronize(s));
+  // every stream with queued calls: they share the handle's error word
+  if (stream) BRX_CUDA(h, cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  for (cudaStream_t s : h->async_streams) BRX_CUDA(h, cudaStreamSynchronize(s));
+  h->async_streams.clear();
   h->async_pending = false;
   if (h->profile) harvest_events(h);
-  return collect_errors(h, h->async_ir, h->async_Q, h->async_n, false);
+  return collect_errors(h, h->async_ir, h->async_Q, h->async_n, h->async_q_host);
 }
 
 const char* brx_last_error(const brx_handle* h) { return h ? h->message.c_str() : "null handle"; }

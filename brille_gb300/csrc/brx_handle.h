@@ -122,10 +122,13 @@ struct brx_handle {
   DevBuf sf_atoms, sf_B;
   bool test_stall = false;  // this call carries BRX_FLAG_TEST_TIMEOUT
   bool async_pending = false;
-  cudaStream_t async_stream = nullptr;
+  cudaStream_t async_stream = nullptr;           // stream of the last queued call
+  std::vector<cudaStream_t> async_streams;       // every stream with queued calls
+  long long chunk_seq = 0;  // host-I/O chunks so far: chunks alternate streams across calls too
   int async_ir = 0;
   const double* async_Q = nullptr;
   long long async_n = 0;
+  bool async_q_host = false;
 };
 
 namespace brx_detail {

@@ -182,6 +182,7 @@ extern "C" brx_status brx_ir_interpolate_at_noalloc(brx_handle* h, const double*
   if (flags & BRX_FLAG_ASYNC) {
     h->async_pending = true;
     h->async_stream = cs;
+    h->async_streams.assign(1, cs);
     h->async_ir = 1;
     h->async_Q = Q;
     h->async_n = n;

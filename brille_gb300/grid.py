@@ -558,7 +558,10 @@ class _Grid:
     def query_into(self, Q, n, values_out, vectors_out, *, ir=True, out_f32=False, no_move=False,
                    async_=False, stream=None):
         """Raw query on caller-owned buffers (numpy arrays, torch tensors or
-        integer addresses; host or device).  Returns nothing; raises on error."""
+        integer addresses; host or device).  Returns nothing; raises on error.
+        async_=True returns at once for device buffers and for page-locked
+        host buffers (outputs complete after sync() or an event recorded on
+        `stream` behind the call); pageable host buffers make it synchronous."""
         flags = ((_abi.BRX_FLAG_NO_MOVE if no_move else 0) | (_abi.BRX_FLAG_OUT_F32 if out_f32 else 0) |
                  (_abi.BRX_FLAG_ASYNC if async_ else 0))
         fn = load().brx_ir_interpolate_at if ir else load().brx_interpolate_at

@@ -63,8 +63,14 @@ enum { BRX_STORE_F64 = 0,  /* as given: float64 / complex128, FP64 arithmetic */
 /* Query flags (brx_ir_interpolate_at / brx_interpolate_at). */
 #define BRX_FLAG_NO_MOVE   0x1u  /* do_not_move_points: Q already irreducible / in the first zone */
 #define BRX_FLAG_OUT_F32   0x2u  /* write float32 / complex64 outputs instead of the input dtype  */
-#define BRX_FLAG_ASYNC     0x4u  /* device I/O only: return without synchronising; errors are read
-                                    later with brx_sync */
+#define BRX_FLAG_ASYNC     0x4u  /* return without synchronising; errors are read later with
+                                    brx_sync.  Q and outputs in device memory, or in page-locked
+                                    host memory (cudaHostAlloc / cudaHostRegister): then the
+                                    outputs are complete only after brx_sync or an event recorded
+                                    on the stream behind the call.  With pageable host memory the
+                                    call synchronises as without the flag.  Calls may be queued on
+                                    several streams; they share one error word until brx_sync,
+                                    which waits for all of them. */
 /* Diagnostic, no counterpart in the reference: the first bounded device
  * wait of every warp of the FP32/BF16 vectors gather, and of every slot of
  * the tensor-core residual network, waits on a barrier that nothing
@@ -380,7 +386,8 @@ brx_status brx_batch_set_config(brx_batch* b, const int32_t* cfg, int32_t n);
 int64_t brx_batch_launch_count(const brx_batch* b);
 const char* brx_batch_last_error(const brx_batch* b);
 
-/* Wait for work queued with BRX_FLAG_ASYNC and report its status. */
+/* Wait for work queued with BRX_FLAG_ASYNC (on `stream`, if given, and on
+ * every stream that queued calls used) and report its status. */
 brx_status brx_sync(brx_handle* h, void* stream);
 
 /* Message for the last non-OK status on this handle (never NULL). */

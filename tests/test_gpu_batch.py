@@ -2,16 +2,19 @@
 trellises, mode counts and ragged q counts in one launch per stage must give
 each grid what its own ir_interpolate_at gives (FP64 bit for bit; FP32 to
 rounding order), through a plain run, a captured graph replayed on new
-inputs, and after autotuning; failures name the item.
+inputs, and after autotuning; failures name the item.  Every item's FP64
+outputs are also held against the oracle on a sample of its q (eigenvalues
+bit-exact, eigenvectors within 1e-12).
 """
 import numpy as np
 import pytest
 
-from _cases import conditioned_modes, crystal_case
+from _cases import conditioned_modes, crystal_case, values_vectors
 from brille_gb300 import BZTrellisQdc
 from brille_gb300.batch import BatchQuery
 from brille_gb300.grid import BZTrellisQdd
 from brille_gb300._lib import BrxError
+from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -63,6 +66,15 @@ def _check(grids, Qs, vals, vecs, out_f32):
             assert np.array_equal(bv, v), i
             if c is not None:
                 assert np.array_equal(vecs[i].cpu().numpy(), c), i
+            # the item against the oracle on a sample of its q
+            case = _case(NAMES[i])
+            k = min(len(Q), 300)
+            ov, oc, rc, _ = Oracle(case["tables"]).interpolate_at(
+                Q[:k], *(values_vectors(case) if c is not None else values_vectors(case)[:1]))
+            assert rc == 0, i
+            assert np.array_equal(bv[:k].reshape(ov.shape), ov), i
+            if c is not None:
+                assert np.abs(vecs[i].cpu().numpy()[:k].reshape(oc.shape) - oc).max() < 1e-12, i
             continue
         assert np.allclose(bv, v, rtol=1e-5, atol=1e-5 * np.abs(v).max()), i
         if c is None:
