@@ -815,8 +815,11 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       __syncthreads();
       // FP64: every staged row of a slot past the pivot is multiplied by its
       // antiphase once here, so that the per-q sums below take one FMA per
-      // weight and component (the pivot's own factor is 1)
-      const bool pre = !kRegTile && CPLX && p.phase_allowed;
+      // weight and component (the pivot's own factor is 1).  A group of one
+      // q (small chunks of host-buffer queries) instead takes the complex
+      // weight w·e in its sum: 2 FMAs more per element, but no pass.
+      const bool phased = !kRegTile && CPLX && p.phase_allowed;
+      const bool pre = phased && count >= 2;
       if constexpr (!kRegTile && CPLX) {
         if (pre) {
           St* Yw = s_Y0 + buf * ybuf;
@@ -866,6 +869,16 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
             const Acc wx = wj[x];
             if (wx == (Acc)0) continue;
             const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
+            if (phased && !pre && x != pivot) {
+              const Acc wr = wx * s_e[2 * (x * MB + b)], wi = wx * s_e[2 * (x * MB + b) + 1];
+              for (int k = 0; k < ne; ++k) {
+                Acc dr, di;
+                ldY<Acc, St, CPLX>(y + k * comps, dr, di);
+                vr[k] = fma(wr, dr, fma(-wi, di, vr[k]));
+                vi[k] = fma(wr, di, fma(wi, dr, vi[k]));
+              }
+              continue;
+            }
             for (int k = 0; k < ne; ++k) {
               Acc dr, di;
               ldY<Acc, St, CPLX>(y + k * comps, dr, di);
