@@ -6,7 +6,7 @@ The reference's Γ-rotation test data (wrap/tests/test_5_gamma.npz, NaCl,
 stage of the query path.  This script copies the arrays the tests use into a
 fixture that travels with the repository.
 
-Usage: python tests/golden/make_golden.py [path/to/test_5_gamma.npz]
+Usage: python tests/golden/make_golden.py <path to the reference's wrap/tests/test_5_gamma.npz>
 """
 import os
 import sys
@@ -27,4 +27,6 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/wrap/tests/test_5_gamma.npz")
+    if len(sys.argv) != 2:
+        sys.exit(__doc__)
+    main(sys.argv[1])
