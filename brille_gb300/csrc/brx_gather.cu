@@ -219,9 +219,10 @@ __device__ void matrix_item(const GatherParams& p, const St* s_Y, int rs, const 
   Acc vr[9], vi[9];
   for (int k = 0; k < 9; ++k) { vr[k] = 0; vi[k] = 0; }
   for (int x = pivot; x < nslot; ++x) {
-    const Acc wx = wj[x];
+    // pre: the staged rows past the pivot already carry their antiphase, as
+    // differences from the pivot row, whose weight is then 1
+    const Acc wx = (pre && x == pivot) ? (Acc)1 : wj[x];
     if (wx == (Acc)0) continue;
-    // pre: the staged rows already carry their antiphase
     const Acc er = pre ? (Acc)1 : s_e[2 * (x * MB + b)], ei = pre ? (Acc)0 : s_e[2 * (x * MB + b) + 1];
     const Acc wr = A::mul(wx, er), wi = A::mul(wx, ei);
     const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
@@ -814,10 +815,12 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
       }
       __syncthreads();
       // FP64: every staged row of a slot past the pivot is multiplied by its
-      // antiphase once here, so that the per-q sums below take one FMA per
-      // weight and component (the pivot's own factor is 1).  A group of one
-      // q (small chunks of host-buffer queries) instead takes the complex
-      // weight w·e in its sum: 2 FMAs more per element, but no pass.
+      // antiphase once here and stored as its difference from the pivot row
+      // (whose factor is 1): the weights sum to 1, so a q's sum is
+      // y_pivot + Σ w_x (e_x y_x − y_pivot), one FMA per weight and
+      // component and none for the pivot.  A group of one q (small chunks
+      // of host-buffer queries) instead takes the complex weight w·e in its
+      // sum: 2 FMAs more per element, but no pass.
       const bool phased = !kRegTile && CPLX && p.phase_allowed;
       const bool pre = phased && count >= 2;
       if constexpr (!kRegTile && CPLX) {
@@ -829,9 +832,10 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
             const int b = r % mb, x = pivot + 1 + r / mb;
             const Acc er = s_e[2 * (x * MB + b)], ei = s_e[2 * (x * MB + b) + 1];
             St* y = Yw + (size_t)(x * MB + b) * rs + 2 * e;
+            const St* yp = Yw + (size_t)(pivot * MB + b) * rs + 2 * e;
             const Acc dr = y[0], di = y[1];
-            y[0] = fma(er, dr, -(ei * di));
-            y[1] = fma(er, di, ei * dr);
+            y[0] = fma(er, dr, -(ei * di)) - yp[0];
+            y[1] = fma(er, di, ei * dr) - yp[1];
           }
           __syncthreads();
         }
@@ -869,6 +873,10 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
             const Acc wx = wj[x];
             if (wx == (Acc)0) continue;
             const St* y = s_Y + (size_t)(x * MB + b) * rs + e0 * comps;
+            if (pre && x == pivot) {  // the differences' base: the pivot row itself
+              for (int k = 0; k < ne; ++k) ldY<Acc, St, CPLX>(y + k * comps, vr[k], vi[k]);
+              continue;
+            }
             if (phased && !pre && x != pivot) {
               const Acc wr = wx * s_e[2 * (x * MB + b)], wi = wx * s_e[2 * (x * MB + b) + 1];
               for (int k = 0; k < ne; ++k) {
