@@ -67,6 +67,17 @@ class SortCost(C.Structure):
     _fields_ = [("scalar_fn", C.c_int32), ("vector_fn", C.c_int32), ("weight", C.c_double * 3)]
 
 
+class TrellisIn(C.Structure):
+    _fields_ = [("n_vertices", C.c_int32), ("vertices", _dp), ("n_planes", C.c_int32), ("planes", _dp),
+                ("n_edges", C.c_int32), ("edges", _ip), ("n_knots", C.c_int32 * 3), ("knots", _dp * 3),
+                ("tol", C.c_double), ("always_triangulate", C.c_int32)]
+
+
+class TrellisCells(C.Structure):
+    _fields_ = [("n_nodes", C.c_int64), ("node_type", _ip), ("n_poly", C.c_int64), ("poly_node", _ip),
+                ("point_offset", _lp), ("points", _dp), ("tet_offset", _lp), ("tets", _ip)]
+
+
 class Atoms(C.Structure):
     _fields_ = [("n_atoms", C.c_int32), ("weight", C.POINTER(C.c_double)), ("position", C.POINTER(C.c_double))]
 

@@ -8,7 +8,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 
-from ._abi import Atoms, Data, Geometry, LocateOut, MlpDims, SortCost
+from ._abi import Atoms, Data, Geometry, LocateOut, MlpDims, SortCost, TrellisCells, TrellisIn
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libbrx.so")
@@ -58,6 +58,10 @@ def load(build_if_missing=True):
     lib.brx_ir_interpolate_at_noalloc.restype = C.c_int
     lib.brx_locate.argtypes = [h, C.c_void_p, C.c_int64, C.c_int32, C.c_uint32, C.POINTER(LocateOut), C.c_void_p]
     lib.brx_locate.restype = C.c_int
+    lib.brx_trellis_cells_build.argtypes = [C.POINTER(TrellisIn), C.c_int32, C.POINTER(TrellisCells)]
+    lib.brx_trellis_cells_build.restype = C.c_int
+    lib.brx_trellis_cells_free.argtypes = [C.POINTER(TrellisCells)]
+    lib.brx_trellis_cells_free.restype = None
     lib.brx_sync.argtypes = [h, C.c_void_p]
     lib.brx_sync.restype = C.c_int
     lib.brx_last_error.argtypes = [h]

@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libbrx.so")
 SOURCES = ["brx_api.cu", "brx_locate.cu", "brx_gather.cu", "brx_noalloc.cu", "brx_mlp.cu", "brx_batch.cu", "brx_sort.cu",
-           "brx_phase.cu"]
+           "brx_phase.cu", "brx_build.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr"]

@@ -96,14 +96,27 @@ def oriented_tets(points, tets):
 
 
 class TrellisBuild:
-    """Flat trellis tables (numpy) ready for the query-path C ABI."""
+    """Flat trellis tables (numpy) ready for the query-path C ABI.
 
-    def __init__(self, ir_vertices, ir_halfspaces, max_volume, always_triangulate=False):
+    backend "host" builds every node here (cut cells tetrahedralised by
+    Delaunay); "gpu" classifies the cells and splits the cut cells into
+    tetrahedra on the GPU (``brx_trellis_cells_build``) and only merges the
+    vertices here.  Both give the same knots, node types, vertices and cube
+    nodes; the cut cells' tetrahedra differ (a fan over the facets instead
+    of a Delaunay tetrahedralisation) and tile the same polytopes."""
+
+    def __init__(self, ir_vertices, ir_halfspaces, max_volume, always_triangulate=False, backend="host",
+                 device=0):
         verts = np.asarray(ir_vertices, float)
         hs = np.asarray(ir_halfspaces, float)
         scale = float(np.max(np.abs(verts)))
         tol = 1e-10 * max(scale, 1e-30)
         self.knots = make_knots(verts.min(axis=0), verts.max(axis=0), float(max_volume))
+        if backend == "gpu":
+            self._build_gpu(verts, hs, tol, always_triangulate, device)
+            return
+        if backend != "host":
+            raise ValueError(f"unknown trellis backend {backend!r}")
         kx, ky, kz = self.knots
         nx, ny, nz = len(kx) - 1, len(ky) - 1, len(kz) - 1
         A, b = hs[:, :3], hs[:, 3]
@@ -177,6 +190,99 @@ class TrellisBuild:
         self.node_type = node_type
         self.node_index = node_index
         self.poly_tet_offset = np.array(tet_off, dtype=np.int32)
+        self.tet_vertices = tets
+        self.tet_sphere = spheres
+        self.tet_volume = vols
+        self.shape = (nx, ny, nz)
+
+    def _build_gpu(self, verts, hs, tol, always_triangulate, device):
+        import ctypes as C
+
+        from . import _abi
+        from ._lib import load
+
+        kx, ky, kz = self.knots
+        nx, ny, nz = len(kx) - 1, len(ky) - 1, len(kz) - 1
+        A, b = hs[:, :3], hs[:, 3]
+        nrm = np.linalg.norm(A, axis=1)
+        planes = np.concatenate([A / nrm[:, None], (b / nrm)[:, None]], axis=1)
+        # no two planes alike (the kernel takes each plane as one facet)
+        keep = []
+        for i, pl in enumerate(planes):
+            if not any(np.allclose(pl, planes[k], rtol=0, atol=1e-12) for k in keep):
+                keep.append(i)
+        planes = np.ascontiguousarray(planes[keep])
+        edges = np.ascontiguousarray(_poly_edges(verts, hs, tol), np.int32)
+        verts_c = np.ascontiguousarray(verts)
+        knots = [np.ascontiguousarray(k, float) for k in self.knots]
+        dp = C.POINTER(C.c_double)
+        tin = _abi.TrellisIn()
+        tin.n_vertices = len(verts_c)
+        tin.vertices = verts_c.ctypes.data_as(dp)
+        tin.n_planes = len(planes)
+        tin.planes = planes.ctypes.data_as(dp)
+        tin.n_edges = len(edges)
+        tin.edges = edges.ctypes.data_as(C.POINTER(C.c_int32))
+        for d in range(3):
+            tin.n_knots[d] = len(knots[d])
+            tin.knots[d] = knots[d].ctypes.data_as(dp)
+        tin.tol = tol
+        tin.always_triangulate = 1 if always_triangulate else 0
+        cells = _abi.TrellisCells()
+        lib = load()
+        st = lib.brx_trellis_cells_build(C.byref(tin), int(device), C.byref(cells))
+        if st != 0:
+            raise RuntimeError(f"brx_trellis_cells_build failed: {_abi.STATUS_NAMES.get(st, st)}")
+        try:
+            n_nodes, n_poly = int(cells.n_nodes), int(cells.n_poly)
+            node_type = np.ctypeslib.as_array(cells.node_type, (n_nodes,)).copy()
+            poly_node = np.ctypeslib.as_array(cells.poly_node, (max(n_poly, 1),))[:n_poly].copy()
+            poff = np.ctypeslib.as_array(cells.point_offset, (n_poly + 1,)).copy()
+            toff = np.ctypeslib.as_array(cells.tet_offset, (n_poly + 1,)).copy()
+            cut_pts = np.ctypeslib.as_array(cells.points, (max(int(poff[-1]), 1) * 3,))[:3 * poff[-1]].copy()
+            local = np.ctypeslib.as_array(cells.tets, (max(int(toff[-1]), 1) * 4,))[:4 * toff[-1]].copy()
+        finally:
+            lib.brx_trellis_cells_free(C.byref(cells))
+        cut_pts = cut_pts.reshape(-1, 3)
+        local = local.reshape(-1, 4).astype(np.int64)
+        # cube nodes: knot points of their corners, first in the vertex list
+        lin_cube = np.nonzero(node_type == NODE_CUBE)[0]
+        ci, cj, ck = lin_cube % nx, (lin_cube // nx) % ny, lin_cube // (nx * ny)
+        g = ((ci[:, None] + CUBE_CORNERS[None, :, 0]) * (ny + 1) + (cj[:, None] + CUBE_CORNERS[None, :, 1])) * (nz + 1) \
+            + (ck[:, None] + CUBE_CORNERS[None, :, 2])
+        used = np.unique(g)
+        ga, gb, gc = used // ((ny + 1) * (nz + 1)), (used // (nz + 1)) % (ny + 1), used % (nz + 1)
+        grid_pts = np.stack([kx[ga], ky[gb], kz[gc]], axis=1)
+        all_pts = np.concatenate([grid_pts, cut_pts]).reshape(-1, 3)
+        uniq_map = self._merge(all_pts, tol)
+        keepv, inv = np.unique(uniq_map, return_inverse=True)
+        self.vertices = all_pts[keepv]
+        self.cube_vertices = inv[np.searchsorted(used, g)].astype(np.int32).reshape(-1, 8)
+        tet_cell = np.repeat(np.arange(n_poly), np.diff(toff))
+        gtets = inv[len(used) + poff[tet_cell][:, None] + local]
+        # corners of one cell merged into one vertex by the global merge
+        # (closer than tol to the same point of a neighbour) leave a flat
+        # tetrahedron: drop it, and a cell left without any
+        ok = np.ones(len(gtets), bool)
+        for a_, b_ in ((0, 1), (0, 2), (0, 3), (1, 2), (1, 3), (2, 3)):
+            ok &= gtets[:, a_] != gtets[:, b_]
+        if not ok.all():
+            gtets, tet_cell = gtets[ok], tet_cell[ok]
+            cnt = np.bincount(tet_cell, minlength=n_poly)
+            node_type[poly_node[cnt == 0]] = NODE_NULL
+            live = cnt > 0
+            renum = np.cumsum(live) - 1
+            tet_cell = renum[tet_cell]
+            poly_node = poly_node[live]
+            n_poly = len(poly_node)
+            toff = np.concatenate([[0], np.cumsum(cnt[live])])
+        tets, spheres, vols = oriented_tets(self.vertices, gtets)
+        node_index = np.full(n_nodes, -1, np.int32)
+        node_index[lin_cube] = np.arange(len(lin_cube), dtype=np.int32)
+        node_index[poly_node] = np.arange(n_poly, dtype=np.int32)
+        self.node_type = node_type.astype(np.int32)
+        self.node_index = node_index
+        self.poly_tet_offset = toff.astype(np.int32)
         self.tet_vertices = tets
         self.tet_sphere = spheres
         self.tet_volume = vols

@@ -258,6 +258,52 @@ brx_status brx_interpolate_at(brx_handle* h, const double* Q, int64_t n,
 brx_status brx_locate(brx_handle* h, const double* Q, int64_t n, int32_t ir,
                       uint32_t flags, const brx_locate_out* out, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Trellis construction on the GPU (reference: PolyTrellis::construct,
+ * src/trellis_poly_parallel.tpp:74-482, which classifies the knot grid's
+ * cells and tetrahedralises the cells the polyhedron's surface cuts with
+ * TetGen).  One thread per cell classifies it from its corners' signed
+ * distances to the polyhedron's planes: cube (every corner inside), null
+ * (every corner outside one plane) or cut.  One thread per cut cell gathers
+ * the corners of the cell ∩ polyhedron (cell corners inside, polyhedron
+ * vertices in the cell, cell edges through polyhedron planes, polyhedron
+ * edges through cell faces), merges them within tol, and splits the convex
+ * polytope into tetrahedra by a fan from its first corner over each facet
+ * it does not touch.  Cut cells that span no volume become null nodes.
+ * The caller merges the cut cells' corners with the knot points of the
+ * cube nodes into one vertex list.
+ */
+typedef struct brx_trellis_in {
+  int32_t n_vertices;
+  const double* vertices;     /* polyhedron vertices, n × 3 (Å⁻¹) */
+  int32_t n_planes;
+  const double* planes;       /* n × 4 (unit normal, offset): inside where n·x + d ≤ tol; no two alike */
+  int32_t n_edges;
+  const int32_t* edges;       /* n × 2 vertex indices of the polyhedron's edges */
+  int32_t n_knots[3];
+  const double* knots[3];     /* strictly increasing */
+  double tol;                 /* absolute distance tolerance */
+  int32_t always_triangulate; /* 1: no cube nodes */
+} brx_trellis_in;
+
+typedef struct brx_trellis_cells {
+  int64_t n_nodes;
+  int32_t* node_type;         /* BRX_NODE_* per node, linear index i + nx(j + ny k) */
+  int64_t n_poly;
+  int32_t* poly_node;         /* n_poly linear node indices of the POLY nodes, increasing */
+  int64_t* point_offset;      /* n_poly + 1 */
+  double* points;             /* point_offset[n_poly] × 3 corners of each cut polytope */
+  int64_t* tet_offset;        /* n_poly + 1 */
+  int32_t* tets;              /* tet_offset[n_poly] × 4, indices into the cell's own corners */
+} brx_trellis_cells;
+
+/* Fills *out with arrays this library allocates in host memory; release
+ * them with brx_trellis_cells_free.  BRX_ERR_UNSUPPORTED if a cut cell has
+ * more than 128 corners or 512 tetrahedra, or the polyhedron more than 64
+ * planes; BRX_ERR_IMPOSSIBLE if the write pass disagrees with the count pass. */
+brx_status brx_trellis_cells_build(const brx_trellis_in* in, int32_t device, brx_trellis_cells* out);
+void brx_trellis_cells_free(brx_trellis_cells* out);
+
 /* ir_interpolate_at for callers that must not allocate device memory while
  * they run: serving loops that cannot take the device-wide synchronisation
  * of cudaMalloc/cudaFree inside a request, and plugins of host frameworks
