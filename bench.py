@@ -77,7 +77,7 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def build_workload(name):
+def build_workload(name, gpu_build=True):
     from brille_gb300 import workloads as W
     from brille_gb300.bz import BrillouinZone
     from brille_gb300.trellis import TrellisBuild
@@ -87,14 +87,28 @@ def build_workload(name):
     bz = BrillouinZone(lat)
     t = time.time()
     tr = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * fraction)
+    build_s = dict(host=round(time.time() - t, 2))
     log(f"[setup] trellis {tr.summary()} in {time.time() - t:.1f}s")
+    # the same trellis built on the GPU (cut cells fanned into tetrahedra
+    # there): set-up time only, the query runs on the host-built tables
+    try:
+        if not gpu_build:
+            raise RuntimeError("not built in this run")
+        t = time.time()
+        trg = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * fraction, backend="gpu")
+        build_s["gpu"] = round(time.time() - t, 2)
+        build_s["gpu_same_vertices"] = len(trg.vertices) == len(tr.vertices)
+        log(f"[setup] trellis on the GPU {trg.summary()} in {build_s['gpu']:.1f}s")
+        del trg
+    except Exception as e:  # no GPU in this process: set-up timing only
+        build_s["gpu"] = f"unavailable: {e}"
     model = W.bvk_for(lat, masses)
     qv = tr.vertices @ np.linalg.inv(lat.B)
     t = time.time()
     procs = min(16, os.cpu_count() or 1)
     w, v = model.modes(qv, chunk=2048, processes=procs if len(qv) > 8192 else 0)
     log(f"[setup] BvK modes for {len(qv)} vertices in {time.time() - t:.1f}s ({procs} processes)")
-    return dict(name=name, lat=lat, bz=bz, tr=tr, model=model, w=w, v=v, q_range=qr)
+    return dict(name=name, lat=lat, bz=bz, tr=tr, model=model, w=w, v=v, q_range=qr, build_s=build_s)
 
 
 def bytes_per_q(B, n_atoms, out_f32):
@@ -192,7 +206,7 @@ def cpu_baseline(wl, target_s=12.0, threads=0):
 def run_reference(args, rank):
     if rank != 0:
         return
-    wl = build_workload(args.workload)
+    wl = build_workload(args.workload, gpu_build=False)
     vals = []
     import oracle.oracle as orc
     nthreads = orc.Oracle.max_threads()
@@ -345,13 +359,11 @@ def run_batch(args):
     from a captured CUDA graph.  All outputs of 5e7 q do not fit in HBM, so
     the q run in W waves of one graph replay each into reused output
     buffers."""
-    import multiprocessing as mp
-    from concurrent.futures import ProcessPoolExecutor
-
     import torch
 
     from brille_gb300 import BZTrellisQdc
     from brille_gb300.batch import BatchQuery
+    from brille_gb300.bvk import spawn_pool
     from brille_gb300.bz import BrillouinZone
 
     n_items = args.batch_items
@@ -359,7 +371,7 @@ def run_batch(args):
     vmin, vmax = 2e3, args.batch_vmax
     t0 = time.time()
     procs = min(16, os.cpu_count() or 1)
-    with ProcessPoolExecutor(max_workers=procs, mp_context=mp.get_context("spawn")) as ex:
+    with spawn_pool(procs) as ex:
         items = list(ex.map(_batch_item, range(n_items), [9000 + k for k in range(n_items)], [vmin] * n_items,
                             [vmax] * n_items))
     log(f"[batch] {n_items} trellises in {time.time() - t0:.1f}s")
@@ -382,6 +394,8 @@ def run_batch(args):
                torch.from_numpy(v).to(dev, torch.complex64), [0, 3 * nat, 0, 2, 1], storage="f32")
         g._fill["values"] = g._fill["vectors"] = None  # the device copy is the handle's
         grids[i], B[i], na[i], V[i] = g, 3 * nat, nat, len(tr.vertices)
+        if i % 16 == 15:
+            log(f"[batch] BvK data of {i + 1} items in {time.time() - t0:.1f}s")
 
     modes_each([(W.bvk_for(lat, masses), tr.vertices @ np.linalg.inv(lat.B)) for _, lat, masses, tr in items], fill,
                processes=procs)
@@ -421,16 +435,22 @@ def run_batch(args):
         bq.sync(sp)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = bq.launch_count()
+    # per wave: events around each replay, so that the host's set_io and
+    # synchronisation between replays (the bubble) is measured apart
+    wev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(waves)]
     with Clocks(0) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
         for w in range(waves):
             wave_io(w)
+            wev[w][0].record(stream)
             bq.launch(sp)
+            wev[w][1].record(stream)
             bq.sync(sp)  # the next set_io rewrites the pinned tables this replay reads
         ev1.record(stream)
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
+    replay_ms = [a.elapsed_time(b) for a, b in wev]
     launches = bq.launch_count() - l0
     # the same waves, one query per grid
     for i, g in enumerate(grids):
@@ -458,6 +478,8 @@ def run_batch(args):
                per_grid_queries=dict(value=done_q / (ms_single / 1e3), ms_total=ms_single,
                                      note="the same waves as one ir_interpolate_at call per grid, queued async"),
                speedup_vs_per_grid=ms_single / ms,
+               replay_ms=[round(x, 2) for x in replay_ms],
+               between_replays_ms=round(ms - sum(replay_ms), 2),
                config=dict(space_groups=list(BATCH_GROUPS), vertices=[int(min(V)), int(max(V)), int(np.median(V))],
                            modes=[int(min(B)), int(max(B))], atoms=[int(min(na)), int(max(na))],
                            q_per_item=[int(nq.min()), int(nq.max())], q_range=1.0, storage="f32",
@@ -1053,6 +1075,7 @@ def run_throughput(args):
             data="synthetic (seeded BvK model at trellis vertices, q uniform)",
             config=dict(workload=args.workload, path="plain fine trellis, ir_interpolate_at",
                         trellis_vertices=int(len(wl["tr"].vertices)), modes=int(B), atoms=int(na),
+                        trellis_build_s=wl["build_s"],
                         q_per_step=n, q_range=qr, storage=args.storage,
                         outputs="f32/c64" if out_f32 else "f64/c128",
                         chunk_q=main["chunk_q"], chunks_per_step=main["chunks"],

@@ -18,7 +18,9 @@ the Γ table).
 """
 from __future__ import annotations
 
+import contextlib
 import itertools
+import os
 
 import numpy as np
 
@@ -150,26 +152,53 @@ class BvKModel:
         return np.sign(lam) * np.sqrt(np.abs(lam)) * HBAR_OMEGA_MEV
 
 
+# BLAS thread counts the pool's workers start with: one each, since the
+# pool already has one worker per core (16 workers with 16 BLAS threads each
+# run the small batched eigensolves several times slower than 16 with one)
+_WORKER_THREAD_VARS = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+
+
+@contextlib.contextmanager
+def spawn_pool(processes):
+    """A spawn-started process pool whose workers run single-threaded BLAS
+    (safe in a process that has already initialised CUDA).  The variables
+    are set while the pool lives, because workers start on first use."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    saved = {k: os.environ.get(k) for k in _WORKER_THREAD_VARS}
+    os.environ.update({k: "1" for k in _WORKER_THREAD_VARS})
+    try:
+        with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
+            yield ex
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def modes_each(items, on_item, processes=0, chunk=4096):
     """modes() of many (model, q_rlu) items through one process pool, one
     item at a time: on_item(i, w, v) receives each item's results before the
     next item starts, so only one item's eigenvectors are held at once."""
-    import multiprocessing as mp
-    from concurrent.futures import ProcessPoolExecutor
     from multiprocessing import shared_memory
 
     if processes <= 1:
         for i, (model, q) in enumerate(items):
             on_item(i, *model.modes(q, chunk=chunk))
         return
-    with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
+    with spawn_pool(processes) as ex:
         for i, (model, q) in enumerate(items):
             q = np.atleast_2d(np.asarray(q, float))
             N, n = q.shape[0], model.n_atoms
             shm_w = shared_memory.SharedMemory(create=True, size=max(1, N * 3 * n * 8))
             shm_v = shared_memory.SharedMemory(create=True, size=max(1, N * 3 * n * n * 3 * 16))
             try:
-                parts = [(a, min(N, a + chunk)) for a in range(0, N, chunk)]
+                # at least two parts per worker where the item allows
+                step = max(64, min(chunk, -(-N // (2 * processes))))
+                parts = [(a, min(N, a + step)) for a in range(0, N, step)]
                 for f in [ex.submit(_modes_worker, model, q[a:b], a, N, shm_w.name, shm_v.name) for a, b in parts]:
                     f.result()
                 on_item(i, np.ndarray((N, 3 * n), float, buffer=shm_w.buf),
@@ -184,10 +213,7 @@ def _run_pool(processes, fn, jobs):
     """Run fn(*job) for every job on a spawn-started process pool.  A worker
     that cannot start (e.g. a __main__ that spawn cannot re-import) raises
     BrokenProcessPool here instead of being restarted forever."""
-    import multiprocessing as mp
-    from concurrent.futures import ProcessPoolExecutor
-
-    with ProcessPoolExecutor(max_workers=processes, mp_context=mp.get_context("spawn")) as ex:
+    with spawn_pool(processes) as ex:
         for f in [ex.submit(fn, *j) for j in jobs]:
             f.result()
 

@@ -438,14 +438,20 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
   for (long long base = 0; base < n; base += chunk, ++ci) {
     const long long m = std::min(chunk, n - base);
     // host I/O: consecutive chunks, of this call and of the next, take turns
-    // on the two streams, so a queued call computes while this one copies
-    Scratch& s = h->sc[nstreams == 2 ? ((h->chunk_seq + ci) & 1) : 0];
+    // on the two streams, so a queued call computes while this one copies.
+    // A chunk's kernels start after the previous chunk's kernels (on the
+    // other stream) have finished, not beside them: two chunks computing at
+    // once finish together, leave the host link idle meanwhile and then
+    // copy together, and the steps fall into compute-then-copy lock step.
+    const int slot = nstreams == 2 ? (int)((h->chunk_seq + ci) & 1) : 0;
+    Scratch& s = h->sc[slot];
     cudaStream_t cs = nstreams == 2 ? s.stream : main_s;
     const double* Qd = Q + 3 * base;
     if (q_host) {
       BRX_CUDA(h, cudaMemcpyAsync(s.qbuf.p, Q + 3 * base, 24 * (size_t)m, cudaMemcpyHostToDevice, cs));
       Qd = static_cast<const double*>(s.qbuf.p);
     }
+    if (nstreams == 2) BRX_CUDA(h, cudaStreamWaitEvent(cs, h->sc[slot ^ 1].computed, 0));
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     if (h->profile && !locate_only) {
       for (auto& e : ev) e = next_event(h);
@@ -456,6 +462,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     ++h->launches;
     if (ev[1]) cudaEventRecord(ev[1], cs);
     if (locate_only) {
+      if (nstreams == 2) BRX_CUDA(h, cudaEventRecord(s.computed, cs));
       auto cp = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
         if (!dst) return cudaSuccess;
         return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, cs);
@@ -510,6 +517,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       if (int32_t* slot = next_group_slot(h)) cudaMemcpyAsync(slot, s.n_groups, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
     }
     BRX_CUDA(h, cudaGetLastError());
+    if (nstreams == 2) BRX_CUDA(h, cudaEventRecord(s.computed, cs));
     if (o_host) {
       BRX_CUDA(h, cudaMemcpyAsync(static_cast<char*>(vals_out) + vrow * (size_t)base, vdst, vrow * (size_t)m,
                                   cudaMemcpyDeviceToHost, cs));
@@ -527,8 +535,10 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
       BRX_CUDA(h, cudaStreamWaitEvent(main_s, h->sc[k].done, 0));
     }
   }
-  BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(ErrorWord), cudaMemcpyDeviceToHost, main_s));
   if (async) {
+    // the error word is read once, by brx_sync: a small copy queued behind
+    // each call would wait in the copy engine behind the next call's output
+    // copies, so each call would finish only with the next one
     h->async_pending = true;
     h->async_stream = main_s;
     if (std::find(h->async_streams.begin(), h->async_streams.end(), main_s) == h->async_streams.end())
@@ -539,6 +549,7 @@ brx_status run_query(brx_handle* h, int ir, const double* Q, long long n, void* 
     h->async_q_host = q_host;
     return BRX_OK;
   }
+  BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(ErrorWord), cudaMemcpyDeviceToHost, main_s));
   BRX_CUDA(h, cudaStreamSynchronize(main_s));
   if (h->profile) harvest_events(h);
   return collect_errors(h, ir, Q, n, q_host);
@@ -849,6 +860,7 @@ brx_status brx_create(const brx_geometry* gin, int32_t device, brx_handle** out)
   for (auto& s : h->sc) {
     if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess) return bail(BRX_ERR_CUDA);
     if (cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess) return bail(BRX_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&s.computed, cudaEventDisableTiming) != cudaSuccess) return bail(BRX_ERR_CUDA);
   }
   if (cudaMalloc(&h->err, sizeof(ErrorWord)) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
   if (cudaHostAlloc(&h->err_host, sizeof(ErrorWord), cudaHostAllocDefault) != cudaSuccess) return bail(BRX_ERR_OUT_OF_MEMORY);
@@ -868,6 +880,7 @@ void brx_destroy(brx_handle* h) {
     s.vbuf.release();
     s.cbuf.release();
     if (s.done) cudaEventDestroy(s.done);
+    if (s.computed) cudaEventDestroy(s.computed);
     if (s.stream) cudaStreamDestroy(s.stream);
   }
   for (auto& b : h->tables) b.release();
@@ -1090,6 +1103,8 @@ brx_status brx_sync(brx_handle* h, void* stream) {
   for (cudaStream_t s : h->async_streams) BRX_CUDA(h, cudaStreamSynchronize(s));
   h->async_streams.clear();
   h->async_pending = false;
+  BRX_CUDA(h, cudaMemcpyAsync(h->err_host, h->err, sizeof(ErrorWord), cudaMemcpyDeviceToHost, h->sc[0].stream));
+  BRX_CUDA(h, cudaStreamSynchronize(h->sc[0].stream));
   if (h->profile) harvest_events(h);
   return collect_errors(h, h->async_ir, h->async_Q, h->async_n, h->async_q_host);
 }

@@ -57,6 +57,7 @@ struct Scratch {
   int32_t* counters = nullptr;  // one work-queue cursor per interpolator
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
+  cudaEvent_t computed = nullptr;  // after this slot's latest chunk's kernels, before its copies
 };
 
 }  // namespace brx_detail
