@@ -65,11 +65,16 @@ PROFILED_TRAFFIC = {
 # FP64 instructions (DFMA + DMUL + DADD, per thread) per q of the FP64 gather,
 # from ncu on a small case of the same trellis; the FP64 pipe issues
 # `lanes_per_sm_cycle` of them per SM and cycle
+# FP64 thread instructions (DFMA + DMUL + DADD) per q of the FP64 vectors
+# gather: a per-q part plus the once-per-group antiphase pass shared by the
+# group's q, fitted to two ncu captures on the 882-vertex P6_3/mmc trellis
+# (131072 q: 26.1 q per group, 6.572e9; 45000 q: 18.0 q per group, 2.293e9)
 PROFILED_FP64 = {
     ("hex16", "gather_vectors", "f64"): dict(
-        thread_ops_per_q=(6_066_665_984 + 749_573_120 + 231_063_552) / 131072, lanes_per_sm_cycle=2,
-        source="ncu on the 882-vertex P6_3/mmc trellis, 131072 q (26 q per group; the full workload's groups are "
-               "smaller, so its count per q is a little higher); pipe 85% busy over the launch"),
+        per_q=48_305.0, per_group=47_900.0, lanes_per_sm_cycle=2,
+        source="ncu on the 882-vertex P6_3/mmc trellis at 26.1 and 18.0 q per group "
+               "(50 140 and 50 960 FP64 instructions per q; pipe 87 % and 78 % busy over the launch), "
+               "fitted as per_q + per_group / (q per group)"),
 }
 
 
@@ -919,10 +924,12 @@ def run_throughput(args):
             # (ncu) over its measured time, against the pipe's issue rate
             sms = torch.cuda.get_device_properties(dev).multi_processor_count
             mhz = clk.summary().get("sm_mhz") or 2070.0
-            rate = fp["thread_ops_per_q"] * stage_q / (stage_ms[dom] / 1e3)
+            qpg = stage_q / max(stage_groups, 1)
+            ops_q = fp["per_q"] + fp["per_group"] / max(qpg, 1.0)
+            rate = ops_q * stage_q / (stage_ms[dom] / 1e3)
             pk = sms * fp["lanes_per_sm_cycle"] * mhz * 1e6
             roof["fp64_pipe"] = dict(achieved_ops_per_s=rate, peak_ops_per_s=pk, frac=round(rate / pk, 4),
-                                     ops_per_q=fp["thread_ops_per_q"], source=fp["source"])
+                                     ops_per_q=round(ops_q, 1), source=fp["source"])
         res = dict(value=world * n * steps / (ms / 1e3), ms_per_step=ms / steps, roofline=roof,
                    gpu_launches=int(launches), clocks=clk.summary(), chunk_q=m, chunks=len(chunks),
                    tuning=None if tuned is None else dict(
