@@ -33,7 +33,8 @@ def test_struct_layout_matches_header(tmp_path):
     """ctypes mirrors of brx_geometry / brx_data / brx_locate_out have the C
     sizes and field offsets."""
     fields = {"brx_geometry": _abi.Geometry, "brx_data": _abi.Data, "brx_locate_out": _abi.LocateOut,
-              "brx_mlp_dims": _abi.MlpDims, "brx_sort_cost": _abi.SortCost}
+              "brx_mlp_dims": _abi.MlpDims, "brx_sort_cost": _abi.SortCost, "brx_trellis_in": _abi.TrellisIn,
+              "brx_trellis_cells": _abi.TrellisCells}
     src = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(void){"]
     for cname, py in fields.items():
         src.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
@@ -95,3 +96,58 @@ int main(void) {{
     cpp.write_text(f'#include "{HEADER}"\nint main() {{ return brx_abi_version() == BRX_ABI_VERSION ? 0 : 1; }}\n')
     subprocess.run(["g++", "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-fsyntax-only", str(cpp)],
                    check=True)
+
+
+def _cube_polyhedron(n_planes=6):
+    """The unit cube [0,1]^3 as brx_trellis_in arrays (vertices, unit
+    outward planes n.x + d <= 0 inside, edges); extra planes repeat the
+    first face."""
+    v = np.array([[x, y, z] for x in (0, 1) for y in (0, 1) for z in (0, 1)], float)
+    planes = [[-1, 0, 0, 0], [1, 0, 0, -1], [0, -1, 0, 0], [0, 1, 0, -1], [0, 0, -1, 0], [0, 0, 1, -1]]
+    planes = np.array((planes * (n_planes // 6 + 1))[:n_planes], float)
+    edges = np.array([[i, j] for i in range(8) for j in range(i + 1, 8)
+                      if np.abs(v[i] - v[j]).sum() == 1], np.int32)
+    return v, planes, edges
+
+
+def _trellis_in(v, planes, edges, knots, tol=1e-12):
+    dp = C.POINTER(C.c_double)
+    t = _abi.TrellisIn()
+    t.n_vertices, t.vertices = len(v), v.ctypes.data_as(dp)
+    t.n_planes, t.planes = len(planes), planes.ctypes.data_as(dp)
+    t.n_edges, t.edges = len(edges), edges.ctypes.data_as(C.POINTER(C.c_int32))
+    for d in range(3):
+        t.n_knots[d], t.knots[d] = len(knots[d]), knots[d].ctypes.data_as(dp)
+    t.tol = tol
+    return t
+
+
+def test_trellis_build_rejects_bad_input_on_the_host():
+    """brx_trellis_cells_build checks its input before any CUDA call:
+    missing arrays, out-of-range edges, unsorted knots and a negative
+    tolerance are invalid arguments; more planes than the kernels hold is
+    unsupported; the output struct is cleared either way."""
+    lib = load()
+    v, planes, edges = _cube_polyhedron()
+    k = np.linspace(0, 1, 5)
+    knots = [k, k.copy(), k.copy()]
+    out = _abi.TrellisCells()
+    bad_edges = edges.copy()
+    bad_edges[0, 1] = 8
+    unsorted = [k, k[::-1].copy(), k.copy()]
+    cases = [
+        (_trellis_in(v, planes, bad_edges, knots), 1),
+        (_trellis_in(v, planes, edges, unsorted), 1),
+        (_trellis_in(v, planes, edges, knots, tol=-1.0), 1),
+        (_trellis_in(v, planes[:3], edges, knots), 1),
+    ]
+    many_v, many_p, many_e = _cube_polyhedron(65)
+    cases.append((_trellis_in(many_v, many_p, many_e, knots), 8))  # BRX_ERR_UNSUPPORTED
+    for tin, want in cases:
+        out.n_nodes = 7
+        assert lib.brx_trellis_cells_build(C.byref(tin), 0, C.byref(out)) == want
+        assert out.n_nodes == 0 and not out.node_type
+    assert lib.brx_trellis_cells_build(None, 0, C.byref(out)) == 1
+    lib.brx_trellis_cells_free(C.byref(out))
+    lib.brx_trellis_cells_free(None)
+
