@@ -463,17 +463,29 @@ def run_batch(args):
             g.query_into(Qall[i][:m[i]], m[i], vals[i], vecs[i], out_f32=True, stream=sp)
     torch.cuda.synchronize()
     ev2, ev3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # per item: events around its query in the first wave
+    iev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in grids]
     ev2.record(stream)
     for w in range(waves):
         for i, g in enumerate(grids):
             if m[i]:
+                if w == 0:
+                    iev[i][0].record(stream)
                 g.query_into(Qall[i][w * m[i]:(w + 1) * m[i]], m[i], vals[i], vecs[i], out_f32=True, async_=True,
                              stream=sp)
+                if w == 0:
+                    iev[i][1].record(stream)
     ev3.record(stream)
     for g in grids:
         g.sync(sp)
     torch.cuda.synchronize()
     ms_single = ev2.elapsed_time(ev3)
+    items_ms = [iev[i][0].elapsed_time(iev[i][1]) if m[i] else 0.0 for i in range(len(grids))]
+    order = np.argsort(items_ms)[::-1]
+    per_item = [dict(item=int(i), group=items[i][0], atoms=int(na[i]), modes=int(B[i]), vertices=int(V[i]),
+                     q=int(m[i]), ms=round(items_ms[i], 3),
+                     gbs=round(float(per_q[i]) * m[i] / max(items_ms[i], 1e-9) / 1e6, 1)) for i in order[:12]]
+    log(f"[batch] per item, first wave, slowest first: {per_item}")
     out_bytes = float((per_q * m).sum()) * waves
     peaks = measured_peaks()
     peak = float(peaks["hbm_gbs"]) if peaks else 6800.0
@@ -483,6 +495,7 @@ def run_batch(args):
                per_grid_queries=dict(value=done_q / (ms_single / 1e3), ms_total=ms_single,
                                      note="the same waves as one ir_interpolate_at call per grid, queued async"),
                speedup_vs_per_grid=ms_single / ms,
+               per_grid_first_wave_ms=round(float(sum(items_ms)), 2), slowest_items_first_wave=per_item,
                replay_ms=[round(x, 2) for x in replay_ms],
                between_replays_ms=round(ms - sum(replay_ms), 2),
                config=dict(space_groups=list(BATCH_GROUPS), vertices=[int(min(V)), int(max(V)), int(np.median(V))],
