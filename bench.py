@@ -867,9 +867,13 @@ def run_throughput(args):
         grid.fill(wl["w"], [1, 0, 0, 0, 3], wl["v"], [0, 3 * na, 0, 2, 1], storage=storage)
         _, bq_vals, bq_vecs = bytes_per_q(B, na, out_f32)
         free, _ = torch.cuda.mem_get_info(dev)
-        # one output buffer of m q within 60 % of the free memory (the rest:
-        # per-chunk records, grouping and tuning scratch)
-        m = int(min(n, max(1 << 16, 0.6 * (free - (4 << 30)) / (bq_vals + bq_vecs + 500))))
+        # one output buffer within 75 % of the free memory (the rest:
+        # per-chunk records, grouping and tuning scratch), as few chunks as
+        # that allows, of equal size: every chunk groups its q by node anew,
+        # so the per-group work grows with the number of chunks
+        cap = int(max(1 << 16, 0.75 * (free - (4 << 30)) / (bq_vals + bq_vecs + 500)))
+        nch = -(-n // cap)
+        m = -(-n // nch)
         chunks = [(a, min(n, a + m)) for a in range(0, n, m)]
         fdt = torch.float32 if out_f32 else torch.float64
         cdt = torch.complex64 if out_f32 else torch.complex128
