@@ -32,10 +32,10 @@ def _crystal(name):
     return CRYSTALS[name]() if name in CRYSTALS else W.random_crystal(name, 2, seed=3)
 
 
-def _both(name, frac):
+def _both(name, frac, always_triangulate=False):
     lat, _ = _crystal(name)
     bz = BrillouinZone(lat)
-    args = (bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * frac)
+    args = (bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume * frac, always_triangulate)
     return bz, TrellisBuild(*args), TrellisBuild(*args, backend="gpu")
 
 
@@ -98,3 +98,20 @@ def test_query_on_gpu_built_trellis_matches_oracle(name):
     assert rc == 0
     assert np.array_equal(gv, ov[:, :, 0])
     assert np.abs(gc.reshape(oc.shape) - oc).max() < 1e-12
+
+
+@pytest.mark.parametrize("name", ["diamond2", "hex16"])
+def test_gpu_build_always_triangulate(name):
+    """always_triangulate: every non-null cell is a poly node on both
+    builders, with the same per-node volumes and vertex set."""
+    bz, h, g = _both(name, 1 / 2000, always_triangulate=True)
+    assert not (h.node_type == NODE_CUBE).any() and not (g.node_type == NODE_CUBE).any()
+    assert np.array_equal(h.node_type == NODE_POLY, g.node_type == NODE_POLY)
+    kx, ky, kz = h.knots
+    cell = (kx[1] - kx[0]) * (ky[1] - ky[0]) * (kz[1] - kz[0])
+    assert np.abs(_node_volumes(h) - _node_volumes(g)).max() <= 1e-9 * cell
+    scale = float(np.max(np.abs(bz.ir_vertices_invA)))
+    dist, _ = cKDTree(h.vertices).query(g.vertices)
+    assert len(h.vertices) == len(g.vertices) and dist.max() <= 1e-9 * scale
+    assert np.all(orient_many(g.vertices[g.tet_vertices]) > 0)
+
