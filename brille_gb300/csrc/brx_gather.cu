@@ -913,8 +913,14 @@ __device__ __forceinline__ void gather_groups(const GatherParams* single, const 
   cp_async_wait_all();
 }
 
+// Blocks per SM the FP64 complex gather is compiled for: four 128-thread
+// blocks (16 warps) fit the register file at 128 registers a thread, and its
+// FP64 pipe waits less with more warps to pick from
+template <typename Acc, bool CPLX>
+constexpr int kGatherMinBlocks = (sizeof(Acc) == 8 && CPLX) ? 4 : 1;
+
 template <typename Acc, typename St, bool CPLX, typename Out>
-__global__ void __launch_bounds__(kGatherThreads) group_gather_kernel(GatherParams p) {
+__global__ void __launch_bounds__(kGatherThreads, kGatherMinBlocks<Acc, CPLX>) group_gather_kernel(GatherParams p) {
   GatherBatch gb{};
   gb.groups = p.groups;
   gb.n_groups = p.n_groups;
