@@ -24,7 +24,7 @@ from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("diamond2", 1 / 2000), ("diamond8", 1 / 5000), ("hex16", 1 / 2000), ("P-1", 1 / 2000),
+CASES = [("diamond2", 1 / 2000), ("diamond8", 1 / 2000), ("diamond8", 1 / 5000), ("hex16", 1 / 2000), ("P-1", 1 / 2000),
          ("R-3m", 1 / 2000), ("Im-3m", 1 / 2000), ("hex16", 1 / 20000)]
 
 
