@@ -230,14 +230,17 @@ class _Grid:
     VECTOR_COMPLEX = True
 
     def __init__(self, bz: BrillouinZone, node_volume_fraction=0.1, always_triangulate=False, approx_config=None, *,
-                 max_volume=None, trellis=None, device=0, float_tolerance=None, digit=None):
+                 max_volume=None, trellis=None, device=0, float_tolerance=None, digit=None,
+                 trellis_backend="host"):
         """(wrap/_trellis.hpp:36-38) The reference's ``node_volume_fraction``
         is handed to its PolyTrellis as the maximum node volume in Å⁻³
         (src/trellis_poly.hpp:148-160), and so it is here; ``max_volume`` is
         the same number under its own name and wins when given.  Tolerances:
         ``approx_config`` (an ApproxConfig), else the zone's, else the global
         configuration (brille_gb300.approx); ``float_tolerance`` / ``digit``
-        override them."""
+        override them.  ``trellis_backend="gpu"`` builds the trellis on the
+        grid's device (brx_trellis_cells_build: cells classified and cut
+        polytopes split into tetrahedra by kernels), "host" on the host."""
         from . import approx
 
         cfg = approx_config or getattr(bz, "approx_config", None) or approx.config
@@ -247,7 +250,8 @@ class _Grid:
             vol = float(node_volume_fraction if max_volume is None else max_volume)
             if not vol > 0:
                 raise ValueError("the maximum node volume must be positive")
-            trellis = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, vol, always_triangulate)
+            trellis = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, vol, always_triangulate,
+                                   backend=trellis_backend, device=device)
         self.bz = bz
         self.trellis = trellis
         self.tables = geometry_tables(bz, trellis, gamma=True, float_tolerance=float_tolerance, digit=digit)

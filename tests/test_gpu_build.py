@@ -115,3 +115,19 @@ def test_gpu_build_always_triangulate(name):
     assert len(h.vertices) == len(g.vertices) and dist.max() <= 1e-9 * scale
     assert np.all(orient_many(g.vertices[g.tet_vertices]) > 0)
 
+
+def test_grid_constructor_builds_on_the_gpu():
+    """BZTrellisQdc(..., trellis_backend="gpu") builds its trellis on the
+    device, like TrellisBuild(backend="gpu"), and answers queries."""
+    lat, masses = _crystal("diamond8")
+    bz = BrillouinZone(lat)
+    g = BZTrellisQdc(bz, bz.volume / 2000, trellis_backend="gpu")
+    ref = TrellisBuild(bz.ir_vertices_invA, bz.ir_halfspaces, bz.volume / 2000, backend="gpu")
+    assert g.trellis.summary() == ref.summary()
+    model = W.bvk_for(lat, masses)
+    w, v = model.modes(g.trellis.vertices @ np.linalg.inv(lat.B))
+    g.fill(w, [1, 0, 0, 0, 3], v, [0, 3 * v.shape[2], 0, 2, 1])
+    Q = np.random.default_rng(2).uniform(-1, 1, size=(500, 3))
+    vals, _ = g.ir_interpolate_at(Q)
+    assert np.isfinite(vals).all() and vals.shape == (500, w.shape[1])
+
