@@ -290,21 +290,20 @@ class TrellisBuild:
 
     @staticmethod
     def _merge(points, tol):
-        tree = cKDTree(points)
-        pairs = tree.query_pairs(r=tol, output_type="ndarray")
-        parent = np.arange(len(points))
+        """Index of each point's representative: the lowest index among the
+        points joined to it by chains of pairs closer than tol."""
+        from scipy.sparse import coo_matrix
+        from scipy.sparse.csgraph import connected_components
 
-        def find(a):
-            while parent[a] != a:
-                parent[a] = parent[parent[a]]
-                a = parent[a]
-            return a
-
-        for a, b in pairs:
-            ra, rb = find(a), find(b)
-            if ra != rb:
-                parent[max(ra, rb)] = min(ra, rb)
-        return np.array([find(a) for a in range(len(points))])
+        n = len(points)
+        pairs = cKDTree(points).query_pairs(r=tol, output_type="ndarray")
+        if len(pairs) == 0:
+            return np.arange(n)
+        graph = coo_matrix((np.ones(len(pairs), np.int8), (pairs[:, 0], pairs[:, 1])), shape=(n, n))
+        _, label = connected_components(graph, directed=False)
+        rep = np.full(label.max() + 1, n, np.int64)
+        np.minimum.at(rep, label, np.arange(n))
+        return rep[label]
 
     @staticmethod
     def _cut_cell(lo, hi, verts, pedges, An, bn, tol):
