@@ -62,13 +62,11 @@ PROFILED_TRAFFIC = {
                                              source="ncu, one full-size warp_gather_kernel launch (1e7 q)"),
 }
 
-# FP64 instructions (DFMA + DMUL + DADD, per thread) per q of the FP64 gather,
-# from ncu on a small case of the same trellis; the FP64 pipe issues
-# `lanes_per_sm_cycle` of them per SM and cycle
 # FP64 thread instructions (DFMA + DMUL + DADD) per q of the FP64 vectors
 # gather: a per-q part plus the once-per-group antiphase pass shared by the
 # group's q, fitted to two ncu captures on the 882-vertex P6_3/mmc trellis
-# (131072 q: 26.1 q per group, 6.572e9; 45000 q: 18.0 q per group, 2.293e9)
+# (131072 q: 26.1 q per group, 6.572e9; 45000 q: 18.0 q per group, 2.293e9);
+# the FP64 pipe issues `lanes_per_sm_cycle` of them per SM and cycle
 PROFILED_FP64 = {
     ("hex16", "gather_vectors", "f64"): dict(
         per_q=48_305.0, per_group=47_900.0, lanes_per_sm_cycle=2,
