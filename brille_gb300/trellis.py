@@ -205,6 +205,8 @@ class TrellisBuild:
         nx, ny, nz = len(kx) - 1, len(ky) - 1, len(kz) - 1
         A, b = hs[:, :3], hs[:, 3]
         nrm = np.linalg.norm(A, axis=1)
+        if not np.all(np.isfinite(hs)) or not np.all(nrm > 0):
+            raise ValueError("every half-space needs a finite, non-zero normal")
         planes = np.concatenate([A / nrm[:, None], (b / nrm)[:, None]], axis=1)
         # no two planes alike (the kernel takes each plane as one facet)
         keep = []
