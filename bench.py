@@ -765,6 +765,13 @@ def learned_curve(args, n_eval, steps, warmup, plain=LEARNED_PLAIN, coarse=LEARN
             finest = max(curve, key=lambda c: c["vertices"])
             r["matched_plain"] = None
             r["ratio_vs_finest_plain"] = r["q_per_s"] / finest["q_per_s"]
+        # the same at matched RMS error (secondary; the metric is max error)
+        okr = [c for c in curve if c["rms_meV"] <= r["rms_meV"]]
+        if okr:
+            mr = min(okr, key=lambda c: c["vertices"])
+            r["matched_plain_rms"] = dict(trellis=mr["trellis"], vertices=mr["vertices"], rms_meV=mr["rms_meV"],
+                                          q_per_s=mr["q_per_s"])
+            r["ratio_at_matched_rms_error"] = r["q_per_s"] / mr["q_per_s"]
         learned.append(r)
         if log_progress:
             log(f"[learned] learned {name}: max {r['max_meV']:.3g} rms {r['rms_meV']:.3g} meV, {r['q_per_s']:.3g} q/s")
@@ -1084,6 +1091,8 @@ def run_throughput(args):
         best = max(lc["learned"], key=lambda r: r.get("ratio_at_matched_max_error", r.get("ratio_vs_finest_plain", 0)))
         learned = dict(
             ratio_at_matched_max_error=best.get("ratio_at_matched_max_error"),
+            ratio_at_matched_rms_error=best.get("ratio_at_matched_rms_error"),
+            matched_plain_rms=best.get("matched_plain_rms"),
             learned=dict((k, best[k]) for k in ("trellis", "vertices", "max_meV", "rms_meV", "q_per_s")),
             matched_plain=best.get("matched_plain"),
             target=lc["target"], target_met=lc["target_met"],
