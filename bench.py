@@ -114,6 +114,13 @@ def build_workload(name, gpu_build=True):
     return dict(name=name, lat=lat, bz=bz, tr=tr, model=model, w=w, v=v, q_range=qr, build_s=build_s)
 
 
+def matched_plain(curve, rec, key):
+    """The coarsest plain trellis of `curve` whose error `key` is at or
+    below the record's, or None."""
+    ok = [c for c in curve if c[key] <= rec[key]]
+    return min(ok, key=lambda c: c["vertices"]) if ok else None
+
+
 def bytes_per_q(B, n_atoms, out_f32):
     s = 4 if out_f32 else 8
     vals = B * s
@@ -755,9 +762,8 @@ def learned_curve(args, n_eval, steps, warmup, plain=LEARNED_PLAIN, coarse=LEARN
                                      frac=round(ach / pk, 4), flops_per_q=flops_q, ms_per_step=round(mlp_ms, 3),
                                      peak_source="measured" if peaks else "fallback")
         # matched accuracy: the coarsest plain trellis at or below this max error
-        ok = [c for c in curve if c["max_meV"] <= r["max_meV"]]
-        if ok:
-            match = min(ok, key=lambda c: c["vertices"])
+        match = matched_plain(curve, r, "max_meV")
+        if match:
             r["matched_plain"] = dict(trellis=match["trellis"], vertices=match["vertices"], max_meV=match["max_meV"],
                                       q_per_s=match["q_per_s"])
             r["ratio_at_matched_max_error"] = r["q_per_s"] / match["q_per_s"]
@@ -766,9 +772,8 @@ def learned_curve(args, n_eval, steps, warmup, plain=LEARNED_PLAIN, coarse=LEARN
             r["matched_plain"] = None
             r["ratio_vs_finest_plain"] = r["q_per_s"] / finest["q_per_s"]
         # the same at matched RMS error (secondary; the metric is max error)
-        okr = [c for c in curve if c["rms_meV"] <= r["rms_meV"]]
-        if okr:
-            mr = min(okr, key=lambda c: c["vertices"])
+        mr = matched_plain(curve, r, "rms_meV")
+        if mr:
             r["matched_plain_rms"] = dict(trellis=mr["trellis"], vertices=mr["vertices"], rms_meV=mr["rms_meV"],
                                           q_per_s=mr["q_per_s"])
             r["ratio_at_matched_rms_error"] = r["q_per_s"] / mr["q_per_s"]
