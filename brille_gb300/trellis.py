@@ -245,8 +245,22 @@ class TrellisBuild:
             local = np.ctypeslib.as_array(cells.tets, (max(int(toff[-1]), 1) * 4,))[:4 * toff[-1]].copy()
         finally:
             lib.brx_trellis_cells_free(C.byref(cells))
-        cut_pts = cut_pts.reshape(-1, 3)
-        local = local.reshape(-1, 4).astype(np.int64)
+        self._assemble(node_type, poly_node, poff, toff, cut_pts.reshape(-1, 3), local.reshape(-1, 4), tol)
+
+    def _assemble(self, node_type, poly_node, poff, toff, cut_pts, local, tol):
+        """Trellis tables from per-cell results (brx_trellis_cells layout):
+        node types, the poly nodes' linear indices, and per poly node its
+        corner points (poff offsets into cut_pts) and tetrahedra as local
+        corner indices (toff offsets into local).  Cube nodes take the knot
+        points of their corners; all points are merged within tol."""
+        kx, ky, kz = self.knots
+        nx, ny, nz = len(kx) - 1, len(ky) - 1, len(kz) - 1
+        node_type = np.array(node_type, np.int32)
+        poly_node = np.asarray(poly_node, np.int64)
+        poff, toff = np.asarray(poff, np.int64), np.asarray(toff, np.int64)
+        n_nodes, n_poly = len(node_type), len(poly_node)
+        cut_pts = np.asarray(cut_pts, float).reshape(-1, 3)
+        local = np.asarray(local).reshape(-1, 4).astype(np.int64)
         # cube nodes: knot points of their corners, first in the vertex list
         lin_cube = np.nonzero(node_type == NODE_CUBE)[0]
         ci, cj, ck = lin_cube % nx, (lin_cube // nx) % ny, lin_cube // (nx * ny)
